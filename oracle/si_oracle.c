@@ -1,0 +1,336 @@
+/*
+ * si_oracle.c -- the ORACLE for the SuperIntervals batch overlap-query path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This file is a plain-C restatement of the
+ * reference algorithm (kcleal/superintervals, src/superintervals.hpp and
+ * src/c_superintervals.h).  It is used by the test-suite as the checker, and
+ * by bench.py as the timed CPU baseline ("port").  No product code path links,
+ * loads or calls it.
+ *
+ * Parity pin: this restatement is checked against fixtures produced by the
+ * reference itself (oracle/ref_shim.cpp compiled against the reference header,
+ * see tests/golden/make_golden.py) and against the known answers of the
+ * reference's own unit tests (test/tests.cpp).
+ *
+ * What is restated, with the reference line each part follows:
+ *   - add() sortedness flags ........ src/superintervals.hpp:95-105
+ *   - sort_intervals / sort_block ... src/superintervals.hpp:1396-1439
+ *       The reference sorts with std::sort (unstable).  This restatement uses
+ *       a STABLE merge sort on the same key (start asc, end desc).  Starts and
+ *       ends come out identical; the payload order can only differ inside runs
+ *       of exact (start, end) duplicates, where std::sort's order is an
+ *       artefact of libstdc++ introsort.
+ *   - build() branch pass ........... src/superintervals.hpp:112-130
+ *   - upper_bound ................... src/superintervals.hpp:501-516
+ *   - count (count_linear form) ..... src/superintervals.hpp:623-649, 651-825
+ *   - search_idxs (ascending head) .. src/superintervals.hpp:879-905
+ *   - search_values (descending) .... src/superintervals.hpp:551-579
+ *   - searchIdxs C API (descending) . src/c_superintervals.h:610-643
+ *   - has_overlaps .................. src/superintervals.hpp:865-871
+ *   - coverage ...................... src/superintervals.hpp:979-1006
+ *   - per-query batch loops ......... src/superintervals/intervalmap.pyx:363-494
+ *
+ * Index sentinel: the reference uses SIZE_MAX; this file uses -1 (int64).
+ */
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+#include <pthread.h>
+
+#define SIO_NONE ((int64_t)-1)
+
+/* order codes for the search family */
+#define SIO_ORDER_IDXS_CPP 0   /* C++ search_idxs: head run ascending, rest descending */
+#define SIO_ORDER_DESC 1       /* search_values / C searchIdxs: fully descending */
+
+typedef struct {
+    int64_t begin, end;   /* query range handled by one worker claim */
+} sio_range;
+
+/* ------------------------------------------------------------------------- */
+/* A tiny dynamic work queue over [0, n) for the multi-threaded batch loops.  */
+/* ------------------------------------------------------------------------- */
+typedef struct {
+    int64_t n;
+    int64_t chunk;
+    int64_t next;   /* accessed with __atomic builtins */
+} sio_queue;
+
+static int sio_claim(sio_queue* q, sio_range* r) {
+    int64_t b = __atomic_fetch_add(&q->next, q->chunk, __ATOMIC_RELAXED);
+    if (b >= q->n) return 0;
+    r->begin = b;
+    r->end = (b + q->chunk < q->n) ? b + q->chunk : q->n;
+    return 1;
+}
+
+typedef void (*sio_worker_fn)(void* ctx, int64_t begin, int64_t end);
+
+typedef struct {
+    sio_queue* q;
+    sio_worker_fn fn;
+    void* ctx;
+} sio_thread_arg;
+
+static void* sio_thread_main(void* p) {
+    sio_thread_arg* a = (sio_thread_arg*)p;
+    sio_range r;
+    while (sio_claim(a->q, &r)) a->fn(a->ctx, r.begin, r.end);
+    return NULL;
+}
+
+static void sio_parallel_for(int64_t n, int nthreads, sio_worker_fn fn, void* ctx) {
+    if (n <= 0) return;
+    if (nthreads <= 1) {
+        fn(ctx, 0, n);
+        return;
+    }
+    sio_queue q;
+    q.n = n;
+    q.chunk = 2048;
+    q.next = 0;
+    pthread_t* th = (pthread_t*)malloc(sizeof(pthread_t) * (size_t)nthreads);
+    sio_thread_arg arg = {&q, fn, ctx};
+    int started = 0;
+    for (int t = 0; t < nthreads; ++t) {
+        if (pthread_create(&th[t], NULL, sio_thread_main, &arg) == 0) ++started;
+        else break;
+    }
+    if (started == 0) fn(ctx, 0, n);
+    for (int t = 0; t < started; ++t) pthread_join(th[t], NULL);
+    free(th);
+}
+
+/* ------------------------------------------------------------------------- */
+/* Type-generic body, instantiated for int32 and int64 coordinates.          */
+/* ------------------------------------------------------------------------- */
+#define SIO_DEFINE(SFX, S)                                                              \
+                                                                                        \
+/* Key order of sort_intervals (hpp:1418): start ascending, then end descending.   */   \
+static int sio_less_##SFX(const S* s, const S* e, int64_t a, int64_t b) {               \
+    if (s[a] != s[b]) return s[a] < s[b];                                               \
+    return e[a] > e[b];                                                                 \
+}                                                                                       \
+                                                                                        \
+static void sio_msort_##SFX(const S* s, const S* e, int64_t* idx, int64_t* tmp,         \
+                            int64_t n) {                                                \
+    /* bottom-up stable merge sort of idx by (start asc, end desc) */                   \
+    for (int64_t w = 1; w < n; w *= 2) {                                                \
+        for (int64_t lo = 0; lo < n; lo += 2 * w) {                                     \
+            int64_t mid = lo + w < n ? lo + w : n;                                      \
+            int64_t hi = lo + 2 * w < n ? lo + 2 * w : n;                               \
+            int64_t i = lo, j = mid, k = lo;                                            \
+            while (i < mid && j < hi) {                                                 \
+                /* take from the right only if strictly less: keeps stability */        \
+                if (sio_less_##SFX(s, e, idx[j], idx[i])) tmp[k++] = idx[j++];          \
+                else tmp[k++] = idx[i++];                                               \
+            }                                                                           \
+            while (i < mid) tmp[k++] = idx[i++];                                        \
+            while (j < hi) tmp[k++] = idx[j++];                                         \
+        }                                                                               \
+        memcpy(idx, tmp, sizeof(int64_t) * (size_t)n);                                  \
+    }                                                                                   \
+}                                                                                       \
+                                                                                        \
+/* Sort + branch build for one map.  Follows build() (hpp:112-130) and           */     \
+/* sort_intervals (hpp:1415-1439) with the stable-sort substitution noted above.  */    \
+/* perm (optional) receives the input position of each sorted slot.              */     \
+/* Returns 1 when the input was already in canonical order (no sort performed).  */     \
+int sio_build_##SFX(int64_t n, const S* s_in, const S* e_in, const int32_t* d_in,      \
+                    S* s_out, S* e_out, int32_t* d_out, int64_t* perm,                 \
+                    int64_t* branch) {                                                  \
+    if (n <= 0) return 1;                                                               \
+    /* replay of add()'s flag maintenance (hpp:95-105) */                               \
+    int start_sorted = 1, end_sorted = 1;                                               \
+    for (int64_t i = 1; i < n && start_sorted; ++i) {                                   \
+        start_sorted = (s_in[i] < s_in[i - 1]) ? 0 : 1;                                 \
+        if (start_sorted && s_in[i] == s_in[i - 1] && e_in[i] > e_in[i - 1])            \
+            end_sorted = 0;                                                             \
+    }                                                                                   \
+    int64_t* idx = (int64_t*)malloc(sizeof(int64_t) * (size_t)n);                       \
+    for (int64_t i = 0; i < n; ++i) idx[i] = i;                                         \
+    int sorted = start_sorted && end_sorted;                                            \
+    if (!sorted) {                                                                      \
+        int64_t* tmp = (int64_t*)malloc(sizeof(int64_t) * (size_t)n);                   \
+        sio_msort_##SFX(s_in, e_in, idx, tmp, n);                                       \
+        free(tmp);                                                                      \
+    }                                                                                   \
+    for (int64_t i = 0; i < n; ++i) {                                                   \
+        s_out[i] = s_in[idx[i]];                                                        \
+        e_out[i] = e_in[idx[i]];                                                        \
+        if (d_in && d_out) d_out[i] = d_in[idx[i]];                                     \
+        if (perm) perm[i] = idx[i];                                                     \
+    }                                                                                   \
+    free(idx);                                                                          \
+    /* monotonic stack: branch[i] = nearest j < i with ends[j] >= ends[i] */            \
+    if (branch) {                                                                       \
+        int64_t* st = (int64_t*)malloc(sizeof(int64_t) * (size_t)n);                    \
+        int64_t top = 0;                                                                \
+        branch[0] = SIO_NONE;                                                           \
+        st[top++] = 0;                                                                  \
+        for (int64_t i = 1; i < n; ++i) {                                               \
+            while (top > 0 && e_out[st[top - 1]] < e_out[i]) --top;                     \
+            branch[i] = top > 0 ? st[top - 1] : SIO_NONE;                               \
+            st[top++] = i;                                                              \
+        }                                                                               \
+        free(st);                                                                       \
+    }                                                                                   \
+    return sorted;                                                                      \
+}                                                                                       \
+                                                                                        \
+/* upper_bound (hpp:501-516): last k with starts[k] <= v, else -1.               */     \
+int64_t sio_upper_bound_##SFX(int64_t n, const S* starts, S v) {                        \
+    if (n <= 0) return SIO_NONE;                                                        \
+    int64_t length = n, idx = 0;                                                        \
+    while (length > 1) {                                                                \
+        int64_t half = length / 2;                                                      \
+        idx += (starts[idx + half] <= v) * (length - half);                             \
+        length = half;                                                                  \
+    }                                                                                   \
+    if (starts[idx] > v) --idx;                                                         \
+    return idx;                                                                         \
+}                                                                                       \
+                                                                                        \
+/* count (hpp:623-649): size of { k <= ub(qe) : ends[k] >= qs }.                 */     \
+int64_t sio_count_##SFX(int64_t n, const S* starts, const S* ends,                      \
+                        const int64_t* branch, S qs, S qe) {                            \
+    int64_t i = sio_upper_bound_##SFX(n, starts, qe);                                   \
+    if (i == SIO_NONE) return 0;                                                        \
+    int64_t top = i;                                                                    \
+    while (i != SIO_NONE && qs <= ends[i]) --i;                                         \
+    int64_t c = top - i;                                                                \
+    if (i == SIO_NONE) return c;                                                        \
+    i = branch[i];                                                                      \
+    while (i != SIO_NONE) {                                                             \
+        if (qs <= ends[i]) { ++c; --i; }                                                \
+        else i = branch[i];                                                             \
+    }                                                                                   \
+    return c;                                                                           \
+}                                                                                       \
+                                                                                        \
+/* has_overlaps (hpp:865-871) */                                                        \
+int sio_has_overlaps_##SFX(int64_t n, const S* starts, const S* ends, S qs, S qe) {     \
+    int64_t i = sio_upper_bound_##SFX(n, starts, qe);                                   \
+    return i != SIO_NONE && qs <= ends[i];                                              \
+}                                                                                       \
+                                                                                        \
+/* search_idxs (hpp:879-905, order 0) / search_values + C searchIdxs             */     \
+/* (hpp:551-579, c:610-643, order 1).  Writes positions (or data[pos] when       */     \
+/* data != NULL) to out and returns how many were written.                       */     \
+int64_t sio_search_##SFX(int64_t n, const S* starts, const S* ends,                     \
+                         const int64_t* branch, const int32_t* data, S qs, S qe,        \
+                         int order, int64_t* out) {                                     \
+    int64_t idx = sio_upper_bound_##SFX(n, starts, qe);                                 \
+    if (idx == SIO_NONE) return 0;                                                      \
+    int64_t i = idx, w = 0;                                                             \
+    while (i != SIO_NONE && qs <= ends[i]) --i;                                         \
+    /* head run i+1 .. idx */                                                           \
+    if (order == SIO_ORDER_IDXS_CPP) {                                                  \
+        for (int64_t k = i + 1; k <= idx; ++k) out[w++] = data ? data[k] : k;           \
+    } else {                                                                            \
+        for (int64_t k = idx; k > i; --k) out[w++] = data ? data[k] : k;               \
+    }                                                                                   \
+    if (i == SIO_NONE) return w;                                                        \
+    i = branch[i];                                                                      \
+    while (i != SIO_NONE) {                                                             \
+        if (qs <= ends[i]) { out[w++] = data ? data[i] : i; --i; }                      \
+        else i = branch[i];                                                             \
+    }                                                                                   \
+    return w;                                                                           \
+}                                                                                       \
+                                                                                        \
+/* coverage (hpp:979-1006): count and sum of min(e)-max(s) (no +1).              */     \
+void sio_coverage_##SFX(int64_t n, const S* starts, const S* ends,                      \
+                        const int64_t* branch, S qs, S qe, int64_t* cnt, S* cov) {      \
+    *cnt = 0; *cov = 0;                                                                 \
+    int64_t i = sio_upper_bound_##SFX(n, starts, qe);                                   \
+    if (i == SIO_NONE) return;                                                          \
+    while (i != SIO_NONE && qs <= ends[i]) {                                            \
+        ++*cnt;                                                                         \
+        *cov += (ends[i] < qe ? ends[i] : qe) - (starts[i] > qs ? starts[i] : qs);      \
+        --i;                                                                            \
+    }                                                                                   \
+    if (i == SIO_NONE) return;                                                          \
+    i = branch[i];                                                                      \
+    while (i != SIO_NONE) {                                                             \
+        if (qs <= ends[i]) {                                                            \
+            ++*cnt;                                                                     \
+            *cov += (ends[i] < qe ? ends[i] : qe) - (starts[i] > qs ? starts[i] : qs);  \
+            --i;                                                                        \
+        } else i = branch[i];                                                           \
+    }                                                                                   \
+}                                                                                       \
+                                                                                        \
+/* ---- batch loops over many queries (intervalmap.pyx:363-494), optionally    */       \
+/* against a set of per-contig maps concatenated with segment offsets.         */       \
+typedef struct {                                                                        \
+    const int64_t* seg; /* n_seg+1 offsets into the concatenated arrays */              \
+    const S* starts; const S* ends; const int64_t* branch; const int32_t* data;         \
+    const int32_t* qc; const S* qs; const S* qe;                                        \
+    int order;                                                                          \
+    uint32_t* counts; const int64_t* offsets; int32_t* out32; int64_t* scratch;         \
+} sio_batch_ctx_##SFX;                                                                  \
+                                                                                        \
+static void sio_count_worker_##SFX(void* p, int64_t b, int64_t e) {                     \
+    sio_batch_ctx_##SFX* c = (sio_batch_ctx_##SFX*)p;                                   \
+    for (int64_t q = b; q < e; ++q) {                                                   \
+        int32_t g = c->qc ? c->qc[q] : 0;                                               \
+        int64_t lo = c->seg[g], n = c->seg[g + 1] - lo;                                 \
+        c->counts[q] = (uint32_t)sio_count_##SFX(n, c->starts + lo, c->ends + lo,      \
+                                                 c->branch + lo, c->qs[q], c->qe[q]);   \
+    }                                                                                   \
+}                                                                                       \
+                                                                                        \
+static void sio_search_worker_##SFX(void* p, int64_t b, int64_t e) {                    \
+    sio_batch_ctx_##SFX* c = (sio_batch_ctx_##SFX*)p;                                   \
+    int64_t cap = 0; int64_t* buf = NULL;                                               \
+    for (int64_t q = b; q < e; ++q) {                                                   \
+        int32_t g = c->qc ? c->qc[q] : 0;                                               \
+        int64_t lo = c->seg[g], n = c->seg[g + 1] - lo;                                 \
+        int64_t need = c->offsets[q + 1] - c->offsets[q];                               \
+        if (need > cap) { cap = need * 2; buf = (int64_t*)realloc(buf, 8 * (size_t)cap); } \
+        int64_t w = sio_search_##SFX(n, c->starts + lo, c->ends + lo, c->branch + lo,   \
+                                     c->data ? c->data + lo : NULL, c->qs[q], c->qe[q], \
+                                     c->order, buf);                                    \
+        int32_t* dst = c->out32 + c->offsets[q];                                        \
+        for (int64_t k = 0; k < w && k < need; ++k) dst[k] = (int32_t)buf[k];           \
+    }                                                                                   \
+    free(buf);                                                                          \
+}                                                                                       \
+                                                                                        \
+void sio_count_batch_##SFX(const int64_t* seg, const S* starts, const S* ends,          \
+                           const int64_t* branch, int64_t nq, const int32_t* qc,        \
+                           const S* qs, const S* qe, uint32_t* counts, int nthreads) {  \
+    sio_batch_ctx_##SFX c;                                                              \
+    memset(&c, 0, sizeof(c));                                                           \
+    c.seg = seg; c.starts = starts; c.ends = ends; c.branch = branch;                   \
+    c.qc = qc; c.qs = qs; c.qe = qe; c.counts = counts;                                 \
+    sio_parallel_for(nq, nthreads, sio_count_worker_##SFX, &c);                         \
+}                                                                                       \
+                                                                                        \
+void sio_search_batch_##SFX(const int64_t* seg, const S* starts, const S* ends,         \
+                            const int64_t* branch, const int32_t* data, int64_t nq,     \
+                            const int32_t* qc, const S* qs, const S* qe, int order,     \
+                            const int64_t* offsets, int32_t* out, int nthreads) {       \
+    sio_batch_ctx_##SFX c;                                                              \
+    memset(&c, 0, sizeof(c));                                                           \
+    c.seg = seg; c.starts = starts; c.ends = ends; c.branch = branch; c.data = data;    \
+    c.qc = qc; c.qs = qs; c.qe = qe; c.order = order; c.offsets = offsets;              \
+    c.out32 = out;                                                                      \
+    sio_parallel_for(nq, nthreads, sio_search_worker_##SFX, &c);                        \
+}                                                                                       \
+                                                                                        \
+/* Per-contig build over concatenated input segments (each segment is one map). */     \
+void sio_build_segments_##SFX(int64_t n_seg, const int64_t* seg, const S* s_in,         \
+                              const S* e_in, const int32_t* d_in, S* s_out, S* e_out,   \
+                              int32_t* d_out, int64_t* perm, int64_t* branch) {         \
+    for (int64_t g = 0; g < n_seg; ++g) {                                               \
+        int64_t lo = seg[g], n = seg[g + 1] - lo;                                       \
+        sio_build_##SFX(n, s_in + lo, e_in + lo, d_in ? d_in + lo : NULL, s_out + lo,   \
+                        e_out + lo, d_out ? d_out + lo : NULL, perm ? perm + lo : NULL, \
+                        branch + lo);                                                   \
+    }                                                                                   \
+}
+
+SIO_DEFINE(i32, int32_t)
+SIO_DEFINE(i64, int64_t)

@@ -1,0 +1,110 @@
+"""The oracle pinned against the reference: every golden fixture (produced by
+the reference's own header and C API, tests/golden/make_golden.py) and the
+known answers asserted by the reference's unit tests (test/tests.cpp)."""
+import numpy as np
+import pytest
+
+from golden_util import (assert_data_parity, assert_values_parity, csr_lists, fixture_names,
+                         load)
+from oracle.oracle import ORDER_DESC, ORDER_IDXS_CPP, Oracle
+
+
+@pytest.fixture(scope="module")
+def oracle():
+    return Oracle()
+
+
+@pytest.mark.parametrize("name", fixture_names())
+def test_oracle_matches_reference_fixture(oracle, name):
+    g = load(name)
+    m = oracle.build(g["starts"], g["ends"], g["data"])
+    n = g["starts"].shape[0]
+    assert np.array_equal(m["starts"], g["ref_sorted_starts"])
+    assert np.array_equal(m["ends"], g["ref_sorted_ends"])
+    assert np.array_equal(m["branch"], g["ref_branch"].astype(np.int64))
+    assert_data_parity(m["starts"], m["ends"], g["ref_sorted_data"], m["data"])
+    if n == 0:
+        return
+    qs, qe = g["q_starts"], g["q_ends"]
+    cnt = oracle.count_batch(m, qs, qe)
+    assert np.array_equal(cnt.astype(np.int64), g["ref_count"].astype(np.int64))
+    off, out = oracle.search_batch(m, qs, qe, order=ORDER_IDXS_CPP)
+    assert np.array_equal(off, g["ref_search_idxs_off"])
+    assert np.array_equal(out, g["ref_search_idxs"])
+    offd, outd = oracle.search_batch(m, qs, qe, order=ORDER_DESC)
+    assert np.array_equal(offd, off)
+    if "ref_c_search_idxs" in g:
+        assert np.array_equal(outd, g["ref_c_search_idxs"])
+        assert np.array_equal(offd, g["ref_c_search_idxs_off"])
+    offv, outv = oracle.search_batch(m, qs, qe, order=ORDER_DESC, values=True)
+    assert np.array_equal(offv, g["ref_search_values_off"])
+    assert_values_parity(outd, offd, g["ref_sorted_data"], m["data"], g["ref_search_values"], outv)
+    hv = oracle.has_overlaps_batch(m, qs, qe)
+    assert np.array_equal(hv, g["ref_has_overlaps"].astype(np.int32))
+    ccount, ccov = oracle.coverage(m, qs[:2000], qe[:2000])
+    assert np.array_equal(ccount, g["ref_coverage_count"][:2000].astype(np.int64))
+    assert np.array_equal(ccov, g["ref_coverage"][:2000])
+
+
+def _vals(g, key, q):
+    off = g[f"ref_{key}_off"]
+    return g[f"ref_{key}"][off[q]:off[q + 1]].tolist()
+
+
+@pytest.mark.parametrize("dt", ["int32", "int64"])
+def test_reference_unit_test_known_answers(dt):
+    """The assertions of test/tests.cpp, checked on the stored reference outputs."""
+    g = load(f"kat_basics_{dt}")
+    assert _vals(g, "search_values", 0) == [4, 0]          # tests.cpp:84-86
+    assert int(g["ref_count"][0]) == 2                        # tests.cpp:89
+    assert _vals(g, "search_idxs", 0) == [4, 0]              # tests.cpp:94-95
+    assert int(g["ref_has_overlaps"][0]) == 1 and int(g["ref_has_overlaps"][1]) == 0
+    assert int(g["ref_coverage"][2]) == 17                    # tests.cpp:105-106
+    g = load(f"kat_nested_{dt}")
+    v = _vals(g, "search_values", 0)
+    assert v[-1] == 0 and len(v) == 12                        # tests.cpp:154-155
+    g = load(f"kat_shared_endpoints_{dt}")
+    assert [len(_vals(g, "search_values", q)) for q in range(3)] == [3, 2, 3]
+    g = load(f"kat_duplicates_{dt}")
+    assert [len(_vals(g, "search_values", q)) for q in range(2)] == [6, 3]
+    g = load(f"kat_coverage_{dt}")
+    assert int(g["ref_coverage_count"][0]) == 3 and int(g["ref_coverage"][0]) == 25
+    g = load(f"kat_single_{dt}")
+    assert int(g["ref_count"][0]) == 1 and int(g["ref_count"][1]) == 0
+    g = load(f"kat_readme_batch_{dt}")
+    assert [int(c) for c in g["ref_count"][:3]] == [1, 2, 1]  # README.md:26
+    assert csr_lists(g["ref_search_idxs_off"][:4], g["ref_search_idxs"]) == [[0], [0, 1], [2]]
+
+
+def test_multicontig_stream_matches_per_contig_fixtures(oracle):
+    s = load("contigs3_stream_int32")
+    m = oracle.build(s["starts"], s["ends"], s["data"], seg=s["seg"])
+    off, out = oracle.search_batch(m, s["q_starts"], s["q_ends"], qc=s["q_contig"],
+                                   order=ORDER_IDXS_CPP, nthreads=2)
+    for gi in range(3):
+        g = load(f"contigs3_g{gi}_int32")
+        qi = g["q_index"]
+        got = [out[off[q]:off[q + 1]].tolist() for q in qi]
+        assert got == csr_lists(g["ref_search_idxs_off"], g["ref_search_idxs"])
+
+
+def test_oracle_threads_agree(oracle):
+    g = load("nested_dups_int32")
+    m = oracle.build(g["starts"], g["ends"], g["data"])
+    a = oracle.search_batch(m, g["q_starts"], g["q_ends"], nthreads=1)
+    b = oracle.search_batch(m, g["q_starts"], g["q_ends"], nthreads=4)
+    assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+
+
+def test_planted_mistake_is_caught(oracle):
+    """The parity check is not vacuous: a branch array with one planted error
+    changes the reference-order output."""
+    g = load("nested_dups_int32")
+    m = oracle.build(g["starts"], g["ends"], g["data"])
+    bad = dict(m)
+    bad["branch"] = m["branch"].copy()
+    k = int(np.nonzero(m["branch"] > 0)[0][len(m["branch"]) // 2 % max(1, (m["branch"] > 0).sum())])
+    bad["branch"][k] = -1
+    off, out = oracle.search_batch(bad, g["q_starts"], g["q_ends"])
+    assert not (np.array_equal(off, g["ref_search_idxs_off"]) and
+                np.array_equal(out, g["ref_search_idxs"]))
