@@ -1,0 +1,423 @@
+"""Benchmark of the batch overlap-query path (search_idxs) on one GB300.
+
+One step = one search_idxs pass (count -> scan -> emit, exact per-query CSR
+offsets, the reference's C++ order) over the whole query batch of the chosen
+workload, against a device-resident index.  Inputs are seeded synthetic
+intervals with the configuration's sizes and length distributions (the
+reference's published timings use BED files that are not available here).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--config config3]
+                  [--path batched|plain] [--ub learned|eytzinger|binary]
+  python bench.py --impl reference ...   # the reference algorithm on the host cores
+
+Prints one JSON line.  `value` = queries/s with inputs resident in HBM;
+`e2e` = the same through the C-ABI with pinned host buffers (H2D of the
+queries and D2H of the CSR result inside the timed region).  Under torchrun
+(N > 1) each rank holds its own replica of the index and processes its own
+query batch of the configuration's size (weak scaling, no data-path
+collective); rank 0 prints the line.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = ("overlap queries/s + result pairs/s on 1 GB300; % HBM peak; batched+learned vs plain")
+PEAK_FALLBACK_GBS = 6800.0
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", default="config3",
+                    choices=["config1", "config2", "config3", "config4"])
+    ap.add_argument("--scale", type=float, default=1.0, help="shrink N and Q (tests only)")
+    ap.add_argument("--path", default="batched", choices=["batched", "plain", "auto"])
+    ap.add_argument("--ub", default="learned", choices=["learned", "eytzinger", "binary"])
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--profile-only", action="store_true",
+                    help="run warmup+steps without the extra legs (for ncu launch lists)")
+    return ap.parse_args()
+
+
+# ----------------------------------------------------------------------------- workload
+def make_workload(cfg, scale, rank):
+    from superintervals_gb300 import workloads as W
+    sizes = {"config1": (100_000, 100_000), "config2": (10_000_000, 10_000_000),
+             "config3": (50_000_000, 50_000_000), "config4": (100_000_000, 100_000_000)}
+    n, nq = sizes[cfg]
+    n, nq = max(1000, int(n * scale)), max(1000, int(nq * scale))
+    wl = getattr(W, cfg)(n=n, nq=nq)
+    if rank:
+        # weak scaling: every rank gets its own query batch of the same size
+        rng = np.random.Generator(np.random.PCG64(1000 + rank))
+        perm = rng.permutation(wl.nq)
+        wl.q_starts, wl.q_ends = wl.q_starts[perm], wl.q_ends[perm]
+        if wl.q_contig is not None:
+            wl.q_contig = wl.q_contig[perm]
+    return wl
+
+
+def workload_desc(cfg, wl):
+    d = {"workload": wl.name, "n_intervals": wl.n, "n_queries": wl.nq,
+         "coord": str(wl.dtype), "contigs": int(len(wl.seg) - 1), "op": "search_idxs (C++ order)",
+         "inputs": "larger than L2 (index + queries > 129 MB); L2 flushed between steps"}
+    if wl.notes:
+        d["notes"] = wl.notes
+    return d
+
+
+# ----------------------------------------------------------------------------- clocks
+class ClockSampler:
+    """nvidia-smi clocks/throttle sampling during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            try:
+                sm.append(float(r[1]))
+                mx = float(r[2])
+                for k, nm in enumerate(names):
+                    if r[5 + k].lower().startswith("active"):
+                        reasons.add(nm)
+            except (ValueError, IndexError):
+                pass
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peak():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return PEAK_FALLBACK_GBS, "fallback"
+
+
+# ----------------------------------------------------------------------------- GPU arm
+def run_gpu(args, rank, world, dist):
+    from superintervals_gb300 import _capi
+    from superintervals_gb300.interval_map import GpuIndex
+    lib = _capi.load()
+    wl = make_workload(args.config, args.scale, rank)
+    s_bytes = wl.dtype.itemsize
+    idx = GpuIndex(64 if s_bytes == 8 else 32, 0)
+    idx.add_arrays(wl.starts, wl.ends, wl.data, seg=wl.seg if len(wl.seg) > 2 else None)
+    t0 = time.perf_counter()
+    idx.build()
+    build_s = time.perf_counter() - t0
+    path = {"batched": _capi.PATH_BATCHED, "plain": _capi.PATH_PLAIN, "auto": _capi.PATH_AUTO}[args.path]
+    ub = {"learned": _capi.UB_LEARNED, "eytzinger": _capi.UB_EYTZINGER, "binary": _capi.UB_BINARY}[args.ub]
+    idx.set_path(path)
+    idx.set_upper_bound(ub)
+    st = idx.stream
+    nq = wl.nq
+
+    def dalloc(nbytes):
+        p = C.c_void_p()
+        _capi.check(lib.deviceMallocGpu(C.byref(p), max(int(nbytes), 1)))
+        return p
+
+    def h2d(dst, arr):
+        _capi.check(lib.memcpyGpu(dst, C.c_void_p(arr.ctypes.data), arr.nbytes, st))
+
+    d_qs, d_qe = dalloc(wl.q_starts.nbytes), dalloc(wl.q_ends.nbytes)
+    h2d(d_qs, np.ascontiguousarray(wl.q_starts))
+    h2d(d_qe, np.ascontiguousarray(wl.q_ends))
+    d_qc = None
+    if wl.q_contig is not None:
+        d_qc = dalloc(wl.q_contig.nbytes)
+        h2d(d_qc, np.ascontiguousarray(wl.q_contig))
+    d_off = dalloc(8 * (nq + 1))
+    total = C.c_size_t(0)
+    st_ = lib.searchDeviceGpu(idx.h, d_qs, d_qe, d_qc, nq, 0, 0, d_off, None, 0, C.byref(total), st)
+    if st_ not in (_capi.SI_OK, _capi.SI_ERR_CAPACITY):
+        _capi.check(st_)
+    P = int(total.value)
+    d_out = dalloc(4 * max(P, 1))
+
+    def step():
+        _capi.check(lib.searchDeviceGpu(idx.h, d_qs, d_qe, d_qc, nq, 0, 0, d_off, d_out, P,
+                                        C.byref(total), st))
+
+    ev = [C.c_void_p(), C.c_void_p()]
+    for e in ev:
+        _capi.check(lib.eventCreateGpu(C.byref(e)))
+
+    def timed(k, w, fn):
+        for _ in range(w):
+            _capi.check(lib.flushL2Gpu(st))
+            fn()
+        _capi.check(lib.streamSynchronizeGpu(st))
+        if dist:
+            dist.barrier()
+        total_ms = 0.0
+        for _ in range(k):
+            _capi.check(lib.flushL2Gpu(st))
+            _capi.check(lib.eventRecordGpu(ev[0], st))
+            fn()
+            _capi.check(lib.eventRecordGpu(ev[1], st))
+            _capi.check(lib.streamSynchronizeGpu(st))
+            ms = C.c_float()
+            _capi.check(lib.eventElapsedMsGpu(ev[0], ev[1], C.byref(ms)))
+            total_ms += ms.value
+        if dist:
+            dist.barrier()
+        return total_ms
+
+    with ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) as clk:
+        total_ms = timed(args.steps, args.warmup, step)
+    if dist:
+        import torch
+        t = torch.tensor([total_ms], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    ms_per_step = total_ms / args.steps
+    res = {"wl": wl, "P": P, "nq": nq, "ms_per_step": ms_per_step, "build_s": build_s,
+           "clocks": clk.summary(), "s_bytes": s_bytes}
+    if args.profile_only:
+        return res
+
+    # per-phase device times (count / scan / emit / prepare) for the roofline
+    _capi.check(lib.setProfilingGpu(idx.h, 1))
+    for _ in range(max(1, min(3, args.steps))):
+        _capi.check(lib.flushL2Gpu(st))
+        step()
+    ms4 = (C.c_double * 4)()
+    n4 = (C.c_int64 * 4)()
+    _capi.check(lib.getPhaseTimesGpu(idx.h, ms4, n4))
+    _capi.check(lib.setProfilingGpu(idx.h, 0))
+    res["phase_ms"] = [ms4[k] / max(1, n4[k]) for k in range(4)]
+
+    # the plain one-query-per-thread GPU path on the same inputs (the 1.0x baseline)
+    if not args.no_plain and args.path != "plain":
+        idx.set_path(_capi.PATH_PLAIN)
+        idx.set_upper_bound(_capi.UB_BINARY)
+        res["plain_ms"] = timed(max(1, args.steps // 2), 1, step) / max(1, args.steps // 2)
+        idx.set_path(path)
+        idx.set_upper_bound(ub)
+
+    # e2e through the C-ABI with pinned host buffers
+    if not args.no_e2e:
+        def pinned(nbytes):
+            p = C.c_void_p()
+            _capi.check(lib.hostMallocPinnedGpu(C.byref(p), max(int(nbytes), 1)))
+            return p
+        hq_s, hq_e = pinned(wl.q_starts.nbytes), pinned(wl.q_ends.nbytes)
+        C.memmove(hq_s, wl.q_starts.ctypes.data, wl.q_starts.nbytes)
+        C.memmove(hq_e, wl.q_ends.ctypes.data, wl.q_ends.nbytes)
+        hq_c = None
+        if wl.q_contig is not None:
+            hq_c = pinned(wl.q_contig.nbytes)
+            C.memmove(hq_c, wl.q_contig.ctypes.data, wl.q_contig.nbytes)
+        h_off = pinned(8 * (nq + 1))
+        h_out = pinned(4 * max(P, 1))
+        idx.set_output_budget(max(4 * P, 1 << 20))
+
+        def e2e_step():
+            _capi.check(lib.searchBatchIntoGpu(idx.h, hq_s, hq_e, hq_c, nq, 0, 0, h_off, h_out, P,
+                                               C.byref(total)))
+        for _ in range(max(1, args.warmup)):
+            e2e_step()
+        if dist:
+            dist.barrier()
+        t0 = time.perf_counter()
+        k = max(1, args.steps)
+        for _ in range(k):
+            e2e_step()
+        e2e_s = (time.perf_counter() - t0) / k
+        if dist:
+            import torch
+            t = torch.tensor([e2e_s], dtype=torch.float64)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            e2e_s = float(t.item())
+        res["e2e_s"] = e2e_s
+        res["h2d_bytes"] = wl.q_starts.nbytes + wl.q_ends.nbytes + (wl.q_contig.nbytes if hq_c else 0)
+        res["d2h_bytes"] = 8 * (nq + 1) + 4 * P
+        for p in (hq_s, hq_e, hq_c, h_off, h_out):
+            if p:
+                lib.hostFreePinnedGpu(p)
+    for p in (d_qs, d_qe, d_qc, d_off, d_out):
+        if p:
+            lib.deviceFreeGpu(p)
+    idx.close()
+    return res
+
+
+# ----------------------------------------------------------------------------- CPU arm
+def cpu_run(wl, seconds, nthreads):
+    """The reference algorithm (oracle port, oracle/si_oracle.c) on the host
+    cores: count + emit (search_idxs, C++ order) over a bounded query sample."""
+    from oracle.oracle import ORDER_IDXS_CPP, Oracle
+    o = Oracle()
+    m = o.build(wl.starts, wl.ends, wl.data, seg=wl.seg)
+    probe = min(wl.nq, 20_000)
+    t0 = time.perf_counter()
+    qc = None if wl.q_contig is None else wl.q_contig[:probe]
+    o.search_batch(m, wl.q_starts[:probe], wl.q_ends[:probe], qc, order=ORDER_IDXS_CPP,
+                   nthreads=nthreads)
+    dt = max(time.perf_counter() - t0, 1e-6)
+    k = int(min(wl.nq, max(probe, probe * seconds / dt)))
+    qc = None if wl.q_contig is None else wl.q_contig[:k]
+    t0 = time.perf_counter()
+    off, _ = o.search_batch(m, wl.q_starts[:k], wl.q_ends[:k], qc, order=ORDER_IDXS_CPP,
+                            nthreads=nthreads)
+    dt = time.perf_counter() - t0
+    return {"q_per_s": k / dt, "pairs_per_s": float(off[-1]) / dt, "sample_q": k, "seconds": dt,
+            "pairs": int(off[-1])}
+
+
+def host_threads():
+    try:
+        return len(os.sched_getaffinity(0))
+    except Exception:
+        return os.cpu_count() or 1
+
+
+# ----------------------------------------------------------------------------- main
+def init_dist(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+        return rank, world, dist
+    return rank, world, None
+
+
+def main():
+    args = parse()
+    rank, world, dist = init_dist(args)
+    cfg = args.config
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        wl = make_workload(cfg, args.scale, 0)
+        nth = host_threads()
+        for _ in range(max(0, min(args.warmup, 1))):
+            cpu_run(wl, min(2.0, args.cpu_seconds / 4), nth)
+        runs = [cpu_run(wl, args.cpu_seconds / max(1, args.steps), nth) for _ in range(args.steps)]
+        qps = statistics.median(r["q_per_s"] for r in runs)
+        pps = statistics.median(r["pairs_per_s"] for r in runs)
+        sample = (f"{runs[0]['sample_q']} of {wl.nq} queries per step "
+                  f"({runs[0]['pairs']} result pairs), search_idxs C++ order, {nth} threads")
+        line = {"metric": METRIC, "value": qps, "unit": "queries/s", "impl": "reference",
+                "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+                "ms_per_step": 1000.0 * statistics.median(r["seconds"] for r in runs),
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": str(wl.dtype),
+                "data": "synthetic (seeded)", "config": workload_desc(cfg, wl),
+                "pairs_per_s": pps,
+                "cpu_baseline": {"value": qps, "unit": "queries/s", "cores": nth, "kind": "port",
+                                 "sample": sample},
+                "e2e": {"value": qps, "unit": "queries/s", "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": 0},
+                "note": "reference algorithm restated in C (oracle/si_oracle.c, pinned to the "
+                        "reference's own outputs); the reference header cannot be compiled on "
+                        "the GPU host because its sources are not present there"}
+        print(json.dumps(line), flush=True)
+        return
+
+    res = run_gpu(args, rank, world, dist)
+    if rank != 0:
+        return
+    wl, P, nq = res["wl"], res["P"], res["nq"]
+    s = res["s_bytes"]
+    ms = res["ms_per_step"]
+    qps = world * nq / (ms / 1000.0)
+    pps = world * P / (ms / 1000.0)
+    peak, peak_kind = measured_peak()
+    line = {"metric": METRIC, "value": qps, "unit": "queries/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "int32" if s == 4 else "int64", "data": "synthetic (seeded)",
+            "config": dict(workload_desc(cfg, wl), path=args.path, upper_bound=args.ub),
+            "pairs_per_s": pps, "result_pairs_per_step": P,
+            "build_s": res["build_s"], "clocks": res["clocks"]}
+    if args.profile_only:
+        print(json.dumps(line), flush=True)
+        return
+    # roofline of the dominant kernel (emit) with the algorithmic bytes
+    # B = Q*(2s+8) + P*(s+4): query read, offset read, one end read and one index
+    # write per result pair
+    ph = res.get("phase_ms", [0, 0, 0, 0])
+    emit_ms = ph[2] if ph[2] > 0 else ms
+    algo = nq * (2 * s + 8) + P * (s + 4)
+    achieved = algo / (emit_ms / 1000.0) / 1e9
+    line["roofline"] = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                        "frac": achieved / peak, "traffic": None, "kernel": "emit",
+                        "peak_kind": peak_kind, "algorithmic_bytes": algo,
+                        "phase_ms": {"count": ph[0], "scan": ph[1], "emit": ph[2], "prepare": ph[3]},
+                        "whole_step_frac": (algo / (ms / 1000.0) / 1e9) / peak}
+    line["gpu_launches"] = None
+    if "plain_ms" in res:
+        line["plain_gpu"] = {"ms_per_step": res["plain_ms"], "queries_per_s": nq / (res["plain_ms"] / 1e3),
+                             "speedup_vs_plain": res["plain_ms"] / ms}
+    if "e2e_s" in res:
+        line["e2e"] = {"value": world * nq / res["e2e_s"], "unit": "queries/s",
+                       "h2d_bytes_per_step": res["h2d_bytes"], "d2h_bytes_per_step": res["d2h_bytes"],
+                       "pairs_per_s": world * P / res["e2e_s"]}
+    if not args.no_cpu:
+        nth = host_threads()
+        c = cpu_run(wl, args.cpu_seconds, nth)
+        line["cpu_baseline"] = {"value": c["q_per_s"], "unit": "queries/s", "cores": nth, "kind": "port",
+                                "sample": f"{c['sample_q']} of {nq} queries, search_idxs C++ order "
+                                          f"({c['pairs']} pairs), {nth} threads",
+                                "pairs_per_s": c["pairs_per_s"]}
+    print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,192 @@
+/*
+ * c_api.h -- C-ABI of the GB300 SuperIntervals overlap-query library (libsi_gpu.so).
+ *
+ * Drop-in for the batch overlap-query path of kcleal/superintervals.  Every
+ * entry point below names the reference interface it replaces (file:line in
+ * the reference project).  Semantics follow the reference exactly:
+ *   - intervals are END-INCLUSIVE [start, end];
+ *   - indexSuperIntervalsGpu sorts by (start asc, end desc) and builds the
+ *     branch array (nearest preceding interval with end >= this end);
+ *   - searchIdxs results use the C++ order (ascending head run, then the
+ *     descending branch walk) or the fully descending order of the C API;
+ *   - results are per-query lists, returned in CSR form (offsets + values).
+ * Differences, all deliberate:
+ *   - every call returns an int status (SI_OK = 0) because device work can fail;
+ *     the reference's void returns cannot report that;
+ *   - the sort is stable: payloads of exact (start, end) duplicates keep their
+ *     insertion order (the reference's std::sort / qsort leave it unspecified);
+ *   - a handle may hold several contigs (one independent map per contig, the
+ *     per-chromosome pattern of examples/bed-intersect-si.rs:98-120); queries
+ *     then carry a contig id and results carry contig-local indices.
+ *
+ * Threading: one CUDA stream per handle; calls on one handle must not overlap.
+ * Ownership: the handle owns its device buffers; result buffers belong to the
+ * caller (cCsrResult buffers grown by the library are freed by destroyCsrResult).
+ */
+#ifndef SI_GPU_C_API_H
+#define SI_GPU_C_API_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SI_GPU_VERSION "1.0.0"
+
+/* ---- status codes ------------------------------------------------------ */
+#define SI_OK 0
+#define SI_ERR_INVALID 1      /* bad argument (null pointer, wrong coordinate width, bad contig) */
+#define SI_ERR_OOM 2          /* device allocation failed or exceeded the device budget */
+#define SI_ERR_NOT_BUILT 3    /* query before indexSuperIntervalsGpu (or after a later add) */
+#define SI_ERR_CUDA 4         /* a CUDA call failed; see lastErrorGpu() */
+#define SI_ERR_CAPACITY 5     /* caller-provided output too small; the needed size is reported */
+#define SI_ERR_UNSUPPORTED 6  /* option not available for this handle */
+#define SI_ERR_TOO_LARGE 7    /* more intervals than the 32-bit position space allows */
+
+/* ---- query orders ------------------------------------------------------ */
+#define SI_ORDER_IDXS_CPP 0   /* si::IntervalMap::search_idxs (superintervals.hpp:879-905) */
+#define SI_ORDER_DESC 1       /* search_values (hpp:551-579) and C searchIdxs (c_superintervals.h:610-643) */
+
+/* ---- query paths -------------------------------------------------------- */
+#define SI_PATH_AUTO 0        /* library choice */
+#define SI_PATH_PLAIN 1       /* one query per thread, reference walk */
+#define SI_PATH_BATCHED 2     /* sorted-query tiles sharing one candidate walk */
+
+/* ---- upper-bound search modes -------------------------------------------- */
+#define SI_UB_BINARY 0        /* branch-free halving search (superintervals.hpp:501-516) */
+#define SI_UB_EYTZINGER 1     /* shared-memory Eytzinger top levels + bounded global search */
+#define SI_UB_LEARNED 2       /* two-stage piecewise-linear model + max-error window */
+
+/* Opaque handle: replaces cSuperIntervals (c_superintervals.h:81-91). */
+typedef struct gSuperIntervals gSuperIntervals;
+
+/* CSR result: offsets[n_queries + 1] and values[offsets[n_queries]].
+ * Replaces the per-query cIndexResult buffers (c_superintervals.h:98-102) and the
+ * list-of-lists of the batch methods (intervalmap.pyx:402-494). */
+typedef struct {
+    int64_t* offsets;
+    int32_t* values;
+    size_t n_queries;
+    size_t size;              /* number of values */
+    size_t capacity;          /* allocated values */
+    size_t offsets_capacity;  /* allocated offsets */
+} cCsrResult;
+
+/* ---- lifecycle: createSuperIntervals / destroySuperIntervals /
+ *      clearSuperIntervals / reserveSuperIntervals (c_superintervals.h:135-144) ---- */
+int createSuperIntervalsGpu(gSuperIntervals** out, int coord_bits /* 32 or 64 */, int device);
+void destroySuperIntervalsGpu(gSuperIntervals* si);
+int clearSuperIntervalsGpu(gSuperIntervals* si);
+int reserveSuperIntervalsGpu(gSuperIntervals* si, size_t n);
+
+/* ---- staging: addInterval (c_superintervals.h:153, 402-419; hpp:95-105);
+ *      the array forms replace IntervalMap.from_arrays (intervalmap.pyx:63-131) -- */
+int addIntervalGpu(gSuperIntervals* si, int32_t start, int32_t end, int32_t value);
+int addIntervalGpu_i64(gSuperIntervals* si, int64_t start, int64_t end, int32_t value);
+int addIntervalsGpu(gSuperIntervals* si, const int32_t* starts, const int32_t* ends,
+                    const int32_t* values /* may be NULL: insertion index */, size_t n);
+int addIntervalsGpu_i64(gSuperIntervals* si, const int64_t* starts, const int64_t* ends,
+                        const int32_t* values, size_t n);
+/* Declare that the staged intervals form n_contigs consecutive groups:
+ * contig g holds staged intervals [offsets[g], offsets[g+1]).  No reference
+ * counterpart (one IntervalMap per contig there). */
+int setContigsGpu(gSuperIntervals* si, size_t n_contigs, const int64_t* offsets);
+size_t sizeSuperIntervalsGpu(const gSuperIntervals* si);          /* c_superintervals.h:156 */
+size_t numContigsGpu(const gSuperIntervals* si);
+
+/* ---- index: indexSuperIntervals (c_superintervals.h:169, 487-521);
+ *      IntervalMap::build (superintervals.hpp:112-130) ---------------------- */
+int indexSuperIntervalsGpu(gSuperIntervals* si);
+/* Sorted arrays after indexing (starts/ends as the handle's coordinate width;
+ * branch is contig-local, -1 where the reference holds SIZE_MAX).  Any pointer
+ * may be NULL.  Replaces intervalAt/startAt/endAt/dataAt (c_superintervals.h:176-185) and
+ * the public vectors starts/ends/branch/data (superintervals.hpp:49-61). */
+int getIndexArraysGpu(const gSuperIntervals* si, void* starts, void* ends, int32_t* data,
+                      int64_t* branch);
+
+/* ---- options (no reference counterpart) ------------------------------- */
+int setQueryPathGpu(gSuperIntervals* si, int path);
+int setUpperBoundModeGpu(gSuperIntervals* si, int mode);
+/* Device bytes one search call may use for its result buffer; larger results
+ * are emitted in query chunks against it. */
+int setOutputBudgetGpu(gSuperIntervals* si, size_t bytes);
+/* Per-phase device time of the query pipeline, measured with CUDA events on
+ * the stream the phase runs on while profiling is on (it synchronizes after
+ * each phase).  Phases: 0 count, 1 scan, 2 emit, 3 query preparation (query
+ * sort and upper-bound search of the batched path).  ms and calls hold 4 values. */
+int setProfilingGpu(gSuperIntervals* si, int on);
+int getPhaseTimesGpu(const gSuperIntervals* si, double* ms, int64_t* calls);
+/* Process-wide cap on device bytes the library allocates (0 = no cap). */
+int setDeviceBudgetGpu(size_t bytes);
+size_t deviceBytesInUseGpu(void);
+
+/* ---- batch queries with HOST buffers.  coordinates: int32 (handle made with
+ *      32) or the _i64 forms; qcontig may be NULL (all contig 0). ---------- */
+/* countOverlaps (c_superintervals.h:205, 729-756) / count (hpp:651-825) /
+ * count_batch (intervalmap.pyx:363-400) */
+int countOverlapsBatchGpu(gSuperIntervals* si, const int32_t* qs, const int32_t* qe,
+                          const int32_t* qcontig, size_t nq, uint32_t* counts);
+int countOverlapsBatchGpu_i64(gSuperIntervals* si, const int64_t* qs, const int64_t* qe,
+                              const int32_t* qcontig, size_t nq, uint32_t* counts);
+/* anyOverlaps (c_superintervals.h:202, 570-573) / has_overlaps (hpp:865-871):
+ * true iff the interval at upper_bound(qe) reaches qs */
+int anyOverlapsBatchGpu(gSuperIntervals* si, const int32_t* qs, const int32_t* qe,
+                        const int32_t* qcontig, size_t nq, uint8_t* out);
+int anyOverlapsBatchGpu_i64(gSuperIntervals* si, const int64_t* qs, const int64_t* qe,
+                            const int32_t* qcontig, size_t nq, uint8_t* out);
+/* searchIdxs (c_superintervals.h:214, 610-643) / search_idxs (hpp:879-905) /
+ * search_idxs_batch (intervalmap.pyx:402-446) */
+int searchIdxsBatchGpu(gSuperIntervals* si, const int32_t* qs, const int32_t* qe,
+                       const int32_t* qcontig, size_t nq, int order, cCsrResult* out);
+int searchIdxsBatchGpu_i64(gSuperIntervals* si, const int64_t* qs, const int64_t* qe,
+                           const int32_t* qcontig, size_t nq, int order, cCsrResult* out);
+/* searchValues (c_superintervals.h:211, 575-608) / search_values (hpp:551-579) /
+ * search_values_batch (intervalmap.pyx:448-494): payloads, fully descending */
+int searchValuesBatchGpu(gSuperIntervals* si, const int32_t* qs, const int32_t* qe,
+                         const int32_t* qcontig, size_t nq, cCsrResult* out);
+int searchValuesBatchGpu_i64(gSuperIntervals* si, const int64_t* qs, const int64_t* qe,
+                             const int32_t* qcontig, size_t nq, cCsrResult* out);
+/* Same, into caller-owned host buffers (e.g. pinned): offsets needs nq+1
+ * slots; returns SI_ERR_CAPACITY with *total set when values is too small. */
+int searchBatchIntoGpu(gSuperIntervals* si, const void* qs, const void* qe,
+                       const int32_t* qcontig, size_t nq, int order, int values_not_idxs,
+                       int64_t* offsets, int32_t* values, size_t capacity, size_t* total);
+
+/* ---- batch queries with DEVICE buffers (inputs already in HBM).  stream
+ *      may be NULL (the handle's stream).  Same semantics as above. ---------- */
+int countOverlapsDeviceGpu(gSuperIntervals* si, const void* d_qs, const void* d_qe,
+                           const int32_t* d_qcontig, size_t nq, uint32_t* d_counts, void* stream);
+int searchDeviceGpu(gSuperIntervals* si, const void* d_qs, const void* d_qe,
+                    const int32_t* d_qcontig, size_t nq, int order, int values_not_idxs,
+                    int64_t* d_offsets, int32_t* d_values, size_t capacity, size_t* total,
+                    void* stream);
+
+/* ---- result helpers: createIndexResult / clearIndexResult /
+ *      destroyIndexResult (c_superintervals.h:339-343, 1070-1075) --------- */
+cCsrResult createCsrResult(void);
+void clearCsrResult(cCsrResult* r);
+void destroyCsrResult(cCsrResult* r);
+
+/* ---- small runtime helpers so that hosts need no CUDA headers ---------- */
+const char* lastErrorGpu(void);           /* message of the last failing call on this thread */
+void* getStreamGpu(gSuperIntervals* si);  /* the handle's cudaStream_t */
+int deviceCountGpu(int* count);
+int deviceMallocGpu(void** ptr, size_t bytes);
+int deviceFreeGpu(void* ptr);
+int hostMallocPinnedGpu(void** ptr, size_t bytes);
+int hostFreePinnedGpu(void* ptr);
+int memcpyGpu(void* dst, const void* src, size_t bytes, void* stream); /* any direction, async */
+int streamSynchronizeGpu(void* stream);
+int eventCreateGpu(void** ev);
+int eventDestroyGpu(void* ev);
+int eventRecordGpu(void* ev, void* stream);
+int eventElapsedMsGpu(void* start, void* stop, float* ms);
+/* L2 flush: writes a device buffer larger than L2 on the stream. */
+int flushL2Gpu(void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SI_GPU_C_API_H */

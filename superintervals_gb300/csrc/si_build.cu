@@ -1,0 +1,302 @@
+// si_build.cu -- device side of build(): sortedness check, sort keys, decode,
+// the max-of-32 pyramid over ends, and the branch array.
+//
+// Reference: IntervalMap::build() (src/superintervals.hpp:112-130) and
+// indexSuperIntervals (src/c_superintervals.h:487-521).  The reference computes
+//     branch[i] = nearest j < i with ends[j] >= ends[i]   (else SIZE_MAX)
+// with a sequential monotonic stack (pop while top < ends[i], hpp:122).  Here
+// the same "previous greater-or-equal" relation is found in parallel:
+//   * inside each 32-interval chunk with warp shuffles (one warp = one chunk);
+//   * across chunks by climbing a max-of-32 pyramid of ends: at level h the
+//     warp compares its node's 31 left siblings' maxima (one coalesced 128-byte
+//     load, broadcast by shuffle) against each lane's end, picks the nearest
+//     sibling whose max is >= the end, and the lane descends that sibling's
+//     subtree (always the right-most child whose max is >= the end) down to the
+//     interval.  Ties resolve exactly as the stack does (>=).
+// A result that falls before the lane's contig start becomes -1 (per-contig maps).
+#include <algorithm>
+#include "si_internal.cuh"
+
+namespace sig {
+namespace {
+
+constexpr int kThreads = 256;
+
+__device__ __forceinline__ int64_t seg_of(const int64_t* __restrict__ seg, int G, int64_t i) {
+    // largest g with seg[g] <= i
+    int lo = 0, hi = G - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (seg[mid] <= i) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+template <typename S>
+__global__ void k_check_sorted(const S* __restrict__ s, const S* __restrict__ e, int64_t n,
+                               const int64_t* __restrict__ seg, int G, int* __restrict__ flag) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    bool bad = false;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x + 1; i < n; i += stride) {
+        if (G > 1 && seg[seg_of(seg, G, i)] == i) continue;  // first interval of a contig
+        const S s0 = s[i - 1], s1 = s[i];
+        if (s1 < s0 || (s1 == s0 && e[i] > e[i - 1])) bad = true;
+    }
+    if (__any_sync(kFull, bad) && (threadIdx.x & 31) == 0) atomicOr(flag, 1);
+}
+
+template <typename S>
+__global__ void k_make_keys(const S* __restrict__ s, const S* __restrict__ e, int64_t n,
+                            const int64_t* __restrict__ seg, int G, uint32_t* w0, uint32_t* w1,
+                            uint32_t* w2, uint32_t* w3, uint32_t* w4,
+                            uint32_t* __restrict__ payload) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    if constexpr (sizeof(S) == 4) {
+        // end descending: complement of the order-preserving bias
+        w0[i] = ~((uint32_t)e[i] ^ 0x80000000u);
+        w1[i] = (uint32_t)s[i] ^ 0x80000000u;
+        if (G > 1) w2[i] = (uint32_t)seg_of(seg, G, i);
+    } else {
+        const uint64_t eb = ~((uint64_t)e[i] ^ 0x8000000000000000ull);
+        const uint64_t sb = (uint64_t)s[i] ^ 0x8000000000000000ull;
+        w0[i] = (uint32_t)eb;
+        w1[i] = (uint32_t)(eb >> 32);
+        w2[i] = (uint32_t)sb;
+        w3[i] = (uint32_t)(sb >> 32);
+        if (G > 1) w4[i] = (uint32_t)seg_of(seg, G, i);
+    }
+    payload[i] = (uint32_t)i;
+}
+
+template <typename S>
+__global__ void k_decode(const uint32_t* __restrict__ w0, const uint32_t* __restrict__ w1,
+                         const uint32_t* __restrict__ w2, const uint32_t* __restrict__ w3,
+                         const uint32_t* __restrict__ perm, const int32_t* __restrict__ data_in,
+                         int64_t n, int64_t n_pad, S* __restrict__ starts, S* __restrict__ ends,
+                         int32_t* __restrict__ data) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_pad) return;
+    if (i >= n) {
+        starts[i] = Lim<S>::hi;
+        ends[i] = Lim<S>::lo;
+        return;
+    }
+    if constexpr (sizeof(S) == 4) {
+        ends[i] = (S)((~w0[i]) ^ 0x80000000u);
+        starts[i] = (S)(w1[i] ^ 0x80000000u);
+    } else {
+        const uint64_t eb = ((uint64_t)w1[i] << 32) | w0[i];
+        const uint64_t sb = ((uint64_t)w3[i] << 32) | w2[i];
+        ends[i] = (S)((~eb) ^ 0x8000000000000000ull);
+        starts[i] = (S)(sb ^ 0x8000000000000000ull);
+    }
+    data[i] = data_in[perm[i]];
+}
+
+template <typename S>
+__global__ void k_copy_pad(const S* __restrict__ s_in, const S* __restrict__ e_in,
+                           const int32_t* __restrict__ d_in, int64_t n, int64_t n_pad,
+                           S* __restrict__ starts, S* __restrict__ ends, int32_t* __restrict__ data,
+                           uint32_t* __restrict__ perm) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_pad) return;
+    if (i >= n) {
+        starts[i] = Lim<S>::hi;
+        ends[i] = Lim<S>::lo;
+        return;
+    }
+    starts[i] = s_in[i];
+    ends[i] = e_in[i];
+    data[i] = d_in[i];
+    if (perm) perm[i] = (uint32_t)i;
+}
+
+// out[c] = max(in[32c .. 32c+31]); `in` is padded to a multiple of 32, `out`
+// to a multiple of 32 with S_MIN.
+template <typename S>
+__global__ void k_level_max(const S* __restrict__ in, int64_t n_out, int64_t n_out_pad,
+                            S* __restrict__ out) {
+    const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= n_out_pad) return;
+    if (c >= n_out) {
+        out[c] = Lim<S>::lo;
+        return;
+    }
+    const S* p = in + (c << 5);
+    S m = p[0];
+#pragma unroll
+    for (int k = 1; k < 32; ++k) m = p[k] > m ? p[k] : m;
+    out[c] = m;
+}
+
+template <typename S>
+__global__ void __launch_bounds__(kThreads) k_branch(const S* __restrict__ ends, int64_t n,
+                                                     int64_t n_pad, Levels<S> L, int H,
+                                                     const int64_t* __restrict__ seg, int G,
+                                                     int32_t* __restrict__ branch) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if ((i & ~(int64_t)31) >= n_pad) return;  // warp-uniform: n_pad is a multiple of 32
+    const int lane = threadIdx.x & 31;
+    const bool valid = i < n;
+    const S e = ends[i];
+
+    // level 0: nearest earlier lane of this chunk with end >= e
+    int best = -1;
+#pragma unroll
+    for (int k = 0; k < 31; ++k) {
+        const S v = __shfl_sync(kFull, e, k);
+        if (k < lane && v >= e) best = k;
+    }
+    int64_t res = (best >= 0) ? ((i & ~(int64_t)31) + best) : -1;
+    bool open = valid && best < 0;
+    int tgt_level = 0;
+    int64_t tgt_node = -1;
+    int64_t node = i >> 5;  // level-1 node (chunk) holding i
+    for (int h = 1; h <= H; ++h) {
+        if (!__any_sync(kFull, open)) break;
+        const int64_t grp = node >> 5;
+        const int pos = (int)(node & 31);
+        const S mv = L.p[h - 1][(grp << 5) + lane];
+        int bk = -1;
+#pragma unroll
+        for (int k = 0; k < 31; ++k) {
+            const S v = __shfl_sync(kFull, mv, k);
+            if (k < pos && v >= e) bk = k;
+        }
+        if (open && bk >= 0) {
+            tgt_level = h;
+            tgt_node = (grp << 5) + bk;
+            open = false;
+        }
+        node = grp;
+    }
+    if (tgt_level > 0) {
+        int64_t cur = tgt_node;
+        for (int h = tgt_level; h > 1; --h) {
+            const S* child = L.p[h - 2] + (cur << 5);
+            int k = 31;
+            while (k > 0 && child[k] < e) --k;
+            cur = (cur << 5) + k;
+        }
+        const S* el = ends + (cur << 5);
+        int k = 31;
+        while (k > 0 && el[k] < e) --k;
+        res = (cur << 5) + k;
+    }
+    if (!valid) return;
+    if (G > 1 && res >= 0 && res < seg[seg_of(seg, G, i)]) res = -1;
+    branch[i] = (int32_t)res;
+}
+
+inline unsigned blocks_for(int64_t n, int t = kThreads) {
+    return (unsigned)std::max<int64_t>(1, ceil_div(n, t));
+}
+
+}  // namespace
+
+template <typename S>
+cudaError_t launch_check_sorted(const S* s, const S* e, int64_t n, const int64_t* seg, int G,
+                                int* d_flag, cudaStream_t st) {
+    cudaError_t err = cudaMemsetAsync(d_flag, 0, sizeof(int), st);
+    if (err != cudaSuccess || n <= 1) return err;
+    const unsigned blocks = (unsigned)std::min<int64_t>(ceil_div(n, kThreads), 152 * 16);
+    k_check_sorted<S><<<blocks, kThreads, 0, st>>>(s, e, n, seg, G, d_flag);
+    return cudaGetLastError();
+}
+
+template <typename S>
+int key_words(int G) {
+    return (sizeof(S) == 4 ? 2 : 4) + (G > 1 ? 1 : 0);
+}
+
+template <typename S>
+cudaError_t launch_make_keys(const S* s, const S* e, int64_t n, const int64_t* seg, int G,
+                             uint32_t* const* kw, uint32_t* payload, cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    const int K = key_words<S>(G);
+    uint32_t* w[kMaxKeyWords] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+    for (int k = 0; k < K; ++k) w[k] = kw[k];
+    k_make_keys<S><<<blocks_for(n), kThreads, 0, st>>>(s, e, n, seg, G, w[0], w[1], w[2], w[3],
+                                                      w[4], payload);
+    return cudaGetLastError();
+}
+
+template <typename S>
+cudaError_t launch_decode(const uint32_t* const* kw, const uint32_t* perm, const int32_t* data_in,
+                          int64_t n, int64_t n_pad, S* starts, S* ends, int32_t* data,
+                          cudaStream_t st) {
+    if (n_pad <= 0) return cudaSuccess;
+    const uint32_t* w2 = sizeof(S) == 8 ? kw[2] : nullptr;
+    const uint32_t* w3 = sizeof(S) == 8 ? kw[3] : nullptr;
+    k_decode<S><<<blocks_for(n_pad), kThreads, 0, st>>>(kw[0], kw[1], w2, w3, perm, data_in, n,
+                                                       n_pad, starts, ends, data);
+    return cudaGetLastError();
+}
+
+template <typename S>
+cudaError_t launch_copy_pad(const S* s_in, const S* e_in, const int32_t* d_in, int64_t n,
+                            int64_t n_pad, S* starts, S* ends, int32_t* data, uint32_t* perm,
+                            cudaStream_t st) {
+    if (n_pad <= 0) return cudaSuccess;
+    k_copy_pad<S><<<blocks_for(n_pad), kThreads, 0, st>>>(s_in, e_in, d_in, n, n_pad, starts, ends,
+                                                         data, perm);
+    return cudaGetLastError();
+}
+
+int pyramid_levels(int64_t n_pad, int64_t* sizes) {
+    // sizes[h] = padded length of level h; the top level must hold <= 32 nodes
+    sizes[0] = n_pad;
+    int H = 0;
+    int64_t m = n_pad;
+    while (m > 32 && H < kMaxLevels) {
+        const int64_t nodes = ceil_div(m, 32);
+        ++H;
+        sizes[H] = round_up(nodes, 32);
+        m = nodes;
+    }
+    return H;
+}
+
+template <typename S>
+cudaError_t launch_pyramid(const S* ends, const int64_t* sizes, int H, S* const* lvl,
+                           cudaStream_t st) {
+    const S* in = ends;
+    int64_t m = sizes[0];
+    for (int h = 1; h <= H; ++h) {
+        const int64_t nodes = ceil_div(m, 32);
+        k_level_max<S><<<blocks_for(sizes[h]), kThreads, 0, st>>>(in, nodes, sizes[h], lvl[h - 1]);
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+        in = lvl[h - 1];
+        m = nodes;
+    }
+    return cudaSuccess;
+}
+
+template <typename S>
+cudaError_t launch_branch(const S* ends, int64_t n, int64_t n_pad, Levels<S> L, int H,
+                          const int64_t* seg, int G, int32_t* branch, cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    k_branch<S><<<blocks_for(n_pad), kThreads, 0, st>>>(ends, n, n_pad, L, H, seg, G, branch);
+    return cudaGetLastError();
+}
+
+#define SIG_INST(S)                                                                              \
+    template cudaError_t launch_check_sorted<S>(const S*, const S*, int64_t, const int64_t*, int, \
+                                                int*, cudaStream_t);                             \
+    template int key_words<S>(int);                                                              \
+    template cudaError_t launch_make_keys<S>(const S*, const S*, int64_t, const int64_t*, int,    \
+                                             uint32_t* const*, uint32_t*, cudaStream_t);         \
+    template cudaError_t launch_decode<S>(const uint32_t* const*, const uint32_t*, const int32_t*, \
+                                          int64_t, int64_t, S*, S*, int32_t*, cudaStream_t);     \
+    template cudaError_t launch_copy_pad<S>(const S*, const S*, const int32_t*, int64_t, int64_t, \
+                                            S*, S*, int32_t*, uint32_t*, cudaStream_t);          \
+    template cudaError_t launch_pyramid<S>(const S*, const int64_t*, int, S* const*, cudaStream_t); \
+    template cudaError_t launch_branch<S>(const S*, int64_t, int64_t, Levels<S>, int,           \
+                                          const int64_t*, int, int32_t*, cudaStream_t);
+SIG_INST(int32_t)
+SIG_INST(int64_t)
+
+}  // namespace sig

@@ -1,0 +1,878 @@
+// si_capi.cu -- host runtime behind include/si_gpu/c_api.h.
+//
+// Owns the device index of a handle, its CUDA stream and a grow-only query
+// workspace, drives build() and the count -> scan -> emit query pipeline, and
+// chunks large result sets against a device output budget.  All device memory
+// goes through one allocator that honours a process-wide byte budget, so an
+// oversize request fails with SI_ERR_OOM instead of faulting.
+#include <algorithm>
+#include <atomic>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "si_gpu/c_api.h"
+#include "si_internal.cuh"
+#include "si_batched.cuh"
+
+namespace {
+
+thread_local std::string g_err;
+std::atomic<size_t> g_used{0};
+std::atomic<size_t> g_budget{0};
+
+int fail(int code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_err = buf;
+    return code;
+}
+
+#define SI_CK(call)                                                                          \
+    do {                                                                                     \
+        cudaError_t e_ = (call);                                                             \
+        if (e_ != cudaSuccess)                                                               \
+            return fail(SI_ERR_CUDA, "%s failed: %s", #call, cudaGetErrorString(e_));       \
+    } while (0)
+
+#define SI_TRY(call)                  \
+    do {                              \
+        int r_ = (call);              \
+        if (r_ != SI_OK) return r_;   \
+    } while (0)
+
+struct DevBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    DevBuf() = default;
+    DevBuf(const DevBuf&) = delete;
+    DevBuf& operator=(const DevBuf&) = delete;
+    ~DevBuf() { release(); }
+    void release() {
+        if (p) {
+            cudaFree(p);
+            g_used -= bytes;
+        }
+        p = nullptr;
+        bytes = 0;
+    }
+    // Grow-only: keeps the buffer when it is already large enough.
+    int reserve(size_t b) {
+        if (b <= bytes && p) return SI_OK;
+        release();
+        if (b == 0) b = 256;
+        b = (b + 255) & ~(size_t)255;
+        const size_t cap = g_budget.load();
+        if (cap && g_used.load() + b > cap)
+            return fail(SI_ERR_OOM, "device budget exceeded: %zu in use + %zu requested > %zu", g_used.load(),
+                        b, cap);
+        cudaError_t e = cudaMalloc(&p, b);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            p = nullptr;
+            return fail(SI_ERR_OOM, "cudaMalloc(%zu) failed: %s", b, cudaGetErrorString(e));
+        }
+        bytes = b;
+        g_used += b;
+        return SI_OK;
+    }
+    template <typename T>
+    T* as() const {
+        return static_cast<T*>(p);
+    }
+};
+
+}  // namespace
+
+struct gSuperIntervals {
+    int bits = 32;
+    int device = 0;
+    cudaStream_t st = nullptr;
+    // host staging in insertion order
+    std::vector<int32_t> hs32, he32;
+    std::vector<int64_t> hs64, he64;
+    std::vector<int32_t> hdata;
+    std::vector<int64_t> hseg;  // empty: one contig
+    bool built = false;
+    // device index
+    int64_t n = 0, n_pad = 0;
+    int G = 1, H = 0;
+    int64_t lvl_sizes[sig::kMaxLevels + 1] = {0};
+    DevBuf starts, ends, data, branch, seg, perm;
+    DevBuf lvl[sig::kMaxLevels];
+    int sort_passes = 0;
+    bool input_was_sorted = false;
+    // query workspace
+    DevBuf wq_s, wq_e, wq_c, w_counts, w_offsets, w_out, w_tmp, w_err;
+    sig::BatchedWorkspace bws;
+    // options
+    int path = SI_PATH_AUTO;
+    int ub_mode = SI_UB_BINARY;
+    size_t out_budget = (size_t)4 << 30;
+    // phase profiling (count, scan, emit, prepare)
+    bool prof = false;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    double phase_ms[4] = {0, 0, 0, 0};
+    int64_t phase_n[4] = {0, 0, 0, 0};
+};
+
+namespace {
+
+size_t staged(const gSuperIntervals* si) { return si->hdata.size(); }
+
+// Brackets one pipeline phase with CUDA events when profiling is on.
+struct PhaseTimer {
+    gSuperIntervals* si;
+    int phase;
+    cudaStream_t st;
+    PhaseTimer(gSuperIntervals* s, int p, cudaStream_t t) : si(s), phase(p), st(t) {
+        if (si->prof) cudaEventRecord(si->ev0, st);
+    }
+    ~PhaseTimer() {
+        if (!si->prof) return;
+        cudaEventRecord(si->ev1, st);
+        if (cudaEventSynchronize(si->ev1) == cudaSuccess) {
+            float ms = 0.f;
+            if (cudaEventElapsedTime(&ms, si->ev0, si->ev1) == cudaSuccess) {
+                si->phase_ms[phase] += ms;
+                si->phase_n[phase] += 1;
+            }
+        }
+    }
+};
+
+int set_dev(const gSuperIntervals* si) {
+    SI_CK(cudaSetDevice(si->device));
+    return SI_OK;
+}
+
+template <typename S>
+std::vector<S>& hs(gSuperIntervals* si);
+template <>
+std::vector<int32_t>& hs<int32_t>(gSuperIntervals* si) { return si->hs32; }
+template <>
+std::vector<int64_t>& hs<int64_t>(gSuperIntervals* si) { return si->hs64; }
+template <typename S>
+std::vector<S>& he(gSuperIntervals* si);
+template <>
+std::vector<int32_t>& he<int32_t>(gSuperIntervals* si) { return si->he32; }
+template <>
+std::vector<int64_t>& he<int64_t>(gSuperIntervals* si) { return si->he64; }
+
+template <typename S>
+int check_width(const gSuperIntervals* si) {
+    if (!si) return fail(SI_ERR_INVALID, "null handle");
+    if ((int)sizeof(S) * 8 != si->bits)
+        return fail(SI_ERR_INVALID, "coordinate width %d does not match the handle (%d)",
+                    (int)sizeof(S) * 8, si->bits);
+    return SI_OK;
+}
+
+template <typename S>
+int add_many(gSuperIntervals* si, const S* s, const S* e, const int32_t* v, size_t n) {
+    SI_TRY(check_width<S>(si));
+    if (n && (!s || !e)) return fail(SI_ERR_INVALID, "null interval arrays");
+    const size_t base = staged(si);
+    if (base + n >= (size_t)INT32_MAX - 64)
+        return fail(SI_ERR_TOO_LARGE, "more than 2^31-65 intervals in one handle");
+    hs<S>(si).insert(hs<S>(si).end(), s, s + n);
+    he<S>(si).insert(he<S>(si).end(), e, e + n);
+    if (v) {
+        si->hdata.insert(si->hdata.end(), v, v + n);
+    } else {
+        si->hdata.resize(base + n);
+        for (size_t i = 0; i < n; ++i) si->hdata[base + i] = (int32_t)(base + i);
+    }
+    if (!si->hseg.empty()) si->hseg.back() = (int64_t)staged(si);  // grow the last contig
+    si->built = false;
+    return SI_OK;
+}
+
+template <typename S>
+sig::MapView<S> view(const gSuperIntervals* si) {
+    sig::MapView<S> m;
+    m.starts = si->starts.as<S>();
+    m.ends = si->ends.as<S>();
+    m.branch = si->branch.as<int32_t>();
+    m.data = si->data.as<int32_t>();
+    m.seg = si->seg.as<int64_t>();
+    m.G = si->G;
+    m.n = si->n;
+    return m;
+}
+
+template <typename S>
+sig::Levels<S> levels(const gSuperIntervals* si) {
+    sig::Levels<S> L;
+    for (int h = 0; h < sig::kMaxLevels; ++h) L.p[h] = si->lvl[h].as<S>();
+    return L;
+}
+
+template <typename S>
+int build_impl(gSuperIntervals* si) {
+    SI_TRY(set_dev(si));
+    cudaStream_t st = si->st;
+    const int64_t n = (int64_t)staged(si);
+    std::vector<int64_t> segv = si->hseg;
+    if (segv.empty()) segv = {0, n};
+    const int G = (int)segv.size() - 1;
+    if (G < 1 || segv[0] != 0 || segv[G] != n)
+        return fail(SI_ERR_INVALID, "contig offsets do not cover the %lld staged intervals", (long long)n);
+    for (int g = 0; g < G; ++g)
+        if (segv[g + 1] < segv[g]) return fail(SI_ERR_INVALID, "contig offsets decrease at %d", g);
+    si->built = false;
+    si->n = n;
+    si->G = G;
+    si->n_pad = sig::round_up(std::max<int64_t>(n, 1), 32);
+    const int64_t n_pad = si->n_pad;
+    SI_TRY(si->starts.reserve(sizeof(S) * n_pad));
+    SI_TRY(si->ends.reserve(sizeof(S) * n_pad));
+    SI_TRY(si->data.reserve(sizeof(int32_t) * n_pad));
+    SI_TRY(si->branch.reserve(sizeof(int32_t) * n_pad));
+    SI_TRY(si->perm.reserve(sizeof(uint32_t) * n_pad));
+    SI_TRY(si->seg.reserve(sizeof(int64_t) * (G + 1)));
+    SI_CK(cudaMemcpyAsync(si->seg.p, segv.data(), sizeof(int64_t) * (G + 1), cudaMemcpyHostToDevice, st));
+    si->H = sig::pyramid_levels(n_pad, si->lvl_sizes);
+    for (int h = 1; h <= si->H; ++h) SI_TRY(si->lvl[h - 1].reserve(sizeof(S) * si->lvl_sizes[h]));
+    if (n == 0) {
+        SI_CK(cudaStreamSynchronize(st));
+        si->built = true;
+        return SI_OK;
+    }
+    DevBuf s_in, e_in, d_in, flag;
+    SI_TRY(s_in.reserve(sizeof(S) * n));
+    SI_TRY(e_in.reserve(sizeof(S) * n));
+    SI_TRY(d_in.reserve(sizeof(int32_t) * n));
+    SI_TRY(flag.reserve(sizeof(int)));
+    SI_CK(cudaMemcpyAsync(s_in.p, hs<S>(si).data(), sizeof(S) * n, cudaMemcpyHostToDevice, st));
+    SI_CK(cudaMemcpyAsync(e_in.p, he<S>(si).data(), sizeof(S) * n, cudaMemcpyHostToDevice, st));
+    SI_CK(cudaMemcpyAsync(d_in.p, si->hdata.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice, st));
+    SI_CK(sig::launch_check_sorted<S>(s_in.as<S>(), e_in.as<S>(), n, si->seg.as<int64_t>(), G,
+                                      flag.as<int>(), st));
+    int unsorted = 0;
+    SI_CK(cudaMemcpyAsync(&unsorted, flag.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+    SI_CK(cudaStreamSynchronize(st));
+    si->input_was_sorted = !unsorted;
+    si->sort_passes = 0;
+    if (!unsorted) {
+        SI_CK(sig::launch_copy_pad<S>(s_in.as<S>(), e_in.as<S>(), d_in.as<int32_t>(), n, n_pad,
+                                      si->starts.as<S>(), si->ends.as<S>(), si->data.as<int32_t>(),
+                                      si->perm.as<uint32_t>(), st));
+    } else {
+        const int K = sig::key_words<S>(G);
+        DevBuf kw[sig::kMaxKeyWords], kalt[sig::kMaxKeyWords], pay, palt, tmp;
+        uint32_t* kp[sig::kMaxKeyWords];
+        uint32_t* ka[sig::kMaxKeyWords];
+        for (int k = 0; k < K; ++k) {
+            SI_TRY(kw[k].reserve(sizeof(uint32_t) * n));
+            SI_TRY(kalt[k].reserve(sizeof(uint32_t) * n));
+            kp[k] = kw[k].as<uint32_t>();
+            ka[k] = kalt[k].as<uint32_t>();
+        }
+        SI_TRY(pay.reserve(sizeof(uint32_t) * n));
+        SI_TRY(palt.reserve(sizeof(uint32_t) * n));
+        const size_t tb = sig::radix_temp_bytes(n, K);
+        SI_TRY(tmp.reserve(tb));
+        SI_CK(sig::launch_make_keys<S>(s_in.as<S>(), e_in.as<S>(), n, si->seg.as<int64_t>(), G, kp,
+                                       pay.as<uint32_t>(), st));
+        bool in_alt = false;
+        SI_CK(sig::radix_sort(kp, ka, pay.as<uint32_t>(), palt.as<uint32_t>(), K, n, tmp.p, tb,
+                              &in_alt, &si->sort_passes, st));
+        uint32_t* const* res_k = in_alt ? ka : kp;
+        const uint32_t* res_p = in_alt ? palt.as<uint32_t>() : pay.as<uint32_t>();
+        SI_CK(sig::launch_decode<S>(res_k, res_p, d_in.as<int32_t>(), n, n_pad, si->starts.as<S>(),
+                                    si->ends.as<S>(), si->data.as<int32_t>(), st));
+        SI_CK(cudaMemcpyAsync(si->perm.p, res_p, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, st));
+        SI_CK(cudaStreamSynchronize(st));  // temps are released on scope exit
+    }
+    const S* ends = si->ends.as<S>();
+    S* lp[sig::kMaxLevels];
+    for (int h = 0; h < sig::kMaxLevels; ++h) lp[h] = si->lvl[h].as<S>();
+    SI_CK(sig::launch_pyramid<S>(ends, si->lvl_sizes, si->H, lp, st));
+    SI_CK(sig::launch_branch<S>(ends, n, n_pad, levels<S>(si), si->H, si->seg.as<int64_t>(), G,
+                                si->branch.as<int32_t>(), st));
+    SI_TRY(sig::batched_prepare<S>(si->bws, view<S>(si), levels<S>(si), si->H, si->lvl_sizes,
+                                   si->ub_mode, st));
+    SI_CK(cudaStreamSynchronize(st));
+    SI_CK(cudaGetLastError());
+    si->built = true;
+    return SI_OK;
+}
+
+int check_built(const gSuperIntervals* si) {
+    if (!si) return fail(SI_ERR_INVALID, "null handle");
+    if (!si->built) return fail(SI_ERR_NOT_BUILT, "index not built (call indexSuperIntervalsGpu after adding)");
+    return SI_OK;
+}
+
+int read_dev_err(gSuperIntervals* si) {
+    int e = 0;
+    SI_CK(cudaMemcpyAsync(&e, si->w_err.p, sizeof(int), cudaMemcpyDeviceToHost, si->st));
+    SI_CK(cudaStreamSynchronize(si->st));
+    if (e == sig::kDevBadContig) return fail(SI_ERR_INVALID, "a query names a contig outside [0, %d)", si->G);
+    if (e == sig::kDevOverflow) return fail(SI_ERR_CUDA, "internal: emit overran its offsets");
+    if (e != 0) return fail(SI_ERR_CUDA, "device error word %d", e);
+    return SI_OK;
+}
+
+bool use_batched(const gSuperIntervals* si, int64_t nq) {
+    if (si->path == SI_PATH_PLAIN) return false;
+    if (si->path == SI_PATH_BATCHED) return true;
+    return nq >= 4096 && si->n >= 4096;
+}
+
+// count into d_counts (device) for device-resident queries
+template <typename S>
+int run_count(gSuperIntervals* si, const sig::QueryBatch& q, uint32_t* d_counts, cudaStream_t st) {
+    SI_TRY(si->w_err.reserve(sizeof(int)));
+    SI_CK(cudaMemsetAsync(si->w_err.p, 0, sizeof(int), st));
+    if (si->n == 0) {
+        SI_CK(cudaMemsetAsync(d_counts, 0, sizeof(uint32_t) * std::max<int64_t>(q.nq, 1), st));
+        return SI_OK;
+    }
+    PhaseTimer pt(si, 0, st);
+    if (use_batched(si, q.nq)) {
+        SI_TRY(sig::batched_count<S>(si->bws, view<S>(si), levels<S>(si), si->H, q, d_counts,
+                                     si->w_err.as<int>(), si->ub_mode, st));
+    } else {
+        SI_CK(sig::launch_count_plain<S>(view<S>(si), q, d_counts, si->w_err.as<int>(), st));
+    }
+    return SI_OK;
+}
+
+template <typename S>
+int run_emit(gSuperIntervals* si, const sig::QueryBatch& q, const int64_t* d_offsets, int64_t out_base,
+             int order, bool values, int32_t* d_out, cudaStream_t st) {
+    if (si->n == 0 || q.nq == 0) return SI_OK;
+    PhaseTimer pt(si, 2, st);
+    if (use_batched(si, q.nq)) {
+        SI_TRY(sig::batched_emit<S>(si->bws, view<S>(si), levels<S>(si), si->H, q, d_offsets, out_base,
+                                    order, values, d_out, si->w_err.as<int>(), si->ub_mode, st));
+    } else {
+        SI_CK(sig::launch_emit_plain<S>(view<S>(si), q, d_offsets, out_base, order, values, d_out,
+                                        si->w_err.as<int>(), st));
+    }
+    return SI_OK;
+}
+
+// device-resident queries and outputs
+template <typename S>
+int search_device(gSuperIntervals* si, const sig::QueryBatch& q, int order, bool values,
+                  int64_t* d_offsets, int32_t* d_out, size_t cap, size_t* total, cudaStream_t st) {
+    SI_TRY(check_built(si));
+    SI_TRY(set_dev(si));
+    SI_TRY(si->w_counts.reserve(sizeof(uint32_t) * std::max<int64_t>(q.nq, 1)));
+    SI_TRY(si->w_tmp.reserve(sig::scan_temp_bytes(q.nq)));
+    SI_TRY(run_count<S>(si, q, si->w_counts.as<uint32_t>(), st));
+    {
+        PhaseTimer pt(si, 1, st);
+        SI_CK(sig::exclusive_scan_u32_to_i64(si->w_counts.as<uint32_t>(), d_offsets, q.nq, si->w_tmp.p, st));
+    }
+    int64_t P = 0;
+    SI_CK(cudaMemcpyAsync(&P, d_offsets + q.nq, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+    SI_CK(cudaStreamSynchronize(st));
+    if (total) *total = (size_t)P;
+    if ((size_t)P > cap) return fail(SI_ERR_CAPACITY, "output needs %lld values, capacity %zu", (long long)P, cap);
+    SI_TRY(run_emit<S>(si, q, d_offsets, 0, order, values, d_out, st));
+    return read_dev_err(si);
+}
+
+template <typename S>
+int upload_queries(gSuperIntervals* si, const S* qs, const S* qe, const int32_t* qc, size_t nq,
+                   sig::QueryBatch& q) {
+    if (nq && (!qs || !qe)) return fail(SI_ERR_INVALID, "null query arrays");
+    SI_TRY(si->wq_s.reserve(sizeof(S) * std::max<size_t>(nq, 1)));
+    SI_TRY(si->wq_e.reserve(sizeof(S) * std::max<size_t>(nq, 1)));
+    if (nq) {
+        SI_CK(cudaMemcpyAsync(si->wq_s.p, qs, sizeof(S) * nq, cudaMemcpyHostToDevice, si->st));
+        SI_CK(cudaMemcpyAsync(si->wq_e.p, qe, sizeof(S) * nq, cudaMemcpyHostToDevice, si->st));
+    }
+    q.qs = si->wq_s.p;
+    q.qe = si->wq_e.p;
+    q.qc = nullptr;
+    if (qc) {
+        for (size_t i = 0; i < nq; ++i)
+            if (qc[i] < 0 || qc[i] >= si->G)
+                return fail(SI_ERR_INVALID, "query %zu names contig %d outside [0, %d)", i, qc[i], si->G);
+        SI_TRY(si->wq_c.reserve(sizeof(int32_t) * std::max<size_t>(nq, 1)));
+        if (nq) SI_CK(cudaMemcpyAsync(si->wq_c.p, qc, sizeof(int32_t) * nq, cudaMemcpyHostToDevice, si->st));
+        q.qc = si->wq_c.as<int32_t>();
+    }
+    q.nq = (int64_t)nq;
+    return SI_OK;
+}
+
+// host queries -> host CSR; result grown when `grow` is set, else caller buffers
+template <typename S>
+int search_host(gSuperIntervals* si, const S* qs, const S* qe, const int32_t* qc, size_t nq, int order,
+                bool values, cCsrResult* grow, int64_t* h_off, int32_t* h_out, size_t cap, size_t* total) {
+    SI_TRY(check_width<S>(si));
+    SI_TRY(check_built(si));
+    SI_TRY(set_dev(si));
+    cudaStream_t st = si->st;
+    if (grow) {
+        if (grow->offsets_capacity < nq + 1) {
+            int64_t* p = (int64_t*)realloc(grow->offsets, sizeof(int64_t) * (nq + 1));
+            if (!p) return fail(SI_ERR_OOM, "host allocation of %zu offsets failed", nq + 1);
+            grow->offsets = p;
+            grow->offsets_capacity = nq + 1;
+        }
+        h_off = grow->offsets;
+        grow->n_queries = nq;
+        grow->size = 0;
+    }
+    sig::QueryBatch q;
+    SI_TRY(upload_queries<S>(si, qs, qe, qc, nq, q));
+    SI_TRY(si->w_counts.reserve(sizeof(uint32_t) * std::max<size_t>(nq, 1)));
+    SI_TRY(si->w_offsets.reserve(sizeof(int64_t) * (nq + 1)));
+    SI_TRY(si->w_tmp.reserve(sig::scan_temp_bytes((int64_t)nq)));
+    SI_TRY(run_count<S>(si, q, si->w_counts.as<uint32_t>(), st));
+    int64_t* d_off = si->w_offsets.as<int64_t>();
+    {
+        PhaseTimer pt(si, 1, st);
+        SI_CK(sig::exclusive_scan_u32_to_i64(si->w_counts.as<uint32_t>(), d_off, (int64_t)nq, si->w_tmp.p, st));
+    }
+    SI_CK(cudaMemcpyAsync(h_off, d_off, sizeof(int64_t) * (nq + 1), cudaMemcpyDeviceToHost, st));
+    SI_CK(cudaStreamSynchronize(st));
+    const int64_t P = h_off[nq];
+    if (total) *total = (size_t)P;
+    if (grow) {
+        if (grow->capacity < (size_t)P) {
+            int32_t* p = (int32_t*)realloc(grow->values, sizeof(int32_t) * std::max<int64_t>(P, 1));
+            if (!p) return fail(SI_ERR_OOM, "host allocation of %lld values failed", (long long)P);
+            grow->values = p;
+            grow->capacity = (size_t)P;
+        }
+        h_out = grow->values;
+        grow->size = (size_t)P;
+    } else if ((size_t)P > cap) {
+        return fail(SI_ERR_CAPACITY, "output needs %lld values, capacity %zu", (long long)P, cap);
+    }
+    if (P == 0) return read_dev_err(si);
+    // chunked emit against the device output budget
+    const int64_t budget = std::max<int64_t>((int64_t)(si->out_budget / sizeof(int32_t)), 1 << 20);
+    const int64_t buf = std::min<int64_t>(P, budget);
+    size_t qa = 0;
+    while (qa < nq) {
+        size_t qb = qa;
+        // largest qb with off[qb] - off[qa] <= buf (at least one query)
+        const int64_t limit = h_off[qa] + buf;
+        size_t lo = qa + 1, hi = nq;
+        while (lo < hi) {
+            size_t mid = lo + (hi - lo + 1) / 2;
+            if (h_off[mid] <= limit) lo = mid;
+            else hi = mid - 1;
+        }
+        qb = lo;
+        const int64_t need = h_off[qb] - h_off[qa];
+        SI_TRY(si->w_out.reserve(sizeof(int32_t) * std::max<int64_t>(need, 1)));
+        sig::QueryBatch sub = q;
+        sub.qs = static_cast<const S*>(q.qs) + qa;
+        sub.qe = static_cast<const S*>(q.qe) + qa;
+        sub.qc = q.qc ? q.qc + qa : nullptr;
+        sub.nq = (int64_t)(qb - qa);
+        SI_TRY(run_emit<S>(si, sub, d_off + qa, h_off[qa], order, values, si->w_out.as<int32_t>(), st));
+        if (need)
+            SI_CK(cudaMemcpyAsync(h_out + h_off[qa], si->w_out.p, sizeof(int32_t) * need,
+                                  cudaMemcpyDeviceToHost, st));
+        SI_CK(cudaStreamSynchronize(st));
+        qa = qb;
+    }
+    return read_dev_err(si);
+}
+
+template <typename S>
+int count_host(gSuperIntervals* si, const S* qs, const S* qe, const int32_t* qc, size_t nq, uint32_t* counts) {
+    SI_TRY(check_width<S>(si));
+    SI_TRY(check_built(si));
+    SI_TRY(set_dev(si));
+    if (nq && !counts) return fail(SI_ERR_INVALID, "null output");
+    sig::QueryBatch q;
+    SI_TRY(upload_queries<S>(si, qs, qe, qc, nq, q));
+    SI_TRY(si->w_counts.reserve(sizeof(uint32_t) * std::max<size_t>(nq, 1)));
+    SI_TRY(run_count<S>(si, q, si->w_counts.as<uint32_t>(), si->st));
+    if (nq) SI_CK(cudaMemcpyAsync(counts, si->w_counts.p, sizeof(uint32_t) * nq, cudaMemcpyDeviceToHost, si->st));
+    return read_dev_err(si);
+}
+
+template <typename S>
+int any_host(gSuperIntervals* si, const S* qs, const S* qe, const int32_t* qc, size_t nq, uint8_t* out) {
+    SI_TRY(check_width<S>(si));
+    SI_TRY(check_built(si));
+    SI_TRY(set_dev(si));
+    if (nq && !out) return fail(SI_ERR_INVALID, "null output");
+    sig::QueryBatch q;
+    SI_TRY(upload_queries<S>(si, qs, qe, qc, nq, q));
+    SI_TRY(si->w_err.reserve(sizeof(int)));
+    SI_CK(cudaMemsetAsync(si->w_err.p, 0, sizeof(int), si->st));
+    if (si->n == 0) {
+        memset(out, 0, nq);
+        return SI_OK;
+    }
+    SI_TRY(si->w_out.reserve(std::max<size_t>(nq, 1)));
+    SI_CK(sig::launch_any_plain<S>(view<S>(si), q, si->w_out.as<uint8_t>(), si->w_err.as<int>(), si->st));
+    if (nq) SI_CK(cudaMemcpyAsync(out, si->w_out.p, nq, cudaMemcpyDeviceToHost, si->st));
+    return read_dev_err(si);
+}
+
+template <typename S>
+int get_arrays(const gSuperIntervals* si, S* s, S* e, int32_t* d, int64_t* br) {
+    SI_TRY(check_built(si));
+    SI_TRY(set_dev(si));
+    const int64_t n = si->n;
+    if (n == 0) return SI_OK;
+    cudaStream_t st = si->st;
+    if (s) SI_CK(cudaMemcpyAsync(s, si->starts.p, sizeof(S) * n, cudaMemcpyDeviceToHost, st));
+    if (e) SI_CK(cudaMemcpyAsync(e, si->ends.p, sizeof(S) * n, cudaMemcpyDeviceToHost, st));
+    if (d) SI_CK(cudaMemcpyAsync(d, si->data.p, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, st));
+    std::vector<int32_t> b32;
+    if (br) {
+        b32.resize(n);
+        SI_CK(cudaMemcpyAsync(b32.data(), si->branch.p, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, st));
+    }
+    SI_CK(cudaStreamSynchronize(st));
+    if (br) {
+        std::vector<int64_t> segv = si->hseg;
+        if (segv.empty()) segv = {0, n};
+        for (int g = 0; g < si->G; ++g)
+            for (int64_t i = segv[g]; i < segv[g + 1]; ++i) br[i] = b32[i] < 0 ? -1 : (int64_t)b32[i] - segv[g];
+    }
+    return SI_OK;
+}
+
+}  // namespace
+
+// =====================================================================================
+extern "C" {
+
+int createSuperIntervalsGpu(gSuperIntervals** out, int coord_bits, int device) {
+    if (!out) return fail(SI_ERR_INVALID, "null output handle");
+    *out = nullptr;
+    if (coord_bits != 32 && coord_bits != 64) return fail(SI_ERR_INVALID, "coord_bits must be 32 or 64");
+    int ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        return fail(SI_ERR_CUDA, "no CUDA device: %s", cudaGetErrorString(e));
+    }
+    if (device < 0 || device >= ndev) return fail(SI_ERR_INVALID, "device %d outside [0, %d)", device, ndev);
+    SI_CK(cudaSetDevice(device));
+    auto* si = new gSuperIntervals();
+    si->bits = coord_bits;
+    si->device = device;
+    e = cudaStreamCreateWithFlags(&si->st, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        delete si;
+        return fail(SI_ERR_CUDA, "cudaStreamCreate: %s", cudaGetErrorString(e));
+    }
+    *out = si;
+    return SI_OK;
+}
+
+void destroySuperIntervalsGpu(gSuperIntervals* si) {
+    if (!si) return;
+    cudaSetDevice(si->device);
+    cudaStreamSynchronize(si->st);
+    if (si->ev0) cudaEventDestroy(si->ev0);
+    if (si->ev1) cudaEventDestroy(si->ev1);
+    cudaStream_t st = si->st;
+    delete si;  // releases device buffers
+    cudaStreamDestroy(st);
+}
+
+int clearSuperIntervalsGpu(gSuperIntervals* si) {
+    if (!si) return fail(SI_ERR_INVALID, "null handle");
+    si->hs32.clear(); si->he32.clear(); si->hs64.clear(); si->he64.clear(); si->hdata.clear();
+    si->hseg.clear();
+    si->built = false;
+    si->n = 0;
+    return SI_OK;
+}
+
+int reserveSuperIntervalsGpu(gSuperIntervals* si, size_t n) {
+    if (!si) return fail(SI_ERR_INVALID, "null handle");
+    if (si->bits == 32) { si->hs32.reserve(n); si->he32.reserve(n); }
+    else { si->hs64.reserve(n); si->he64.reserve(n); }
+    si->hdata.reserve(n);
+    return SI_OK;
+}
+
+int addIntervalGpu(gSuperIntervals* si, int32_t start, int32_t end, int32_t value) {
+    return add_many<int32_t>(si, &start, &end, &value, 1);
+}
+int addIntervalGpu_i64(gSuperIntervals* si, int64_t start, int64_t end, int32_t value) {
+    return add_many<int64_t>(si, &start, &end, &value, 1);
+}
+int addIntervalsGpu(gSuperIntervals* si, const int32_t* s, const int32_t* e, const int32_t* v, size_t n) {
+    return add_many<int32_t>(si, s, e, v, n);
+}
+int addIntervalsGpu_i64(gSuperIntervals* si, const int64_t* s, const int64_t* e, const int32_t* v, size_t n) {
+    return add_many<int64_t>(si, s, e, v, n);
+}
+
+int setContigsGpu(gSuperIntervals* si, size_t n_contigs, const int64_t* offsets) {
+    if (!si) return fail(SI_ERR_INVALID, "null handle");
+    if (n_contigs == 0 || !offsets) return fail(SI_ERR_INVALID, "need at least one contig");
+    if (offsets[0] != 0 || offsets[n_contigs] != (int64_t)staged(si))
+        return fail(SI_ERR_INVALID, "contig offsets must run from 0 to the staged count %zu", staged(si));
+    for (size_t g = 0; g < n_contigs; ++g)
+        if (offsets[g + 1] < offsets[g]) return fail(SI_ERR_INVALID, "contig offsets decrease at %zu", g);
+    if (n_contigs >= (size_t)INT32_MAX) return fail(SI_ERR_INVALID, "too many contigs");
+    si->hseg.assign(offsets, offsets + n_contigs + 1);
+    si->built = false;
+    return SI_OK;
+}
+
+size_t sizeSuperIntervalsGpu(const gSuperIntervals* si) { return si ? staged(si) : 0; }
+size_t numContigsGpu(const gSuperIntervals* si) {
+    return si ? (si->hseg.empty() ? 1 : si->hseg.size() - 1) : 0;
+}
+
+int indexSuperIntervalsGpu(gSuperIntervals* si) {
+    if (!si) return fail(SI_ERR_INVALID, "null handle");
+    return si->bits == 64 ? build_impl<int64_t>(si) : build_impl<int32_t>(si);
+}
+
+int getIndexArraysGpu(const gSuperIntervals* si, void* s, void* e, int32_t* d, int64_t* br) {
+    if (!si) return fail(SI_ERR_INVALID, "null handle");
+    if (si->bits == 64) return get_arrays<int64_t>(si, (int64_t*)s, (int64_t*)e, d, br);
+    return get_arrays<int32_t>(si, (int32_t*)s, (int32_t*)e, d, br);
+}
+
+int setQueryPathGpu(gSuperIntervals* si, int path) {
+    if (!si) return fail(SI_ERR_INVALID, "null handle");
+    if (path < SI_PATH_AUTO || path > SI_PATH_BATCHED) return fail(SI_ERR_INVALID, "unknown path %d", path);
+    si->path = path;
+    return SI_OK;
+}
+
+int setUpperBoundModeGpu(gSuperIntervals* si, int mode) {
+    if (!si) return fail(SI_ERR_INVALID, "null handle");
+    if (mode < SI_UB_BINARY || mode > SI_UB_LEARNED) return fail(SI_ERR_INVALID, "unknown mode %d", mode);
+    si->ub_mode = mode;
+    if (si->built) {
+        SI_TRY(set_dev(si));
+        int r = si->bits == 64
+                    ? sig::batched_prepare<int64_t>(si->bws, view<int64_t>(si), levels<int64_t>(si), si->H,
+                                                    si->lvl_sizes, mode, si->st)
+                    : sig::batched_prepare<int32_t>(si->bws, view<int32_t>(si), levels<int32_t>(si), si->H,
+                                                    si->lvl_sizes, mode, si->st);
+        if (r != SI_OK) return r;
+        SI_CK(cudaStreamSynchronize(si->st));
+    }
+    return SI_OK;
+}
+
+int setOutputBudgetGpu(gSuperIntervals* si, size_t bytes) {
+    if (!si) return fail(SI_ERR_INVALID, "null handle");
+    si->out_budget = std::max<size_t>(bytes, 1 << 20);
+    return SI_OK;
+}
+
+int setProfilingGpu(gSuperIntervals* si, int on) {
+    if (!si) return fail(SI_ERR_INVALID, "null handle");
+    SI_TRY(set_dev(si));
+    if (on && !si->ev0) {
+        SI_CK(cudaEventCreate(&si->ev0));
+        SI_CK(cudaEventCreate(&si->ev1));
+    }
+    si->prof = on != 0;
+    for (int k = 0; k < 4; ++k) {
+        si->phase_ms[k] = 0;
+        si->phase_n[k] = 0;
+    }
+    return SI_OK;
+}
+
+int getPhaseTimesGpu(const gSuperIntervals* si, double* ms, int64_t* calls) {
+    if (!si) return fail(SI_ERR_INVALID, "null handle");
+    for (int k = 0; k < 4; ++k) {
+        if (ms) ms[k] = si->phase_ms[k];
+        if (calls) calls[k] = si->phase_n[k];
+    }
+    return SI_OK;
+}
+
+int setDeviceBudgetGpu(size_t bytes) {
+    g_budget = bytes;
+    return SI_OK;
+}
+size_t deviceBytesInUseGpu(void) { return g_used.load(); }
+
+int countOverlapsBatchGpu(gSuperIntervals* si, const int32_t* qs, const int32_t* qe, const int32_t* qc,
+                          size_t nq, uint32_t* counts) {
+    return count_host<int32_t>(si, qs, qe, qc, nq, counts);
+}
+int countOverlapsBatchGpu_i64(gSuperIntervals* si, const int64_t* qs, const int64_t* qe, const int32_t* qc,
+                              size_t nq, uint32_t* counts) {
+    return count_host<int64_t>(si, qs, qe, qc, nq, counts);
+}
+int anyOverlapsBatchGpu(gSuperIntervals* si, const int32_t* qs, const int32_t* qe, const int32_t* qc,
+                        size_t nq, uint8_t* out) {
+    return any_host<int32_t>(si, qs, qe, qc, nq, out);
+}
+int anyOverlapsBatchGpu_i64(gSuperIntervals* si, const int64_t* qs, const int64_t* qe, const int32_t* qc,
+                            size_t nq, uint8_t* out) {
+    return any_host<int64_t>(si, qs, qe, qc, nq, out);
+}
+int searchIdxsBatchGpu(gSuperIntervals* si, const int32_t* qs, const int32_t* qe, const int32_t* qc,
+                       size_t nq, int order, cCsrResult* out) {
+    if (!out) return fail(SI_ERR_INVALID, "null result");
+    return search_host<int32_t>(si, qs, qe, qc, nq, order, false, out, nullptr, nullptr, 0, nullptr);
+}
+int searchIdxsBatchGpu_i64(gSuperIntervals* si, const int64_t* qs, const int64_t* qe, const int32_t* qc,
+                           size_t nq, int order, cCsrResult* out) {
+    if (!out) return fail(SI_ERR_INVALID, "null result");
+    return search_host<int64_t>(si, qs, qe, qc, nq, order, false, out, nullptr, nullptr, 0, nullptr);
+}
+int searchValuesBatchGpu(gSuperIntervals* si, const int32_t* qs, const int32_t* qe, const int32_t* qc,
+                         size_t nq, cCsrResult* out) {
+    if (!out) return fail(SI_ERR_INVALID, "null result");
+    return search_host<int32_t>(si, qs, qe, qc, nq, SI_ORDER_DESC, true, out, nullptr, nullptr, 0, nullptr);
+}
+int searchValuesBatchGpu_i64(gSuperIntervals* si, const int64_t* qs, const int64_t* qe, const int32_t* qc,
+                             size_t nq, cCsrResult* out) {
+    if (!out) return fail(SI_ERR_INVALID, "null result");
+    return search_host<int64_t>(si, qs, qe, qc, nq, SI_ORDER_DESC, true, out, nullptr, nullptr, 0, nullptr);
+}
+int searchBatchIntoGpu(gSuperIntervals* si, const void* qs, const void* qe, const int32_t* qc, size_t nq,
+                       int order, int values_not_idxs, int64_t* offsets, int32_t* values, size_t capacity,
+                       size_t* total) {
+    if (!si || !offsets) return fail(SI_ERR_INVALID, "null handle or offsets");
+    if (order != SI_ORDER_IDXS_CPP && order != SI_ORDER_DESC) return fail(SI_ERR_INVALID, "unknown order");
+    if (si->bits == 64)
+        return search_host<int64_t>(si, (const int64_t*)qs, (const int64_t*)qe, qc, nq, order, values_not_idxs != 0,
+                                    nullptr, offsets, values, capacity, total);
+    return search_host<int32_t>(si, (const int32_t*)qs, (const int32_t*)qe, qc, nq, order, values_not_idxs != 0,
+                                nullptr, offsets, values, capacity, total);
+}
+
+int countOverlapsDeviceGpu(gSuperIntervals* si, const void* d_qs, const void* d_qe, const int32_t* d_qc,
+                           size_t nq, uint32_t* d_counts, void* stream) {
+    SI_TRY(check_built(si));
+    SI_TRY(set_dev(si));
+    cudaStream_t st = stream ? (cudaStream_t)stream : si->st;
+    sig::QueryBatch q{d_qs, d_qe, d_qc, (int64_t)nq};
+    if (si->bits == 64) SI_TRY(run_count<int64_t>(si, q, d_counts, st));
+    else SI_TRY(run_count<int32_t>(si, q, d_counts, st));
+    return SI_OK;
+}
+
+int searchDeviceGpu(gSuperIntervals* si, const void* d_qs, const void* d_qe, const int32_t* d_qc, size_t nq,
+                    int order, int values_not_idxs, int64_t* d_offsets, int32_t* d_values, size_t capacity,
+                    size_t* total, void* stream) {
+    if (!si || !d_offsets) return fail(SI_ERR_INVALID, "null handle or offsets");
+    if (order != SI_ORDER_IDXS_CPP && order != SI_ORDER_DESC) return fail(SI_ERR_INVALID, "unknown order");
+    cudaStream_t st = stream ? (cudaStream_t)stream : si->st;
+    sig::QueryBatch q{d_qs, d_qe, d_qc, (int64_t)nq};
+    if (si->bits == 64)
+        return search_device<int64_t>(si, q, order, values_not_idxs != 0, d_offsets, d_values, capacity, total, st);
+    return search_device<int32_t>(si, q, order, values_not_idxs != 0, d_offsets, d_values, capacity, total, st);
+}
+
+cCsrResult createCsrResult(void) {
+    cCsrResult r;
+    memset(&r, 0, sizeof(r));
+    return r;
+}
+void clearCsrResult(cCsrResult* r) {
+    if (r) { r->size = 0; r->n_queries = 0; }
+}
+void destroyCsrResult(cCsrResult* r) {
+    if (!r) return;
+    free(r->offsets);
+    free(r->values);
+    memset(r, 0, sizeof(*r));
+}
+
+const char* lastErrorGpu(void) { return g_err.c_str(); }
+void* getStreamGpu(gSuperIntervals* si) { return si ? (void*)si->st : nullptr; }
+
+int deviceCountGpu(int* count) {
+    if (!count) return fail(SI_ERR_INVALID, "null output");
+    cudaError_t e = cudaGetDeviceCount(count);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        *count = 0;
+        return fail(SI_ERR_CUDA, "cudaGetDeviceCount: %s", cudaGetErrorString(e));
+    }
+    return SI_OK;
+}
+int deviceMallocGpu(void** ptr, size_t bytes) {
+    if (!ptr) return fail(SI_ERR_INVALID, "null output");
+    const size_t cap = g_budget.load();
+    if (cap && g_used.load() + bytes > cap) return fail(SI_ERR_OOM, "device budget exceeded");
+    cudaError_t e = cudaMalloc(ptr, std::max<size_t>(bytes, 1));
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        *ptr = nullptr;
+        return fail(SI_ERR_OOM, "cudaMalloc(%zu): %s", bytes, cudaGetErrorString(e));
+    }
+    return SI_OK;
+}
+int deviceFreeGpu(void* ptr) {
+    SI_CK(cudaFree(ptr));
+    return SI_OK;
+}
+int hostMallocPinnedGpu(void** ptr, size_t bytes) {
+    if (!ptr) return fail(SI_ERR_INVALID, "null output");
+    cudaError_t e = cudaMallocHost(ptr, std::max<size_t>(bytes, 1));
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        *ptr = nullptr;
+        return fail(SI_ERR_OOM, "cudaMallocHost(%zu): %s", bytes, cudaGetErrorString(e));
+    }
+    return SI_OK;
+}
+int hostFreePinnedGpu(void* ptr) {
+    SI_CK(cudaFreeHost(ptr));
+    return SI_OK;
+}
+int memcpyGpu(void* dst, const void* src, size_t bytes, void* stream) {
+    SI_CK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDefault, (cudaStream_t)stream));
+    return SI_OK;
+}
+int streamSynchronizeGpu(void* stream) {
+    SI_CK(cudaStreamSynchronize((cudaStream_t)stream));
+    return SI_OK;
+}
+int eventCreateGpu(void** ev) {
+    SI_CK(cudaEventCreate((cudaEvent_t*)ev));
+    return SI_OK;
+}
+int eventDestroyGpu(void* ev) {
+    SI_CK(cudaEventDestroy((cudaEvent_t)ev));
+    return SI_OK;
+}
+int eventRecordGpu(void* ev, void* stream) {
+    SI_CK(cudaEventRecord((cudaEvent_t)ev, (cudaStream_t)stream));
+    return SI_OK;
+}
+int eventElapsedMsGpu(void* a, void* b, float* ms) {
+    SI_CK(cudaEventElapsedTime(ms, (cudaEvent_t)a, (cudaEvent_t)b));
+    return SI_OK;
+}
+int flushL2Gpu(void* stream) {
+    static std::mutex mu;
+    static void* buf[64] = {nullptr};
+    static int flip = 0;
+    int dev = 0;
+    SI_CK(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64) return fail(SI_ERR_INVALID, "device id");
+    const size_t bytes = (size_t)512 << 20;  // 4x the 129 MB L2
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        if (!buf[dev]) SI_CK(cudaMalloc(&buf[dev], bytes));
+        flip ^= 1;
+    }
+    SI_CK(cudaMemsetAsync(buf[dev], flip, bytes, (cudaStream_t)stream));
+    return SI_OK;
+}
+
+}  // extern "C"

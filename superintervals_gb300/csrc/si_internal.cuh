@@ -1,0 +1,160 @@
+// si_internal.cuh -- shared device/host helpers of the GB300 overlap-query library.
+//
+// Index layout in HBM (one handle = one set of per-contig maps):
+//   starts[n_pad], ends[n_pad]   coordinate type S (int32 or int64), sorted per
+//                                contig by (start asc, end desc); padded to a
+//                                multiple of 32 with S_MAX / S_MIN
+//   data[n]                      int32 payload, permuted with the intervals
+//   branch[n]                    int32 GLOBAL position of the nearest preceding
+//                                interval of the same contig with end >= ends[i],
+//                                or -1 (the reference's SIZE_MAX)
+//   seg[G+1]                     int64 contig offsets
+//   lvl[h][...]                  max-of-32 pyramid over ends (h = 1..H), each level
+//                                padded to a multiple of 32 with S_MIN
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stddef.h>
+
+namespace sig {
+
+constexpr int kWarp = 32;
+constexpr uint32_t kFull = 0xffffffffu;
+
+template <typename S> struct Lim;
+template <> struct Lim<int32_t> {
+    static constexpr int32_t lo = INT32_MIN;
+    static constexpr int32_t hi = INT32_MAX;
+};
+template <> struct Lim<int64_t> {
+    static constexpr int64_t lo = INT64_MIN;
+    static constexpr int64_t hi = INT64_MAX;
+};
+
+__device__ __forceinline__ uint32_t lanemask_lt() {
+    uint32_t m;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
+}
+
+inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
+inline int64_t round_up(int64_t a, int64_t b) { return ceil_div(a, b) * b; }
+
+// Device-side error word written by kernels that detect bad input or give up
+// on a bounded wait; the host reads it after the launch sequence.
+enum DeviceError : int {
+    kDevOk = 0,
+    kDevBadContig = 1,     // a query named a contig outside [0, G)
+    kDevOverflow = 2,      // an output offset ran past the output capacity
+};
+
+// ---------------------------------------------------------------- scan
+// Exclusive prefix sums over n values; `out` receives n+1 values (the last one
+// is the total).  `temp` must hold scan_temp_bytes(n).
+size_t scan_temp_bytes(int64_t n);
+cudaError_t exclusive_scan_u32_to_i64(const uint32_t* in, int64_t* out, int64_t n, void* temp,
+                                      cudaStream_t st);
+cudaError_t exclusive_scan_u32_to_u32(const uint32_t* in, uint32_t* out, int64_t n, void* temp,
+                                      cudaStream_t st);
+
+// ---------------------------------------------------------------- sort
+// Stable LSD radix sort of n records whose key is K 32-bit words (word 0 least
+// significant) with one 32-bit payload.  keys[w] / payload are double
+// buffered with alt_keys[w] / alt_payload; the sorted result is left in the
+// buffers reported through *result_in_alt.  Passes whose digit is constant
+// over all records are skipped.
+constexpr int kMaxKeyWords = 5;
+size_t radix_temp_bytes(int64_t n, int K);
+cudaError_t radix_sort(uint32_t* const* keys, uint32_t* const* alt_keys, uint32_t* payload,
+                       uint32_t* alt_payload, int K, int64_t n, void* temp, size_t temp_bytes,
+                       bool* result_in_alt, int* passes_run, cudaStream_t st);
+
+// ---------------------------------------------------------------- build
+template <typename S>
+struct IndexView {
+    const S* starts;
+    const S* ends;
+    const int32_t* data;
+    const int32_t* branch;
+    const int64_t* seg;
+    int32_t n_seg;
+    int64_t n;
+    int n_levels;              // H: pyramid levels above ends
+    const S* lvl[8];           // lvl[h-1] = level h maxima
+};
+
+}  // namespace sig
+
+namespace sig {
+
+// Pyramid level pointers passed by value to kernels.
+template <typename S>
+struct Levels {
+    const S* p[8];
+};
+constexpr int kMaxLevels = 8;
+
+// ---------------------------------------------------------------- build launchers (si_build.cu)
+// Sets *d_flag to 1 when some contig is NOT in canonical (start asc, end desc)
+// order, following the add() flag logic of src/superintervals.hpp:95-105.
+template <typename S>
+cudaError_t launch_check_sorted(const S* s, const S* e, int64_t n, const int64_t* seg, int G,
+                                int* d_flag, cudaStream_t st);
+// Number of 32-bit key words for a coordinate type and contig count.
+template <typename S>
+int key_words(int G);
+template <typename S>
+cudaError_t launch_make_keys(const S* s, const S* e, int64_t n, const int64_t* seg, int G,
+                             uint32_t* const* kw, uint32_t* payload, cudaStream_t st);
+// Decode sorted keys back into padded starts/ends and gather the payload.
+template <typename S>
+cudaError_t launch_decode(const uint32_t* const* kw, const uint32_t* perm, const int32_t* data_in,
+                          int64_t n, int64_t n_pad, S* starts, S* ends, int32_t* data,
+                          cudaStream_t st);
+// Identity build (input already canonical): copy + pad.
+template <typename S>
+cudaError_t launch_copy_pad(const S* s_in, const S* e_in, const int32_t* d_in, int64_t n,
+                            int64_t n_pad, S* starts, S* ends, int32_t* data, uint32_t* perm,
+                            cudaStream_t st);
+// Pyramid sizes: fills sizes[0..H] (sizes[0] = n_pad) and returns H.
+int pyramid_levels(int64_t n_pad, int64_t* sizes);
+template <typename S>
+cudaError_t launch_pyramid(const S* ends, const int64_t* sizes, int H, S* const* lvl,
+                           cudaStream_t st);
+template <typename S>
+cudaError_t launch_branch(const S* ends, int64_t n, int64_t n_pad, Levels<S> L, int H,
+                          const int64_t* seg, int G, int32_t* branch, cudaStream_t st);
+
+// ---------------------------------------------------------------- query launchers (si_query.cu)
+struct QueryBatch {
+    const void* qs;          // S[nq]
+    const void* qe;          // S[nq]
+    const int32_t* qc;       // contig per query, or nullptr (all contig 0)
+    int64_t nq;
+};
+
+enum Order : int { kOrderIdxsCpp = 0, kOrderDesc = 1 };
+
+template <typename S>
+struct MapView {
+    const S* starts;
+    const S* ends;
+    const int32_t* branch;
+    const int32_t* data;
+    const int64_t* seg;
+    int32_t G;
+    int64_t n;
+};
+
+// plain one-query-per-thread path: upper_bound + branch walk per query
+template <typename S>
+cudaError_t launch_count_plain(MapView<S> m, QueryBatch q, uint32_t* counts, int* d_err,
+                               cudaStream_t st);
+template <typename S>
+cudaError_t launch_emit_plain(MapView<S> m, QueryBatch q, const int64_t* offsets, int64_t out_base,
+                              int order, bool values, int32_t* out, int* d_err, cudaStream_t st);
+template <typename S>
+cudaError_t launch_any_plain(MapView<S> m, QueryBatch q, uint8_t* out, int* d_err,
+                             cudaStream_t st);
+
+}  // namespace sig

@@ -1,0 +1,309 @@
+"""Python host side over the C-ABI.
+
+* ``GpuIndex`` -- a device-resident set of per-contig interval maps with numpy
+  batch queries in CSR form (the GPU-native surface).
+* ``IntervalMap`` -- a drop-in mirror of the reference's Python class
+  (src/superintervals/intervalmap.pyx:17-819, query/batch part): the same
+  method names, argument meaning and errors, answered by the GPU.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from typing import Optional
+
+import numpy as np
+
+from . import _capi
+from ._capi import (ORDER_DESC, ORDER_IDXS_CPP, PATH_AUTO, PATH_BATCHED, PATH_PLAIN, UB_BINARY,
+                    UB_EYTZINGER, UB_LEARNED, SIError, check)
+
+__all__ = ["GpuIndex", "IntervalMap", "SIError", "ORDER_IDXS_CPP", "ORDER_DESC", "PATH_AUTO",
+           "PATH_PLAIN", "PATH_BATCHED", "UB_BINARY", "UB_EYTZINGER", "UB_LEARNED"]
+
+
+def _p(a: Optional[np.ndarray]):
+    return None if a is None else C.c_void_p(a.ctypes.data)
+
+
+class GpuIndex:
+    """A set of per-contig interval maps resident on one GPU.
+
+    ``coord_bits`` is 32 or 64 (the reference's S = int / int64_t).  Contig
+    ``g`` holds the intervals ``[seg[g], seg[g+1])`` of the arrays passed to
+    :meth:`add_arrays`; results carry contig-local positions, exactly as one
+    reference IntervalMap per contig would return them.
+    """
+
+    def __init__(self, coord_bits: int = 32, device: int = 0):
+        self.lib = _capi.load()
+        self.bits = coord_bits
+        self.dtype = np.dtype(np.int64 if coord_bits == 64 else np.int32)
+        h = C.c_void_p()
+        check(self.lib.createSuperIntervalsGpu(C.byref(h), coord_bits, device))
+        self.h = h
+        self._sfx = "_i64" if coord_bits == 64 else ""
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.destroySuperIntervalsGpu(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- staging / build -----------------------------------------------------
+    def _coords(self, a):
+        return np.ascontiguousarray(a, dtype=self.dtype)
+
+    def add(self, start: int, end: int, value: int):
+        f = self.lib.addIntervalGpu_i64 if self.bits == 64 else self.lib.addIntervalGpu
+        check(f(self.h, int(start), int(end), int(value)))
+
+    def add_arrays(self, starts, ends, values=None, seg=None):
+        s, e = self._coords(starts), self._coords(ends)
+        if s.shape != e.shape:
+            raise ValueError("starts and ends must have the same length")
+        v = None if values is None else np.ascontiguousarray(values, dtype=np.int32)
+        if v is not None and v.shape != s.shape:
+            raise ValueError("values length must match starts/ends length")
+        f = getattr(self.lib, "addIntervalsGpu" + self._sfx)
+        check(f(self.h, _p(s), _p(e), _p(v), s.shape[0]))
+        if seg is not None:
+            seg = np.ascontiguousarray(seg, dtype=np.int64)
+            check(self.lib.setContigsGpu(self.h, seg.shape[0] - 1, _p(seg)))
+
+    def set_contigs(self, seg):
+        seg = np.ascontiguousarray(seg, dtype=np.int64)
+        check(self.lib.setContigsGpu(self.h, seg.shape[0] - 1, _p(seg)))
+
+    def build(self):
+        check(self.lib.indexSuperIntervalsGpu(self.h))
+
+    def clear(self):
+        check(self.lib.clearSuperIntervalsGpu(self.h))
+
+    def reserve(self, n: int):
+        check(self.lib.reserveSuperIntervalsGpu(self.h, int(n)))
+
+    def size(self) -> int:
+        return int(self.lib.sizeSuperIntervalsGpu(self.h))
+
+    def n_contigs(self) -> int:
+        return int(self.lib.numContigsGpu(self.h))
+
+    def arrays(self):
+        """(starts, ends, data, branch) after build(); branch is contig-local, -1 = none."""
+        n = self.size()
+        s, e = np.empty(n, self.dtype), np.empty(n, self.dtype)
+        d, b = np.empty(n, np.int32), np.empty(n, np.int64)
+        check(self.lib.getIndexArraysGpu(self.h, _p(s), _p(e), _p(d), _p(b)))
+        return s, e, d, b
+
+    # -- options ---------------------------------------------------------------
+    def set_path(self, path: int):
+        check(self.lib.setQueryPathGpu(self.h, int(path)))
+
+    def set_upper_bound(self, mode: int):
+        check(self.lib.setUpperBoundModeGpu(self.h, int(mode)))
+
+    def set_output_budget(self, nbytes: int):
+        check(self.lib.setOutputBudgetGpu(self.h, int(nbytes)))
+
+    @property
+    def stream(self):
+        return self.lib.getStreamGpu(self.h)
+
+    # -- queries (host buffers) ------------------------------------------------
+    def _queries(self, qs, qe, qc):
+        qs, qe = self._coords(qs), self._coords(qe)
+        if qs.shape != qe.shape:
+            raise ValueError("starts and ends must have the same length")
+        qc = None if qc is None else np.ascontiguousarray(qc, dtype=np.int32)
+        if qc is not None and qc.shape != qs.shape:
+            raise ValueError("contig ids must match the query count")
+        return qs, qe, qc
+
+    def count(self, qs, qe, qc=None) -> np.ndarray:
+        qs, qe, qc = self._queries(qs, qe, qc)
+        out = np.empty(qs.shape[0], np.uint32)
+        f = getattr(self.lib, "countOverlapsBatchGpu" + self._sfx)
+        check(f(self.h, _p(qs), _p(qe), _p(qc), qs.shape[0], _p(out)))
+        return out
+
+    def has_overlaps(self, qs, qe, qc=None) -> np.ndarray:
+        qs, qe, qc = self._queries(qs, qe, qc)
+        out = np.empty(qs.shape[0], np.uint8)
+        f = getattr(self.lib, "anyOverlapsBatchGpu" + self._sfx)
+        check(f(self.h, _p(qs), _p(qe), _p(qc), qs.shape[0], _p(out)))
+        return out.astype(bool)
+
+    def search(self, qs, qe, qc=None, order=ORDER_IDXS_CPP, values=False):
+        """CSR result: (offsets int64[nq+1], out int32[P]).  ``order`` selects
+        the C++ search_idxs order or the fully descending order; ``values``
+        returns payloads instead of contig-local positions."""
+        qs, qe, qc = self._queries(qs, qe, qc)
+        nq = qs.shape[0]
+        off = np.empty(nq + 1, np.int64)
+        total = C.c_size_t(0)
+        cap = 0
+        out = np.empty(1, np.int32)
+        for _ in range(2):
+            st = self.lib.searchBatchIntoGpu(self.h, _p(qs), _p(qe), _p(qc), nq, int(order),
+                                             1 if values else 0, _p(off), _p(out), cap,
+                                             C.byref(total))
+            if st == _capi.SI_ERR_CAPACITY:
+                cap = int(total.value)
+                out = np.empty(max(cap, 1), np.int32)
+                continue
+            check(st)
+            break
+        return off, out[: int(off[-1])] if nq else out[:0]
+
+
+class IntervalMap:
+    """Drop-in mirror of the reference's Python ``IntervalMap``
+    (src/superintervals/intervalmap.pyx): intervals are end-inclusive, values
+    are arbitrary Python objects, ``build()`` must precede queries, results come
+    in the reference's order.  Queries run on the GPU through the C-ABI."""
+
+    def __init__(self, device: int = 0):
+        self._device = device
+        self._starts: list = []
+        self._ends: list = []
+        self._values: list = []
+        self._idx: Optional[GpuIndex] = None
+        self._sorted = None  # (starts, ends, perm) after build
+
+    # construction (pyx:41-131)
+    def add(self, start: int, end: int, value=None):
+        self._starts.append(int(start))
+        self._ends.append(int(end))
+        self._values.append(value)
+        self._sorted = None
+
+    @classmethod
+    def from_arrays(cls, starts, ends, values=None):
+        inst = cls()
+        s = np.asarray(starts).astype(np.int64).tolist()
+        e = np.asarray(ends).astype(np.int64).tolist()
+        if len(s) != len(e):
+            raise ValueError("starts and ends must have the same length")
+        if values is not None and len(values) != len(s):
+            raise ValueError("values length must match starts/ends length")
+        inst._starts, inst._ends = s, e
+        inst._values = list(values) if values is not None else [None] * len(s)
+        inst.build()
+        return inst
+
+    def build(self):
+        idx = GpuIndex(32, self._device)
+        n = len(self._starts)
+        if n:
+            idx.add_arrays(np.asarray(self._starts, np.int32), np.asarray(self._ends, np.int32),
+                           np.arange(n, dtype=np.int32))
+        idx.build()
+        s, e, perm, _ = idx.arrays()
+        self._idx = idx
+        self._sorted = (s, e, perm)
+        self._values = [self._values[p] for p in perm.tolist()] if n else []
+        self._starts, self._ends = s.tolist(), e.tolist()
+
+    def _need(self):
+        if self._sorted is None:
+            # the reference leaves queries before build() undefined; here they raise
+            raise SIError(_capi.SI_ERR_NOT_BUILT, "call build() before querying")
+
+    # element access (pyx:133-218)
+    def __len__(self):
+        return self.size()
+
+    def __getitem__(self, index: int):
+        return self.at(index)
+
+    def size(self) -> int:
+        return len(self._starts)
+
+    def at(self, index: int):
+        if self.size() == 0 or index < 0 or index >= self.size():
+            raise IndexError("Index out of range")
+        return self._starts[index], self._ends[index], self._values[index]
+
+    def starts_at(self, index: int):
+        return self.at(index)[0]
+
+    def ends_at(self, index: int):
+        return self.at(index)[1]
+
+    def data_at(self, index: int):
+        return self.at(index)[2]
+
+    def clear(self):
+        self._starts, self._ends, self._values = [], [], []
+        self._idx, self._sorted = None, None
+
+    def reserve(self, n: int):
+        pass
+
+    # single queries (pyx:241-361), answered as one-query batches
+    def has_overlaps(self, start: int, end: int) -> bool:
+        return bool(self.has_overlaps_batch([start], [end])[0]) if self.size() else False
+
+    def count(self, start: int, end: int) -> int:
+        return int(self.count_batch([start], [end])[0]) if self.size() else 0
+
+    def search_idxs(self, start: int, end: int) -> list:
+        return self.search_idxs_batch([start], [end])[0] if self.size() else []
+
+    def search_values(self, start: int, end: int) -> list:
+        return self.search_values_batch([start], [end])[0] if self.size() else []
+
+    def search_keys(self, start: int, end: int) -> list:
+        return [(self._starts[i], self._ends[i]) for i in self.search_idxs(start, end)]
+
+    def search_items(self, start: int, end: int) -> list:
+        return [(self._starts[i], self._ends[i], self._values[i]) for i in self.search_idxs(start, end)]
+
+    # batch queries (pyx:363-494)
+    @staticmethod
+    def _q(starts, ends):
+        s = np.ascontiguousarray(starts, dtype=np.int32)
+        e = np.ascontiguousarray(ends, dtype=np.int32)
+        if s.shape[0] != e.shape[0]:
+            raise ValueError("starts and ends must have the same length")
+        return s, e
+
+    def count_batch(self, starts, ends) -> list:
+        s, e = self._q(starts, ends)
+        self._need()
+        if self.size() == 0:
+            return [0] * s.shape[0]
+        return self._idx.count(s, e).astype(np.int64).tolist()
+
+    def has_overlaps_batch(self, starts, ends) -> list:
+        s, e = self._q(starts, ends)
+        self._need()
+        if self.size() == 0:
+            return [False] * s.shape[0]
+        return self._idx.has_overlaps(s, e).tolist()
+
+    def search_idxs_batch(self, starts, ends) -> list:
+        s, e = self._q(starts, ends)
+        self._need()
+        if self.size() == 0:
+            return [[] for _ in range(s.shape[0])]
+        off, out = self._idx.search(s, e, order=ORDER_IDXS_CPP)
+        vals = out.tolist()
+        return [vals[off[i]:off[i + 1]] for i in range(s.shape[0])]
+
+    def search_values_batch(self, starts, ends) -> list:
+        s, e = self._q(starts, ends)
+        self._need()
+        if self.size() == 0:
+            return [[] for _ in range(s.shape[0])]
+        off, out = self._idx.search(s, e, order=ORDER_DESC)
+        v = self._values
+        pos = out.tolist()
+        return [[v[p] for p in pos[off[i]:off[i + 1]]] for i in range(s.shape[0])]

@@ -1,0 +1,229 @@
+"""GPU parity: the CUDA path (called through the C-ABI) against the golden
+fixtures made by the reference itself and against the oracle on seeded
+inputs.  Integer work: everything is compared bit-exactly, except payload
+order inside runs of exact (start, end) duplicates, where the reference's
+std::sort leaves it unspecified (checked as a permutation)."""
+import numpy as np
+import pytest
+
+from golden_util import assert_data_parity, fixture_names, load
+
+pytestmark = pytest.mark.gpu
+
+PATHS = ["plain", "batched"]
+
+
+@pytest.fixture(scope="module")
+def api():
+    import __graft_entry__ as g
+    g.build()
+    from superintervals_gb300 import interval_map as im
+    return im
+
+
+@pytest.fixture(scope="module")
+def oracle():
+    from oracle.oracle import Oracle
+    return Oracle()
+
+
+def _index(api, starts, ends, data=None, seg=None, path="plain"):
+    bits = 64 if np.asarray(starts).dtype == np.int64 else 32
+    idx = api.GpuIndex(bits)
+    idx.add_arrays(starts, ends, data, seg=seg)
+    idx.build()
+    idx.set_path(api.PATH_PLAIN if path == "plain" else api.PATH_BATCHED)
+    return idx
+
+
+@pytest.mark.parametrize("path", PATHS)
+@pytest.mark.parametrize("name", fixture_names())
+def test_fixture_parity(api, name, path):
+    g = load(name)
+    idx = _index(api, g["starts"], g["ends"], g["data"], path=path)
+    s, e, d, b = idx.arrays()
+    assert np.array_equal(s, g["ref_sorted_starts"])
+    assert np.array_equal(e, g["ref_sorted_ends"])
+    assert np.array_equal(b, g["ref_branch"].astype(np.int64))
+    assert_data_parity(s, e, g["ref_sorted_data"], d)
+    qs, qe = g["q_starts"], g["q_ends"]
+    cnt = idx.count(qs, qe)
+    assert np.array_equal(cnt.astype(np.int64), g["ref_count"].astype(np.int64))
+    off, out = idx.search(qs, qe, order=api.ORDER_IDXS_CPP)
+    assert np.array_equal(off, g["ref_search_idxs_off"])
+    assert np.array_equal(out, g["ref_search_idxs"])
+    offd, outd = idx.search(qs, qe, order=api.ORDER_DESC)
+    assert np.array_equal(offd, off)
+    if "ref_c_search_idxs" in g:
+        assert np.array_equal(outd, g["ref_c_search_idxs"])
+    offv, outv = idx.search(qs, qe, order=api.ORDER_DESC, values=True)
+    assert np.array_equal(offv, g["ref_search_values_off"])
+    assert np.array_equal(outv, d[outd])                       # own payload at the hit positions
+    assert np.array_equal(g["ref_search_values"], g["ref_sorted_data"][outd])
+    hv = idx.has_overlaps(qs, qe)
+    assert np.array_equal(hv.astype(np.int32), g["ref_has_overlaps"].astype(np.int32))
+    idx.close()
+
+
+@pytest.mark.parametrize("path", PATHS)
+def test_multicontig_stream(api, path):
+    s = load("contigs3_stream_int32")
+    idx = _index(api, s["starts"], s["ends"], s["data"], seg=s["seg"], path=path)
+    off, out = idx.search(s["q_starts"], s["q_ends"], s["q_contig"], order=api.ORDER_IDXS_CPP)
+    for gi in range(3):
+        g = load(f"contigs3_g{gi}_int32")
+        got = [out[off[q]:off[q + 1]].tolist() for q in g["q_index"]]
+        ro, rv = g["ref_search_idxs_off"], g["ref_search_idxs"]
+        assert got == [rv[ro[i]:ro[i + 1]].tolist() for i in range(len(ro) - 1)]
+    cnt = idx.count(s["q_starts"], s["q_ends"], s["q_contig"])
+    assert np.array_equal(cnt.astype(np.int64), np.diff(off))
+    idx.close()
+
+
+def _oracle_case(api, oracle, wl, path, orders=(0, 1)):
+    idx = _index(api, wl.starts, wl.ends, wl.data, seg=wl.seg, path=path)
+    m = oracle.build(wl.starts, wl.ends, wl.data, seg=wl.seg)
+    s, e, d, b = idx.arrays()
+    assert np.array_equal(s, m["starts"]) and np.array_equal(e, m["ends"])
+    assert np.array_equal(b, m["branch"])
+    assert np.array_equal(d, m["data"])          # both sorts are stable
+    cnt = idx.count(wl.q_starts, wl.q_ends, wl.q_contig)
+    rc = oracle.count_batch(m, wl.q_starts, wl.q_ends, wl.q_contig, nthreads=8)
+    assert np.array_equal(cnt, rc)
+    for order in orders:
+        off, out = idx.search(wl.q_starts, wl.q_ends, wl.q_contig, order=order)
+        ro, rv = oracle.search_batch(m, wl.q_starts, wl.q_ends, wl.q_contig, order=order,
+                                     nthreads=8, counts=rc)
+        assert np.array_equal(off, ro)
+        assert np.array_equal(out, rv)
+    idx.close()
+
+
+@pytest.mark.parametrize("path", PATHS)
+def test_config1_full(api, oracle, path):
+    from superintervals_gb300 import workloads as W
+    _oracle_case(api, oracle, W.config1(), path)
+
+
+@pytest.mark.parametrize("path", PATHS)
+def test_config2_scaled(api, oracle, path):
+    from superintervals_gb300 import workloads as W
+    _oracle_case(api, oracle, W.config2(n=1_000_000, nq=200_000), path, orders=(0,))
+
+
+@pytest.mark.parametrize("path", PATHS)
+def test_config3_scaled(api, oracle, path):
+    from superintervals_gb300 import workloads as W
+    _oracle_case(api, oracle, W.config3(n=1_000_000, nq=300_000), path, orders=(0, 1))
+
+
+@pytest.mark.parametrize("path", PATHS)
+def test_config3_long_queries_scaled(api, oracle, path):
+    from superintervals_gb300 import workloads as W
+    _oracle_case(api, oracle, W.config3(n=200_000, nq=50_000, long_queries=True), path, orders=(0,))
+
+
+@pytest.mark.parametrize("path", PATHS)
+@pytest.mark.parametrize("seed,dt", [(21, np.int32), (22, np.int64), (23, np.int32)])
+def test_random_nested(api, oracle, seed, dt, path):
+    from superintervals_gb300 import workloads as W
+    _oracle_case(api, oracle, W.random_nested(seed, 30_000, 20_000, dtype=dt, span=2_000_000,
+                                              max_len=3_000), path)
+
+
+@pytest.mark.parametrize("path", PATHS)
+def test_config4_scaled_int64(api, oracle, path):
+    from superintervals_gb300 import workloads as W
+    wl = W.config4(n=300_000, nq=20_000, span=3_100_000_000)
+    idx = _index(api, wl.starts, wl.ends, wl.data, path=path)
+    m = oracle.build(wl.starts, wl.ends, wl.data)
+    s, e, d, b = idx.arrays()
+    assert np.array_equal(s, m["starts"]) and np.array_equal(b, m["branch"])
+    cnt = idx.count(wl.q_starts, wl.q_ends)
+    assert np.array_equal(cnt, oracle.count_batch(m, wl.q_starts, wl.q_ends, nthreads=8))
+    hv = idx.has_overlaps(wl.q_starts, wl.q_ends)
+    assert np.array_equal(hv.astype(np.int32), oracle.has_overlaps_batch(m, wl.q_starts, wl.q_ends))
+    idx.close()
+
+
+def test_chunked_emit_matches_unchunked(api, oracle):
+    from superintervals_gb300 import workloads as W
+    wl = W.random_nested(31, 20_000, 20_000, span=500_000, max_len=5_000)
+    idx = _index(api, wl.starts, wl.ends, wl.data)
+    off1, out1 = idx.search(wl.q_starts, wl.q_ends)
+    idx.set_output_budget(1 << 20)       # 1 MiB: forces many chunks
+    off2, out2 = idx.search(wl.q_starts, wl.q_ends)
+    assert int(off1[-1]) * 4 > (1 << 21)
+    assert np.array_equal(off1, off2) and np.array_equal(out1, out2)
+    idx.close()
+
+
+def test_rebuild_after_more_adds(api, oracle):
+    g = load("nested_dups_int32")
+    n = g["starts"].shape[0]
+    idx = api.GpuIndex(32)
+    idx.add_arrays(g["starts"][: n // 2], g["ends"][: n // 2], g["data"][: n // 2])
+    idx.build()
+    idx.add_arrays(g["starts"][n // 2:], g["ends"][n // 2:], g["data"][n // 2:])
+    with pytest.raises(api.SIError):
+        idx.count(g["q_starts"], g["q_ends"])         # added after build: must rebuild
+    idx.build()
+    off, out = idx.search(g["q_starts"], g["q_ends"])
+    assert np.array_equal(off, g["ref_search_idxs_off"]) and np.array_equal(out, g["ref_search_idxs"])
+    idx.close()
+
+
+def test_errors_are_reported(api):
+    idx = api.GpuIndex(32)
+    idx.add_arrays(np.array([1, 5], np.int32), np.array([3, 9], np.int32))
+    with pytest.raises(api.SIError) as ei:
+        idx.count([1], [2])
+    assert ei.value.status == 3                       # NOT_BUILT
+    idx.build()
+    with pytest.raises(api.SIError) as ei:
+        idx.count([1], [2], qc=[1])                   # only contig 0 exists
+    assert ei.value.status == 1
+    idx64 = api.GpuIndex(64)
+    assert idx64.lib.addIntervalGpu(idx64.h, 1, 2, 3) == 1   # 32-bit add on a 64-bit handle
+    assert int(idx.count([1], [2])[0]) == 1           # the handle is still usable
+    idx.close()
+    idx64.close()
+
+
+def test_device_budget_rejects_oversize(api):
+    lib = api._capi.load()
+    used = lib.deviceBytesInUseGpu()
+    lib.setDeviceBudgetGpu(used + (1 << 20))
+    try:
+        idx = api.GpuIndex(32)
+        n = 2_000_000
+        idx.add_arrays(np.arange(n, dtype=np.int32), np.arange(n, dtype=np.int32) + 5)
+        with pytest.raises(api.SIError) as ei:
+            idx.build()
+        assert ei.value.status == 2                   # OOM by admission, no fault
+    finally:
+        lib.setDeviceBudgetGpu(0)
+    idx.build()
+    assert int(idx.count([10], [10])[0]) == 6
+    idx.close()
+
+
+def test_python_intervalmap_dropin(api):
+    """The README batch example of the reference Python API (README.md:16-27)."""
+    from array import array
+    IM = api.IntervalMap
+    imap = IM()
+    imap.add(10, 20, "A")
+    imap.add(15, 25, "B")
+    imap.build()
+    assert imap.search_values(8, 20) == ["B", "A"]
+    imap = IM.from_arrays(array("i", [10, 15, 30]), array("i", [20, 25, 40]), ["A", "B", "C"])
+    qs, qe = array("i", [5, 18, 35]), array("i", [12, 22, 45])
+    assert imap.count_batch(qs, qe) == [1, 2, 1]
+    assert imap.search_idxs_batch(qs, qe) == [[0], [0, 1], [2]]
+    assert imap.search_values_batch(qs, qe) == [["A"], ["B", "A"], ["C"]]
+    assert imap.at(1) == (15, 25, "B")
+    with pytest.raises(IndexError):
+        imap.at(3)
+    with pytest.raises(ValueError):
+        imap.count_batch(array("i", [1, 2]), array("i", [3]))
