@@ -163,6 +163,14 @@ int searchDeviceGpu(gSuperIntervals* si, const void* d_qs, const void* d_qe,
                     int64_t* d_offsets, int32_t* d_values, size_t capacity, size_t* total,
                     void* stream);
 
+/* Upper bound of every query end: contig-local position of the last interval
+ * whose start <= qe, or -1.  upperBound (c_superintervals.h:195, 537-568) /
+ * IntervalMap::upper_bound (superintervals.hpp:501-516), computed with the
+ * provider `mode` (SI_UB_*), which must be the handle's current mode or
+ * SI_UB_BINARY.  Device buffers. */
+int upperBoundDeviceGpu(gSuperIntervals* si, const void* d_qe, const int32_t* d_qcontig, size_t nq,
+                        int mode, int32_t* d_out, void* stream);
+
 /* ---- result helpers: createIndexResult / clearIndexResult /
  *      destroyIndexResult (c_superintervals.h:339-343, 1070-1075) --------- */
 cCsrResult createCsrResult(void);

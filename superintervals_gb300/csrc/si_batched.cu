@@ -1,40 +1,937 @@
-// si_batched.cu -- the BATCHED query path (sorted-query tiles).
+// si_batched.cu -- the BATCHED query path.
+//
+// The reference answers a batch one query at a time (src/superintervals/intervalmap.pyx:363-494
+// loop over IntervalMap::search_idxs, hpp:879-905).  Queries that lie close together on a contig
+// hit nearly the same intervals, so here they are answered together:
+//
+//  1. prepare: queries are radix-sorted by (class, contig, end); each sorted query gets its
+//     upper bound (binary / Eytzinger / learned, si_ubound.cuh).  "class" puts queries longer
+//     than a threshold after the short ones.
+//  2. tiles: a CTA takes `tile_q` consecutive sorted short queries of one contig.  One warp
+//     gathers the candidate set C = { k <= max ub : ends[k] >= min qs } of the tile into
+//     shared memory, in descending position order, by walking the max-of-32 pyramid of ends
+//     (whole 32-chunk groups at a time, coalesced 128-byte loads, chunk runs whose max end is
+//     below the threshold skipped).  C holds every hit of every query of the tile.  Then each
+//     warp filters C for one query at a time (k <= ub_q and ends[k] >= qs_q) with ballots:
+//     the count pass counts and records the query's head-run length (the run of consecutive
+//     hits ending at ub), the emit pass writes the head run arithmetically (ascending for the
+//     C++ search_idxs order, hpp:892-895; descending for search_values / the C API) and then
+//     the remaining hits in descending order -- exactly the reference's output.
+//  3. long queries (and tiles whose C overflows shared memory) take the per-query walk: one
+//     warp per query walks the pyramid with the query's own threshold and counts / writes hits
+//     directly, 32 positions per step.
+// Tiles and long queries are handed out by an atomic work counter (persistent CTAs), so uneven
+// per-query result counts do not leave SMs idle.
+#include <algorithm>
+#include <vector>
+
 #include "si_batched.cuh"
 #include "si_gpu/c_api.h"
+#include "si_ubound.cuh"
 
 namespace sig {
+namespace {
 
-BatchedWorkspace::~BatchedWorkspace() {
-    for (int i = 0; i < 16; ++i)
-        if (blocks[i]) cudaFree(blocks[i]);
+constexpr int kThreads = 256;
+constexpr int kWarpsPerCta = kThreads / kWarp;
+
+template <typename S>
+struct Pyr {
+    const S* ends;
+    const S* m[kMaxLevels];
+    int H;
+};
+
+// Highest chunk index <= cmax whose max end is >= L (or -1), by climbing the pyramid and
+// descending into the nearest qualifying node.  Warp-uniform.
+template <typename S>
+__device__ __forceinline__ int64_t highest_chunk(const Pyr<S>& P, int64_t cmax, S L, int lane) {
+    if (cmax < 0) return -1;
+    if (P.H == 0) return 0;
+    int64_t node = cmax;
+    int h = 1;
+    int64_t found = -1;
+    while (true) {
+        const int64_t grp = node >> 5;
+        const int pos = (int)(node & 31);
+        const S v = P.m[h - 1][(grp << 5) + lane];
+        const unsigned mask = __ballot_sync(kFull, lane <= pos && v >= L);
+        if (mask) {
+            found = (grp << 5) + (31 - __clz(mask));
+            break;
+        }
+        if (h == P.H || grp == 0) return -1;
+        node = grp - 1;
+        ++h;
+    }
+    while (h > 1) {
+        const S v = P.m[h - 2][(found << 5) + lane];
+        const unsigned mask = __ballot_sync(kFull, v >= L);
+        if (!mask) return -1;  // cannot happen: the parent's max is >= L
+        found = (found << 5) + (31 - __clz(mask));
+        --h;
+    }
+    return found;
+}
+
+// Visit in descending position order every position k in [lo, u] with ends[k] >= L.
+// f(chunk, hitmask, value) is called per 32-position chunk holding hits (bit l = position
+// chunk*32+l); it returns false to stop.  Warp-uniform.
+template <typename S, typename F>
+__device__ __forceinline__ void scan_desc(const Pyr<S>& P, int64_t lo, int64_t u, S L, int lane, F&& f) {
+    int64_t cur = u;
+    while (cur >= lo) {
+        const int64_t c = highest_chunk(P, cur >> 5, L, lane);
+        if (c < 0 || ((c << 5) + 31) < lo) return;
+        if (c < (cur >> 5)) cur = (c << 5) + 31;
+        const int64_t grp = c >> 5;
+        unsigned gm;
+        if (P.H == 0) {
+            gm = 1u;
+        } else {
+            const S v1 = P.m[0][(grp << 5) + lane];
+            gm = __ballot_sync(kFull, lane <= (int)(c & 31) && v1 >= L);
+        }
+        while (gm) {
+            int64_t ch[4];
+            S val[4];
+            bool ok[4];
+            int cnt = 0;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                ok[k] = false;
+                if (gm) {
+                    const int b = 31 - __clz(gm);
+                    gm &= ~(1u << b);
+                    ch[k] = (grp << 5) + b;
+                    const int64_t p = (ch[k] << 5) + lane;
+                    ok[k] = p <= cur && p >= lo;
+                    val[k] = ok[k] ? P.ends[p] : Lim<S>::lo;
+                    cnt = k + 1;
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                if (k < cnt) {
+                    const unsigned hm = __ballot_sync(kFull, ok[k] && val[k] >= L);
+                    if (hm && !f(ch[k], hm, val[k])) return;
+                }
+            }
+        }
+        cur = (grp << 10) - 1;
+    }
+}
+
+__device__ __forceinline__ unsigned above_mask(int lane) {
+    // bits strictly above `lane`
+    return lane == 31 ? 0u : ~((2u << lane) - 1u);
 }
 
 template <typename S>
-int batched_prepare(BatchedWorkspace&, MapView<S>, Levels<S>, int, const int64_t*, int, cudaStream_t) {
+struct TileArgs {
+    Pyr<S> P;
+    const int32_t* data;
+    const int64_t* seg;
+    int32_t G;
+    const S* sq_s;
+    const int32_t* sq_u;
+    const uint32_t* sq_c;
+    const int32_t* sq_id;
+    int64_t nq;
+    int tile_q;
+    int cap;
+    int n_tiles;
+    int* tile_counter;
+    // count pass
+    uint32_t* counts;
+    int32_t* heads;
+    // emit pass
+    const int32_t* heads_in;
+    const int64_t* offsets;
+    int64_t out_base;
+    int order;
+    bool values;
+    int32_t* out;
+    int* d_err;
+};
+
+// ---- per-query walk (long queries, overflowing tiles): one warp, direct output ----
+template <typename S, bool EMIT>
+__device__ void walk_query(const TileArgs<S>& a, S qs, int64_t u, int64_t lo, int32_t id, int lane) {
+    if (!EMIT) {
+        uint32_t cnt = 0;
+        int64_t head = 0;
+        bool open = true;
+        int64_t expect = u;
+        if (u >= lo) {
+            scan_desc(a.P, lo, u, qs, lane, [&](int64_t ch, unsigned hm, S) {
+                cnt += __popc(hm);
+                if (open) {
+                    if (ch != (expect >> 5)) {
+                        open = false;
+                    } else {
+                        const int le = (int)(expect & 31);
+                        const unsigned low = (le == 31) ? ~0u : ((1u << (le + 1)) - 1u);
+                        const unsigned zeros = ~hm & low;
+                        if (!zeros) {
+                            head += le + 1;
+                            expect = (ch << 5) - 1;
+                        } else {
+                            head += le - (31 - __clz(zeros));
+                            open = false;
+                        }
+                    }
+                }
+                return true;
+            });
+        }
+        if (lane == 0) {
+            a.counts[id] = cnt;
+            a.heads[id] = (int32_t)head;
+        }
+        return;
+    }
+    const int64_t h = a.heads_in[id];
+    const int64_t base = a.offsets[id] - a.out_base;
+    const int64_t capq = a.offsets[id + 1] - a.offsets[id];
+    if (h > capq) {
+        if (lane == 0) atomicCAS(a.d_err, kDevOk, kDevOverflow);
+        return;
+    }
+    int32_t* dst = a.out + base;
+    for (int64_t r = lane; r < h; r += 32) {
+        const int64_t pos = (a.order == kOrderIdxsCpp) ? (u - h + 1 + r) : (u - r);
+        dst[r] = a.values ? a.data[pos] : (int32_t)(pos - lo);
+    }
+    int64_t w = h;
+    const int64_t start = u - h;
+    if (start >= lo) {
+        scan_desc(a.P, lo, start, qs, lane, [&](int64_t ch, unsigned hm, S) {
+            const int k = __popc(hm);
+            if (w + k > capq) {
+                if (lane == 0) atomicCAS(a.d_err, kDevOk, kDevOverflow);
+                return false;
+            }
+            if ((hm >> lane) & 1u) {
+                const int64_t pos = (ch << 5) + lane;
+                dst[w + __popc(hm & above_mask(lane))] = a.values ? a.data[pos] : (int32_t)(pos - lo);
+            }
+            w += k;
+            return true;
+        });
+    }
+}
+
+template <typename S, bool EMIT>
+__global__ void __launch_bounds__(kThreads) k_tiles(TileArgs<S> a) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int cap = a.cap, T = a.tile_q;
+    S* cend = reinterpret_cast<S*>(smem);
+    int32_t* cpos = reinterpret_cast<int32_t*>(cend + cap);
+    S* q_s = reinterpret_cast<S*>(cpos + cap);
+    int32_t* q_u = reinterpret_cast<int32_t*>(q_s + T);
+    uint32_t* q_c = reinterpret_cast<uint32_t*>(q_u + T);
+    int32_t* q_id = reinterpret_cast<int32_t*>(q_c + T);
+    __shared__ int s_tile, s_nc, s_over;
+    __shared__ S s_red[kWarpsPerCta];
+
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    while (true) {
+        if (tid == 0) s_tile = atomicAdd(a.tile_counter, 1);
+        __syncthreads();
+        const int t = s_tile;
+        if (t >= a.n_tiles) return;
+        const int64_t j0 = (int64_t)t * T;
+        const int nt = (int)((a.nq - j0) < (int64_t)T ? (a.nq - j0) : (int64_t)T);
+        for (int i = tid; i < nt; i += kThreads) {
+            q_s[i] = a.sq_s[j0 + i];
+            q_u[i] = a.sq_u[j0 + i];
+            q_c[i] = a.sq_c[j0 + i];
+            q_id[i] = a.sq_id[j0 + i];
+        }
+        __syncthreads();
+        int r0 = 0;
+        while (r0 < nt) {
+            // run of equal class/contig words [r0, r1): sorted, so binary search the end
+            const uint32_t cw = q_c[r0];
+            int lo_i = r0 + 1, hi_i = nt;
+            while (lo_i < hi_i) {
+                const int mid = (lo_i + hi_i) >> 1;
+                if (q_c[mid] == cw) lo_i = mid + 1;
+                else hi_i = mid;
+            }
+            const int r1 = lo_i;
+            const bool is_long = (cw >> 31) != 0;
+            int g = (int)(cw & 0x7fffffffu);
+            if (g >= a.G) g = 0;  // reported by the prepare kernel
+            const int64_t lo = a.seg[g];
+            bool per_query = is_long;
+            if (!is_long) {
+                // L = min qs over the run, umax = ub of the last query of the run
+                S mn = Lim<S>::hi;
+                for (int i = r0 + tid; i < r1; i += kThreads) mn = q_s[i] < mn ? q_s[i] : mn;
+#pragma unroll
+                for (int d = 16; d > 0; d >>= 1) {
+                    const S o = __shfl_xor_sync(kFull, mn, d);
+                    mn = o < mn ? o : mn;
+                }
+                if (lane == 0) s_red[warp] = mn;
+                __syncthreads();
+                if (warp == 0) {
+                    S L = s_red[lane < kWarpsPerCta ? lane : 0];
+#pragma unroll
+                    for (int d = 16; d > 0; d >>= 1) {
+                        const S o = __shfl_xor_sync(kFull, L, d);
+                        L = o < L ? o : L;
+                    }
+                    const int64_t umax = q_u[r1 - 1];
+                    int nc = 0;
+                    bool over = false;
+                    if (umax >= lo) {
+                        scan_desc(a.P, lo, umax, L, lane, [&](int64_t ch, unsigned hm, S v) {
+                            const int k = __popc(hm);
+                            if (nc + k > cap) {
+                                over = true;
+                                return false;
+                            }
+                            if ((hm >> lane) & 1u) {
+                                const int idx = nc + __popc(hm & above_mask(lane));
+                                cend[idx] = v;
+                                cpos[idx] = (int32_t)((ch << 5) + lane);
+                            }
+                            nc += k;
+                            return true;
+                        });
+                    }
+                    if (lane == 0) {
+                        s_nc = nc;
+                        s_over = over ? 1 : 0;
+                    }
+                }
+                __syncthreads();
+                per_query = s_over != 0;
+            }
+            const int nc = per_query ? 0 : s_nc;
+            for (int i = r0 + warp; i < r1; i += kWarpsPerCta) {
+                const S qs = q_s[i];
+                const int64_t u = q_u[i];
+                const int32_t id = q_id[i];
+                if (per_query) {
+                    walk_query<S, EMIT>(a, qs, u, lo, id, lane);
+                    continue;
+                }
+                // first candidate at or below u: C is sorted by position, descending
+                int b0 = 0, b1 = nc;
+                while (b0 < b1) {
+                    const int mid = (b0 + b1) >> 1;
+                    if (cpos[mid] > u) b0 = mid + 1;
+                    else b1 = mid;
+                }
+                const int t0 = b0;
+                if (!EMIT) {
+                    int head = 0;
+                    bool open = u >= lo;
+                    for (int kk = t0; open && kk < nc; kk += 32) {
+                        const int tt = kk + lane;
+                        const bool c = tt < nc && cpos[tt] == (int32_t)(u - (tt - t0)) && cend[tt] >= qs;
+                        const unsigned m = __ballot_sync(kFull, c);
+                        if (m == kFull) {
+                            head += 32;
+                        } else {
+                            head += __ffs(~m) - 1;
+                            open = false;
+                        }
+                    }
+                    uint32_t cnt = 0;
+                    for (int kk = t0; kk < nc; kk += 32) {
+                        const int tt = kk + lane;
+                        cnt += __popc(__ballot_sync(kFull, tt < nc && cend[tt] >= qs));
+                    }
+                    if (lane == 0) {
+                        a.counts[id] = cnt;
+                        a.heads[id] = head;
+                    }
+                } else {
+                    const int64_t h = a.heads_in[id];
+                    const int64_t base = a.offsets[id] - a.out_base;
+                    const int64_t capq = a.offsets[id + 1] - a.offsets[id];
+                    int32_t* dst = a.out + base;
+                    if (h > capq) {
+                        if (lane == 0) atomicCAS(a.d_err, kDevOk, kDevOverflow);
+                        continue;
+                    }
+                    for (int64_t r = lane; r < h; r += 32) {
+                        const int64_t pos = (a.order == kOrderIdxsCpp) ? (u - h + 1 + r) : (u - r);
+                        dst[r] = a.values ? a.data[pos] : (int32_t)(pos - lo);
+                    }
+                    int64_t w = h;
+                    bool bad = false;
+                    for (int kk = t0 + (int)h; kk < nc; kk += 32) {
+                        const int tt = kk + lane;
+                        const bool hit = tt < nc && cend[tt] >= qs;
+                        const unsigned m = __ballot_sync(kFull, hit);
+                        const int k = __popc(m);
+                        if (w + k > capq) {
+                            bad = true;
+                            break;
+                        }
+                        if (hit) {
+                            const int64_t pos = cpos[tt];
+                            dst[w + __popc(m & lanemask_lt())] = a.values ? a.data[pos] : (int32_t)(pos - lo);
+                        }
+                        w += k;
+                    }
+                    if (bad && lane == 0) atomicCAS(a.d_err, kDevOk, kDevOverflow);
+                }
+            }
+            __syncthreads();
+            r0 = r1;
+        }
+    }
+}
+
+// ---- query keys: (class|contig, end) -------------------------------------------------
+template <typename S>
+__global__ void k_qkeys(const S* __restrict__ qs, const S* __restrict__ qe, const int32_t* __restrict__ qc,
+                        int64_t nq, int64_t long_len, uint32_t* w0, uint32_t* w1, uint32_t* wc,
+                        uint32_t* __restrict__ pay) {
+    const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= nq) return;
+    const int32_t g = qc ? qc[q] : 0;
+    const bool is_long = ((double)qe[q] - (double)qs[q] + 1.0) > (double)long_len;
+    if constexpr (sizeof(S) == 4) {
+        w0[q] = (uint32_t)qe[q] ^ 0x80000000u;
+    } else {
+        const uint64_t b = (uint64_t)qe[q] ^ 0x8000000000000000ull;
+        w0[q] = (uint32_t)b;
+        w1[q] = (uint32_t)(b >> 32);
+    }
+    wc[q] = ((uint32_t)g & 0x7fffffffu) | (is_long ? 0x80000000u : 0u);
+    pay[q] = (uint32_t)q;
+}
+
+template <typename S>
+__global__ void __launch_bounds__(kThreads) k_qprep(const uint32_t* __restrict__ pay,
+                                                    const uint32_t* __restrict__ wc,
+                                                    const S* __restrict__ qs, const S* __restrict__ qe,
+                                                    int64_t nq, MapView<S> m, UbView<S> U,
+                                                    S* __restrict__ sq_s, int32_t* __restrict__ sq_u,
+                                                    uint32_t* __restrict__ sq_c, int32_t* __restrict__ sq_id,
+                                                    int* d_err) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    S* tree = reinterpret_cast<S*>(smem);
+    const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    int g0 = -1;
+    if (U.mode == 1 && U.eytz_n > 1) {
+        const int64_t jb = (int64_t)blockIdx.x * blockDim.x;
+        g0 = (int)(wc[jb < nq ? jb : nq - 1] & 0x7fffffffu);
+        if (g0 >= m.G) g0 = 0;
+        for (int i = threadIdx.x; i < U.eytz_n; i += blockDim.x) tree[i] = U.eytz_keys[(int64_t)g0 * U.eytz_n + i];
+        __syncthreads();
+    }
+    if (j >= nq) return;
+    const uint32_t orig = pay[j];
+    const uint32_t cw = wc[j];
+    int g = (int)(cw & 0x7fffffffu);
+    bool bad = false;
+    if (g >= m.G) {
+        atomicCAS(d_err, kDevOk, kDevBadContig);
+        g = 0;
+        bad = true;
+    }
+    const int64_t lo = m.seg[g];
+    const int64_t n = m.seg[g + 1] - lo;
+    int64_t u = -1;
+    if (!bad && n > 0) {
+        const S* tr = (U.mode == 1) ? ((g == g0) ? tree : U.eytz_keys + (int64_t)g * U.eytz_n) : nullptr;
+        u = ub_search(U, g, m.starts + lo, n, qe[orig], tr);
+    }
+    sq_s[j] = qs[orig];
+    sq_u[j] = (int32_t)(lo + u);
+    sq_c[j] = cw;
+    sq_id[j] = (int32_t)orig;
+}
+
+// upper bounds in the original query order (plain path with an accelerator, tests)
+template <typename S>
+__global__ void k_ub_plain(const S* __restrict__ qe, const int32_t* __restrict__ qc, int64_t nq,
+                           MapView<S> m, UbView<S> U, int32_t* __restrict__ out, int* d_err) {
+    const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= nq) return;
+    int g = qc ? qc[q] : 0;
+    if (g < 0 || g >= m.G) {
+        atomicCAS(d_err, kDevOk, kDevBadContig);
+        out[q] = -1;
+        return;
+    }
+    const int64_t lo = m.seg[g], n = m.seg[g + 1] - lo;
+    const S* tr = (U.mode == 1) ? U.eytz_keys + (int64_t)g * U.eytz_n : nullptr;
+    out[q] = (int32_t)ub_search(U, g, m.starts + lo, n, qe[q], tr);
+}
+
+// ---- learned upper-bound model: GPU least squares ---------------------------------------
+// Per contig: root regression of position on key (centred), then per leaf a regression over
+// the contiguous key range the root sends to it, then the leaf's max error.
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) v += __shfl_xor_sync(kFull, v, d);
+    return v;
+}
+
+__device__ double block_sum(double v, double* red) {
+    v = warp_sum(v);
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    __syncthreads();
+    if (lane == 0) red[w] = v;
+    __syncthreads();
+    double t = 0;
+    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) t += red[k];
+    return t;
+}
+
+// acc[g] += {sum x, sum x^2-ish}: pass 1 sums keys, pass 2 sums centred products.
+template <typename S>
+__global__ void k_root_sums(const S* __restrict__ starts, const int64_t* __restrict__ seg, int G,
+                            const double* __restrict__ mean_x, double* __restrict__ acc, int pass) {
+    __shared__ double red[32];
+    for (int g = blockIdx.y; g < G; g += gridDim.y) {
+        const int64_t lo = seg[g], n = seg[g + 1] - lo;
+        const double my = 0.5 * (double)(n - 1);
+        double a0 = 0, a1 = 0;
+        for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+            const double x = (double)starts[lo + k];
+            if (pass == 0) {
+                a0 += x;
+            } else {
+                const double dx = x - mean_x[g], dy = (double)k - my;
+                a0 += dx * dy;
+                a1 += dx * dx;
+            }
+        }
+        a0 = block_sum(a0, red);
+        a1 = block_sum(a1, red);
+        if (threadIdx.x == 0) {
+            atomicAdd(&acc[2 * g], a0);
+            atomicAdd(&acc[2 * g + 1], a1);
+        }
+    }
+}
+
+// leaf boundaries: bnd[base_g + l] = first local position whose root leaf >= l
+template <typename S>
+__global__ void k_leaf_bounds(const S* __restrict__ starts, const int64_t* __restrict__ seg, int G,
+                              const double2* __restrict__ root, const double* __restrict__ mean_x,
+                              const int32_t* __restrict__ leaf_base, int32_t* __restrict__ bnd) {
+    const int g = blockIdx.y;
+    const int64_t lo = seg[g], n = seg[g + 1] - lo;
+    const int base = leaf_base[g], nl = leaf_base[g + 1] - base;
+    for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+        auto leaf_of = [&](int64_t kk) {
+            const double lf = root[g].x * ((double)starts[lo + kk] - mean_x[g]) + root[g].y;
+            return lf <= 0.0 ? 0 : (lf >= (double)(nl - 1) ? nl - 1 : (int)lf);
+        };
+        const int lk = leaf_of(k);
+        const int lp = (k == 0) ? -1 : leaf_of(k - 1);
+        for (int l = lp + 1; l <= lk; ++l) bnd[base + l] = (int32_t)k;
+    }
+}
+
+template <typename S>
+__global__ void k_leaf_fit(const S* __restrict__ starts, const int64_t* __restrict__ seg,
+                           const int32_t* __restrict__ leaf_contig, const int32_t* __restrict__ leaf_base,
+                           const int32_t* __restrict__ bnd, const double* __restrict__ mean_x,
+                           LeafModel* __restrict__ leaves, int total) {
+    __shared__ double red[32];
+    __shared__ int ired[2][32];
+    for (int L = blockIdx.x; L < total; L += gridDim.x) {
+        const int g = leaf_contig[L];
+        const int64_t lo = seg[g];
+        const int l = L - leaf_base[g];
+        const int nl = leaf_base[g + 1] - leaf_base[g];
+        const int64_t a = bnd[L];
+        const int64_t b = (l + 1 < nl) ? (int64_t)bnd[L + 1] : (seg[g + 1] - lo);
+        const int64_t cnt = b - a;
+        LeafModel M;
+        if (cnt <= 0) {
+            if (threadIdx.x == 0) {
+                M.x0 = 0;
+                M.slope = 0;
+                M.y0 = (double)a;
+                M.err_lo = 1;
+                M.err_hi = 1;
+                leaves[L] = M;
+            }
+            __syncthreads();
+            continue;
+        }
+        double sx = 0;
+        for (int64_t k = a + threadIdx.x; k < b; k += blockDim.x) sx += (double)starts[lo + k] - mean_x[g];
+        sx = block_sum(sx, red);
+        const double x0 = sx / (double)cnt;
+        const double y0 = 0.5 * (double)(a + b - 1);
+        double sxy = 0, sxx = 0;
+        for (int64_t k = a + threadIdx.x; k < b; k += blockDim.x) {
+            const double dx = (double)starts[lo + k] - mean_x[g] - x0, dy = (double)k - y0;
+            sxy += dx * dy;
+            sxx += dx * dx;
+        }
+        sxy = block_sum(sxy, red);
+        sxx = block_sum(sxx, red);
+        const double slope = (sxx > 0.0 && sxy > 0.0) ? sxy / sxx : 0.0;
+        int elo = 0, ehi = 0;
+        for (int64_t k = a + threadIdx.x; k < b; k += blockDim.x) {
+            const double pred = y0 + slope * ((double)starts[lo + k] - mean_x[g] - x0);
+            const double e = (double)k - pred;
+            if (e > 0) ehi = max(ehi, (int)ceil(e));
+            else elo = max(elo, (int)ceil(-e));
+        }
+#pragma unroll
+        for (int d = 16; d > 0; d >>= 1) {
+            elo = max(elo, __shfl_xor_sync(kFull, elo, d));
+            ehi = max(ehi, __shfl_xor_sync(kFull, ehi, d));
+        }
+        __syncthreads();
+        if ((threadIdx.x & 31) == 0) {
+            ired[0][threadIdx.x >> 5] = elo;
+            ired[1][threadIdx.x >> 5] = ehi;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            for (int w = 1; w < (int)(blockDim.x >> 5); ++w) {
+                elo = max(elo, ired[0][w]);
+                ehi = max(ehi, ired[1][w]);
+            }
+            M.x0 = x0;
+            M.slope = slope;
+            M.y0 = y0;
+            M.err_lo = elo;
+            M.err_hi = ehi;
+            leaves[L] = M;
+        }
+        __syncthreads();
+    }
+}
+
+template <typename S>
+__global__ void k_eytz_build(const S* __restrict__ starts, const int64_t* __restrict__ seg, int G, int K,
+                             S* __restrict__ keys) {
+    const int g = blockIdx.y;
+    const int64_t lo = seg[g], n = seg[g + 1] - lo;
+    const int levels = 31 - __clz(K + 1);
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i <= K; i += gridDim.x * blockDim.x) {
+        S key = Lim<S>::hi;
+        if (i >= 1 && n > 0) {
+            const int lvl = 31 - __clz(i);
+            const int64_t off = i - (1 << lvl);
+            const int below = levels - 1 - lvl;
+            const int64_t r = ((2 * off + 1) << below) - 1;
+            key = starts[lo + eytz_sample_pos(r, n, K)];
+        }
+        keys[(int64_t)g * (K + 1) + i] = key;
+    }
+}
+
+inline unsigned nblk(int64_t n, int t = kThreads) { return (unsigned)std::max<int64_t>(1, ceil_div(n, t)); }
+
+template <typename S>
+Pyr<S> make_pyr(MapView<S> m, Levels<S> L, int H) {
+    Pyr<S> P;
+    P.ends = m.ends;
+    for (int h = 0; h < kMaxLevels; ++h) P.m[h] = L.p[h];
+    P.H = H;
+    return P;
+}
+
+template <typename S>
+UbView<S> make_ub(const BatchedWorkspace& ws, int mode) {
+    UbView<S> U;
+    U.mode = mode;
+    U.root = ws.ub.root.as<double2>();
+    U.leaf_base = ws.ub.leaf_base.as<int32_t>();
+    U.leaves = ws.ub.leaves.as<LeafModel>();
+    U.key_mean = ws.ub.key_mean.as<double>();
+    U.eytz_keys = ws.ub.eytz_keys.as<S>();
+    U.eytz_n = ws.ub.eytz_n;
+    if (mode == SI_UB_LEARNED && (!U.leaves || ws.ub.total_leaves == 0)) U.mode = SI_UB_BINARY;
+    if (mode == SI_UB_EYTZINGER && ws.ub.eytz_n <= 1) U.mode = SI_UB_BINARY;
+    return U;
+}
+
+size_t tile_smem(const BatchedParams& p, size_t s) {
+    return (size_t)p.cap * (s + 4) + (size_t)p.tile_q * (s + 12) + 64;
+}
+
+#define SI_CU(call)                                    \
+    do {                                               \
+        if ((call) != cudaSuccess) return SI_ERR_CUDA; \
+    } while (0)
+#define SI_OKR(call)                     \
+    do {                                 \
+        int r_ = (call);                 \
+        if (r_ != SI_OK) return r_;      \
+    } while (0)
+
+template <typename S>
+int build_learned(BatchedWorkspace& ws, MapView<S> m, cudaStream_t st) {
+    const int G = m.G;
+    std::vector<int64_t> seg(G + 1);
+    SI_CU(cudaMemcpyAsync(seg.data(), m.seg, sizeof(int64_t) * (G + 1), cudaMemcpyDeviceToHost, st));
+    SI_CU(cudaStreamSynchronize(st));
+    std::vector<int32_t> base(G + 1, 0), leaf_contig;
+    for (int g = 0; g < G; ++g) {
+        const int64_t n = seg[g + 1] - seg[g];
+        const int nl = (int)std::min<int64_t>(4096, std::max<int64_t>(1, n / 64));
+        base[g + 1] = base[g] + nl;
+        for (int l = 0; l < nl; ++l) leaf_contig.push_back(g);
+    }
+    const int total = base[G];
+    ws.ub.total_leaves = total;
+    DBuf acc, lc, bnd;
+    SI_OKR(acc.reserve(sizeof(double) * 2 * G));
+    SI_OKR(ws.ub.key_mean.reserve(sizeof(double) * G));
+    SI_OKR(ws.ub.root.reserve(sizeof(double2) * G));
+    SI_OKR(ws.ub.leaf_base.reserve(sizeof(int32_t) * (G + 1)));
+    SI_OKR(ws.ub.leaves.reserve(sizeof(LeafModel) * std::max(total, 1)));
+    SI_OKR(lc.reserve(sizeof(int32_t) * std::max(total, 1)));
+    SI_OKR(bnd.reserve(sizeof(int32_t) * std::max(total, 1)));
+    SI_CU(cudaMemcpyAsync(ws.ub.leaf_base.p, base.data(), sizeof(int32_t) * (G + 1), cudaMemcpyHostToDevice, st));
+    SI_CU(cudaMemcpyAsync(lc.p, leaf_contig.data(), sizeof(int32_t) * total, cudaMemcpyHostToDevice, st));
+    // pass 1: mean key per contig
+    SI_CU(cudaMemsetAsync(acc.p, 0, sizeof(double) * 2 * G, st));
+    dim3 grid(64, (unsigned)std::min(G, 65535));
+    k_root_sums<S><<<grid, kThreads, 0, st>>>(m.starts, m.seg, G, nullptr, acc.as<double>(), 0);
+    SI_CU(cudaGetLastError());
+    std::vector<double> a(2 * G), mean(G);
+    SI_CU(cudaMemcpyAsync(a.data(), acc.p, sizeof(double) * 2 * G, cudaMemcpyDeviceToHost, st));
+    SI_CU(cudaStreamSynchronize(st));
+    for (int g = 0; g < G; ++g) {
+        const int64_t n = seg[g + 1] - seg[g];
+        mean[g] = n > 0 ? a[2 * g] / (double)n : 0.0;
+    }
+    SI_CU(cudaMemcpyAsync(ws.ub.key_mean.p, mean.data(), sizeof(double) * G, cudaMemcpyHostToDevice, st));
+    // pass 2: centred products -> root slope; root maps key to leaf coordinate
+    SI_CU(cudaMemsetAsync(acc.p, 0, sizeof(double) * 2 * G, st));
+    k_root_sums<S><<<grid, kThreads, 0, st>>>(m.starts, m.seg, G, ws.ub.key_mean.as<double>(), acc.as<double>(), 1);
+    SI_CU(cudaGetLastError());
+    SI_CU(cudaMemcpyAsync(a.data(), acc.p, sizeof(double) * 2 * G, cudaMemcpyDeviceToHost, st));
+    SI_CU(cudaStreamSynchronize(st));
+    std::vector<double2> root(G);
+    for (int g = 0; g < G; ++g) {
+        const int64_t n = seg[g + 1] - seg[g];
+        const int nl = base[g + 1] - base[g];
+        const double slope_pos = (a[2 * g + 1] > 0 && a[2 * g] > 0) ? a[2 * g] / a[2 * g + 1] : 0.0;
+        const double scale = n > 0 ? (double)nl / (double)n : 0.0;
+        // position ~ my + slope * (x - mean); leaf = position * nl / n
+        root[g] = make_double2(slope_pos * scale, 0.5 * (double)(n - 1) * scale);
+    }
+    SI_CU(cudaMemcpyAsync(ws.ub.root.p, root.data(), sizeof(double2) * G, cudaMemcpyHostToDevice, st));
+    SI_CU(cudaMemsetAsync(bnd.p, 0x7f, sizeof(int32_t) * total, st));
+    k_leaf_bounds<S><<<dim3(256, G), kThreads, 0, st>>>(m.starts, m.seg, G, ws.ub.root.as<double2>(),
+                                                        ws.ub.key_mean.as<double>(), ws.ub.leaf_base.as<int32_t>(),
+                                                        bnd.as<int32_t>());
+    SI_CU(cudaGetLastError());
+    // leaves never reached by any key keep INT32_MAX-ish: clamp to the contig size on the host
+    std::vector<int32_t> hb(total);
+    SI_CU(cudaMemcpyAsync(hb.data(), bnd.p, sizeof(int32_t) * total, cudaMemcpyDeviceToHost, st));
+    SI_CU(cudaStreamSynchronize(st));
+    for (int g = 0; g < G; ++g) {
+        const int32_t n = (int32_t)(seg[g + 1] - seg[g]);
+        for (int l = base[g]; l < base[g + 1]; ++l)
+            if (hb[l] > n) hb[l] = n;
+    }
+    SI_CU(cudaMemcpyAsync(bnd.p, hb.data(), sizeof(int32_t) * total, cudaMemcpyHostToDevice, st));
+    k_leaf_fit<S><<<(unsigned)std::min(total, 152 * 32), kThreads, 0, st>>>(
+        m.starts, m.seg, lc.as<int32_t>(), ws.ub.leaf_base.as<int32_t>(), bnd.as<int32_t>(),
+        ws.ub.key_mean.as<double>(), ws.ub.leaves.as<LeafModel>(), total);
+    SI_CU(cudaGetLastError());
+    SI_CU(cudaStreamSynchronize(st));
+    ws.launches += 5;
     return SI_OK;
 }
 
 template <typename S>
-int batched_count(BatchedWorkspace&, MapView<S> m, Levels<S>, int, const QueryBatch& q, uint32_t* counts,
-                  int* d_err, int, cudaStream_t st) {
-    return launch_count_plain<S>(m, q, counts, d_err, st) == cudaSuccess ? SI_OK : SI_ERR_CUDA;
+int build_eytz(BatchedWorkspace& ws, MapView<S> m, cudaStream_t st) {
+    const int G = m.G;
+    int depth = ws.prm.eytz_depth;
+    if (depth <= 0) {
+        // shared-memory budget: at most 8191 keys, and no deeper than the average contig
+        const int64_t avg = std::max<int64_t>(1, m.n / std::max(1, G));
+        depth = 1;
+        while (depth < 13 && ((int64_t)1 << (depth + 1)) <= avg / 4) ++depth;
+    }
+    const int K = (1 << depth) - 1;
+    ws.ub.eytz_depth = depth;
+    ws.ub.eytz_n = K + 1;
+    SI_OKR(ws.ub.eytz_keys.reserve(sizeof(S) * (size_t)G * (K + 1)));
+    k_eytz_build<S><<<dim3(nblk(K + 1), G), kThreads, 0, st>>>(m.starts, m.seg, G, K, ws.ub.eytz_keys.as<S>());
+    SI_CU(cudaGetLastError());
+    SI_CU(cudaStreamSynchronize(st));
+    ws.launches += 1;
+    return SI_OK;
+}
+
+}  // namespace
+
+template <typename S>
+int batched_prepare(BatchedWorkspace& ws, MapView<S> m, Levels<S>, int, const int64_t*, int ub_mode,
+                    cudaStream_t st) {
+    ws.prepared_nq = -1;
+    ws.prepared_qs = nullptr;
+    ws.ub.mode = ub_mode;
+    ws.ub.G = m.G;
+    ws.ub.total_leaves = 0;
+    ws.ub.eytz_n = 0;
+    if (m.n == 0) return SI_OK;
+    if (ub_mode == SI_UB_LEARNED) return build_learned<S>(ws, m, st);
+    if (ub_mode == SI_UB_EYTZINGER) return build_eytz<S>(ws, m, st);
+    return SI_OK;
 }
 
 template <typename S>
-int batched_emit(BatchedWorkspace&, MapView<S> m, Levels<S>, int, const QueryBatch& q, const int64_t* offsets,
-                 int64_t out_base, int order, bool values, int32_t* out, int* d_err, int, cudaStream_t st) {
-    return launch_emit_plain<S>(m, q, offsets, out_base, order, values, out, d_err, st) == cudaSuccess
-               ? SI_OK
-               : SI_ERR_CUDA;
+int batched_prepare_queries(BatchedWorkspace& ws, MapView<S> m, const QueryBatch& q, int* d_err, int ub_mode,
+                            cudaStream_t st) {
+    const int64_t nq = q.nq;
+    ws.prepared_nq = -1;
+    if (nq <= 0) return SI_OK;
+    if (nq >= (int64_t)INT32_MAX) return SI_ERR_TOO_LARGE;
+    const int K = (sizeof(S) == 4) ? 2 : 3;
+    uint32_t* kp[3];
+    uint32_t* ka[3];
+    for (int k = 0; k < K; ++k) {
+        SI_OKR(ws.kw[k].reserve(sizeof(uint32_t) * nq));
+        SI_OKR(ws.kalt[k].reserve(sizeof(uint32_t) * nq));
+        kp[k] = ws.kw[k].as<uint32_t>();
+        ka[k] = ws.kalt[k].as<uint32_t>();
+    }
+    SI_OKR(ws.pay.reserve(sizeof(uint32_t) * nq));
+    SI_OKR(ws.palt.reserve(sizeof(uint32_t) * nq));
+    const size_t tb = radix_temp_bytes(nq, K);
+    SI_OKR(ws.sort_tmp.reserve(tb));
+    SI_OKR(ws.sq_s.reserve(sizeof(S) * nq));
+    SI_OKR(ws.sq_u.reserve(sizeof(int32_t) * nq));
+    SI_OKR(ws.sq_c.reserve(sizeof(uint32_t) * nq));
+    SI_OKR(ws.sq_id.reserve(sizeof(int32_t) * nq));
+    uint32_t* wc = kp[K - 1];
+    k_qkeys<S><<<nblk(nq), kThreads, 0, st>>>(static_cast<const S*>(q.qs), static_cast<const S*>(q.qe), q.qc, nq,
+                                              ws.prm.long_len, kp[0], K == 3 ? kp[1] : nullptr, wc,
+                                              ws.pay.as<uint32_t>());
+    SI_CU(cudaGetLastError());
+    bool in_alt = false;
+    int passes = 0;
+    SI_CU(radix_sort(kp, ka, ws.pay.as<uint32_t>(), ws.palt.as<uint32_t>(), K, nq, ws.sort_tmp.p, tb, &in_alt,
+                     &passes, st));
+    const uint32_t* spay = in_alt ? ws.palt.as<uint32_t>() : ws.pay.as<uint32_t>();
+    const uint32_t* swc = in_alt ? ka[K - 1] : kp[K - 1];
+    UbView<S> U = make_ub<S>(ws, ub_mode);
+    const size_t sm = (U.mode == 1) ? sizeof(S) * (size_t)U.eytz_n : 0;
+    k_qprep<S><<<nblk(nq), kThreads, sm, st>>>(spay, swc, static_cast<const S*>(q.qs), static_cast<const S*>(q.qe),
+                                              nq, m, U, ws.sq_s.as<S>(), ws.sq_u.as<int32_t>(),
+                                              ws.sq_c.as<uint32_t>(), ws.sq_id.as<int32_t>(), d_err);
+    SI_CU(cudaGetLastError());
+    ws.launches += 2 + 3 * passes + 1;
+    ws.prepared_qs = q.qs;
+    ws.prepared_nq = nq;
+    ws.prepared_mode = ub_mode;
+    return SI_OK;
 }
 
-#define SIG_BINST(S)                                                                                  \
-    template int batched_prepare<S>(BatchedWorkspace&, MapView<S>, Levels<S>, int, const int64_t*, int, \
-                                    cudaStream_t);                                                   \
-    template int batched_count<S>(BatchedWorkspace&, MapView<S>, Levels<S>, int, const QueryBatch&,    \
-                                  uint32_t*, int*, int, cudaStream_t);                               \
-    template int batched_emit<S>(BatchedWorkspace&, MapView<S>, Levels<S>, int, const QueryBatch&,     \
-                                 const int64_t*, int64_t, int, bool, int32_t*, int*, int, cudaStream_t);
+template <typename S>
+static int run_tiles(BatchedWorkspace& ws, MapView<S> m, Levels<S> L, int H, int64_t nq, bool emit,
+                     uint32_t* counts, int32_t* heads, const int32_t* heads_in, const int64_t* offsets,
+                     int64_t out_base, int order, bool values, int32_t* out, int* d_err, cudaStream_t st) {
+    SI_OKR(ws.counters.reserve(sizeof(int) * 4));
+    SI_CU(cudaMemsetAsync(ws.counters.p, 0, sizeof(int) * 4, st));
+    TileArgs<S> a;
+    a.P = make_pyr<S>(m, L, H);
+    a.data = m.data;
+    a.seg = m.seg;
+    a.G = m.G;
+    a.sq_s = ws.sq_s.as<S>();
+    a.sq_u = ws.sq_u.as<int32_t>();
+    a.sq_c = ws.sq_c.as<uint32_t>();
+    a.sq_id = ws.sq_id.as<int32_t>();
+    a.nq = nq;
+    a.tile_q = ws.prm.tile_q;
+    a.cap = ws.prm.cap;
+    a.n_tiles = (int)ceil_div(nq, a.tile_q);
+    a.tile_counter = ws.counters.as<int>();
+    a.counts = counts;
+    a.heads = heads;
+    a.heads_in = heads_in;
+    a.offsets = offsets;
+    a.out_base = out_base;
+    a.order = order;
+    a.values = values;
+    a.out = out;
+    a.d_err = d_err;
+    const size_t sm = tile_smem(ws.prm, sizeof(S));
+    int dev = 0, nsm = 152, per_sm = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    if (emit) {
+        SI_CU(cudaFuncSetAttribute(k_tiles<S, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        SI_CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tiles<S, true>, kThreads, sm));
+    } else {
+        SI_CU(cudaFuncSetAttribute(k_tiles<S, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        SI_CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tiles<S, false>, kThreads, sm));
+    }
+    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)nsm * std::max(per_sm, 1), a.n_tiles));
+    if (emit) k_tiles<S, true><<<grid, kThreads, sm, st>>>(a);
+    else k_tiles<S, false><<<grid, kThreads, sm, st>>>(a);
+    SI_CU(cudaGetLastError());
+    ws.launches += 1;
+    return SI_OK;
+}
+
+template <typename S>
+int batched_count(BatchedWorkspace& ws, MapView<S> m, Levels<S> L, int H, const QueryBatch& q, uint32_t* counts,
+                  int* d_err, cudaStream_t st) {
+    const int64_t nq = q.nq;
+    if (nq <= 0) return SI_OK;
+    if (ws.prepared_nq != nq || ws.prepared_qs != q.qs) return SI_ERR_INVALID;
+    SI_OKR(ws.heads.reserve(sizeof(int32_t) * nq));
+    ws.n_heads = nq;
+    return run_tiles<S>(ws, m, L, H, nq, false, counts, ws.heads.as<int32_t>(), nullptr, nullptr, 0, 0, false,
+                        nullptr, d_err, st);
+}
+
+template <typename S>
+int batched_emit(BatchedWorkspace& ws, MapView<S> m, Levels<S> L, int H, const QueryBatch& q, int64_t q_offset,
+                 const int64_t* offsets, int64_t out_base, int order, bool values, int32_t* out, int* d_err,
+                 int ub_mode, cudaStream_t st) {
+    const int64_t nq = q.nq;
+    if (nq <= 0) return SI_OK;
+    if (q_offset < 0 || q_offset + nq > ws.n_heads) return SI_ERR_INVALID;
+    const bool same = (q_offset == 0 && ws.prepared_nq == nq && ws.prepared_qs == q.qs);
+    if (!same) SI_OKR(batched_prepare_queries<S>(ws, m, q, d_err, ub_mode, st));
+    // sorted ids are relative to q; heads / offsets are shifted to the slice
+    return run_tiles<S>(ws, m, L, H, nq, true, nullptr, nullptr, ws.heads.as<int32_t>() + q_offset, offsets,
+                        out_base, order, values, out, d_err, st);
+}
+
+template <typename S>
+int upper_bounds(BatchedWorkspace& ws, MapView<S> m, const QueryBatch& q, int ub_mode, int32_t* out, int* d_err,
+                 cudaStream_t st) {
+    if (q.nq <= 0) return SI_OK;
+    UbView<S> U = make_ub<S>(ws, ub_mode);
+    k_ub_plain<S><<<nblk(q.nq), kThreads, 0, st>>>(static_cast<const S*>(q.qe), q.qc, q.nq, m, U, out, d_err);
+    SI_CU(cudaGetLastError());
+    ws.launches += 1;
+    return SI_OK;
+}
+
+#define SIG_BINST(S)                                                                                             \
+    template int batched_prepare<S>(BatchedWorkspace&, MapView<S>, Levels<S>, int, const int64_t*, int,            \
+                                    cudaStream_t);                                                              \
+    template int batched_prepare_queries<S>(BatchedWorkspace&, MapView<S>, const QueryBatch&, int*, int,          \
+                                            cudaStream_t);                                                      \
+    template int batched_count<S>(BatchedWorkspace&, MapView<S>, Levels<S>, int, const QueryBatch&, uint32_t*,   \
+                                  int*, cudaStream_t);                                                          \
+    template int batched_emit<S>(BatchedWorkspace&, MapView<S>, Levels<S>, int, const QueryBatch&, int64_t,      \
+                                 const int64_t*, int64_t, int, bool, int32_t*, int*, int, cudaStream_t);        \
+    template int upper_bounds<S>(BatchedWorkspace&, MapView<S>, const QueryBatch&, int, int32_t*, int*,          \
+                                 cudaStream_t);
 SIG_BINST(int32_t)
 SIG_BINST(int64_t)
 

@@ -4,23 +4,87 @@
 
 namespace sig {
 
-// Per-handle state of the batched path: query-sort buffers and the per-contig
-// upper-bound accelerators.  Grown on demand, released with the handle.
+// Device allocation through the library's budgeted allocator (si_capi.cu).
+int dev_reserve(void** p, size_t* bytes, size_t need);
+void dev_release(void** p, size_t* bytes);
+
+struct DBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    DBuf() = default;
+    DBuf(const DBuf&) = delete;
+    DBuf& operator=(const DBuf&) = delete;
+    ~DBuf() { dev_release(&p, &bytes); }
+    int reserve(size_t need) { return dev_reserve(&p, &bytes, need); }
+    template <typename T>
+    T* as() const {
+        return static_cast<T*>(p);
+    }
+};
+
+// Tunables of the batched path (picked by the autotuner, see si_autotune in the C-ABI).
+struct BatchedParams {
+    int tile_q = 256;            // sorted queries per tile
+    int cap = 2048;              // candidate slots per tile (shared memory)
+    int64_t long_len = 16384;    // queries longer than this take the per-query walk
+    int eytz_depth = 0;          // 0: automatic
+};
+
+// Per-contig upper-bound accelerators built once per index.
+struct UpperBoundModel {
+    int mode = 0;                // SI_UB_*
+    int G = 0;
+    // learned: two-stage piecewise-linear model per contig
+    DBuf root;                   // double2 per contig: (slope, intercept) of key -> leaf
+    DBuf leaf_base;              // int32 per contig+1: first leaf of each contig
+    DBuf leaves;                 // LeafModel per leaf
+    DBuf key_mean;               // double per contig: key offset for conditioning
+    int total_leaves = 0;
+    int leaves_per_contig = 0;
+    // eytzinger: top levels of each contig, laid out breadth-first
+    DBuf eytz_keys;              // S[G * eytz_n]
+    DBuf eytz_pos;               // int32[G * eytz_n]: position of each sampled key
+    int eytz_n = 0;              // keys per contig (2^depth - 1)
+    int eytz_depth = 0;
+};
+
 struct BatchedWorkspace {
-    void* blocks[16] = {nullptr};
-    size_t bytes[16] = {0};
-    ~BatchedWorkspace();
+    BatchedParams prm;
+    UpperBoundModel ub;
+    // query sort
+    DBuf kw[3], kalt[3], pay, palt, sort_tmp;
+    // sorted query records
+    DBuf sq_s, sq_u, sq_c, sq_id;
+    DBuf heads;                  // head-run length per query (original order)
+    DBuf counters;               // work-queue counters
+    // identity of the batch the sorted records belong to
+    const void* prepared_qs = nullptr;
+    int64_t prepared_nq = -1;
+    int prepared_mode = -1;
+    int64_t n_heads = 0;
+    long long launches = 0;      // kernels launched by this path
 };
 
 template <typename S>
 int batched_prepare(BatchedWorkspace& ws, MapView<S> m, Levels<S> L, int H, const int64_t* lvl_sizes,
                     int ub_mode, cudaStream_t st);
+// Sorts the queries by (class, contig, end) and finds each one's upper bound.
+template <typename S>
+int batched_prepare_queries(BatchedWorkspace& ws, MapView<S> m, const QueryBatch& q, int* d_err,
+                            int ub_mode, cudaStream_t st);
 template <typename S>
 int batched_count(BatchedWorkspace& ws, MapView<S> m, Levels<S> L, int H, const QueryBatch& q,
-                  uint32_t* counts, int* d_err, int ub_mode, cudaStream_t st);
+                  uint32_t* counts, int* d_err, cudaStream_t st);
+// q may be a slice [q_offset, q_offset + q.nq) of the batch counted last.
 template <typename S>
 int batched_emit(BatchedWorkspace& ws, MapView<S> m, Levels<S> L, int H, const QueryBatch& q,
-                 const int64_t* offsets, int64_t out_base, int order, bool values, int32_t* out,
-                 int* d_err, int ub_mode, cudaStream_t st);
+                 int64_t q_offset, const int64_t* offsets, int64_t out_base, int order, bool values,
+                 int32_t* out, int* d_err, int ub_mode, cudaStream_t st);
+
+// Upper bound of every query (original order) with the handle's accelerator; used by
+// the plain path when a learned / Eytzinger mode is selected, and by tests.
+template <typename S>
+int upper_bounds(BatchedWorkspace& ws, MapView<S> m, const QueryBatch& q, int ub_mode, int32_t* out,
+                 int* d_err, cudaStream_t st);
 
 }  // namespace sig

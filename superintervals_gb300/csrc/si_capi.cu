@@ -90,6 +90,35 @@ struct DevBuf {
 
 }  // namespace
 
+namespace sig {
+int dev_reserve(void** p, size_t* bytes, size_t need) {
+    if (*p && need <= *bytes) return SI_OK;
+    dev_release(p, bytes);
+    if (need == 0) need = 256;
+    need = (need + 255) & ~(size_t)255;
+    const size_t cap = g_budget.load();
+    if (cap && g_used.load() + need > cap)
+        return fail(SI_ERR_OOM, "device budget exceeded: %zu in use + %zu requested > %zu", g_used.load(), need, cap);
+    cudaError_t e = cudaMalloc(p, need);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        *p = nullptr;
+        return fail(SI_ERR_OOM, "cudaMalloc(%zu) failed: %s", need, cudaGetErrorString(e));
+    }
+    *bytes = need;
+    g_used += need;
+    return SI_OK;
+}
+void dev_release(void** p, size_t* bytes) {
+    if (*p) {
+        cudaFree(*p);
+        g_used -= *bytes;
+    }
+    *p = nullptr;
+    *bytes = 0;
+}
+}  // namespace sig
+
 struct gSuperIntervals {
     int bits = 32;
     int device = 0;
@@ -336,24 +365,32 @@ int run_count(gSuperIntervals* si, const sig::QueryBatch& q, uint32_t* d_counts,
         SI_CK(cudaMemsetAsync(d_counts, 0, sizeof(uint32_t) * std::max<int64_t>(q.nq, 1), st));
         return SI_OK;
     }
-    PhaseTimer pt(si, 0, st);
     if (use_batched(si, q.nq)) {
-        SI_TRY(sig::batched_count<S>(si->bws, view<S>(si), levels<S>(si), si->H, q, d_counts,
-                                     si->w_err.as<int>(), si->ub_mode, st));
+        {
+            PhaseTimer pt(si, 3, st);
+            int r = sig::batched_prepare_queries<S>(si->bws, view<S>(si), q, si->w_err.as<int>(), si->ub_mode, st);
+            if (r != SI_OK) return fail(r, "batched query preparation failed (status %d)", r);
+        }
+        PhaseTimer pt(si, 0, st);
+        int r = sig::batched_count<S>(si->bws, view<S>(si), levels<S>(si), si->H, q, d_counts, si->w_err.as<int>(), st);
+        if (r != SI_OK) return fail(r, "batched count failed (status %d)", r);
     } else {
+        PhaseTimer pt(si, 0, st);
         SI_CK(sig::launch_count_plain<S>(view<S>(si), q, d_counts, si->w_err.as<int>(), st));
     }
     return SI_OK;
 }
 
+// q may be a slice starting at query q_offset of the batch counted last.
 template <typename S>
-int run_emit(gSuperIntervals* si, const sig::QueryBatch& q, const int64_t* d_offsets, int64_t out_base,
-             int order, bool values, int32_t* d_out, cudaStream_t st) {
+int run_emit(gSuperIntervals* si, const sig::QueryBatch& q, int64_t q_offset, const int64_t* d_offsets,
+             int64_t out_base, int order, bool values, int32_t* d_out, cudaStream_t st) {
     if (si->n == 0 || q.nq == 0) return SI_OK;
     PhaseTimer pt(si, 2, st);
-    if (use_batched(si, q.nq)) {
-        SI_TRY(sig::batched_emit<S>(si->bws, view<S>(si), levels<S>(si), si->H, q, d_offsets, out_base,
-                                    order, values, d_out, si->w_err.as<int>(), si->ub_mode, st));
+    if (use_batched(si, q.nq + q_offset)) {
+        int r = sig::batched_emit<S>(si->bws, view<S>(si), levels<S>(si), si->H, q, q_offset, d_offsets, out_base,
+                                     order, values, d_out, si->w_err.as<int>(), si->ub_mode, st);
+        if (r != SI_OK) return fail(r, "batched emit failed (status %d)", r);
     } else {
         SI_CK(sig::launch_emit_plain<S>(view<S>(si), q, d_offsets, out_base, order, values, d_out,
                                         si->w_err.as<int>(), st));
@@ -379,7 +416,7 @@ int search_device(gSuperIntervals* si, const sig::QueryBatch& q, int order, bool
     SI_CK(cudaStreamSynchronize(st));
     if (total) *total = (size_t)P;
     if ((size_t)P > cap) return fail(SI_ERR_CAPACITY, "output needs %lld values, capacity %zu", (long long)P, cap);
-    SI_TRY(run_emit<S>(si, q, d_offsets, 0, order, values, d_out, st));
+    SI_TRY(run_emit<S>(si, q, 0, d_offsets, 0, order, values, d_out, st));
     return read_dev_err(si);
 }
 
@@ -477,7 +514,7 @@ int search_host(gSuperIntervals* si, const S* qs, const S* qe, const int32_t* qc
         sub.qe = static_cast<const S*>(q.qe) + qa;
         sub.qc = q.qc ? q.qc + qa : nullptr;
         sub.nq = (int64_t)(qb - qa);
-        SI_TRY(run_emit<S>(si, sub, d_off + qa, h_off[qa], order, values, si->w_out.as<int32_t>(), st));
+        SI_TRY(run_emit<S>(si, sub, (int64_t)qa, d_off + qa, h_off[qa], order, values, si->w_out.as<int32_t>(), st));
         if (need)
             SI_CK(cudaMemcpyAsync(h_out + h_off[qa], si->w_out.p, sizeof(int32_t) * need,
                                   cudaMemcpyDeviceToHost, st));
@@ -876,3 +913,25 @@ int flushL2Gpu(void* stream) {
 }
 
 }  // extern "C"
+
+extern "C" int upperBoundDeviceGpu(gSuperIntervals* si, const void* d_qe, const int32_t* d_qc, size_t nq, int mode,
+                                   int32_t* d_out, void* stream) {
+    SI_TRY(check_built(si));
+    SI_TRY(set_dev(si));
+    if (mode != SI_UB_BINARY && mode != si->ub_mode)
+        return fail(SI_ERR_INVALID, "upper-bound mode %d is not prepared on this handle (current %d)", mode,
+                    si->ub_mode);
+    cudaStream_t st = stream ? (cudaStream_t)stream : si->st;
+    SI_TRY(si->w_err.reserve(sizeof(int)));
+    SI_CK(cudaMemsetAsync(si->w_err.p, 0, sizeof(int), st));
+    if (si->n == 0) {
+        if (nq) SI_CK(cudaMemsetAsync(d_out, 0xff, sizeof(int32_t) * nq, st));
+        return SI_OK;
+    }
+    sig::QueryBatch q{d_qe, d_qe, d_qc, (int64_t)nq};
+    int r = si->bits == 64
+                ? sig::upper_bounds<int64_t>(si->bws, view<int64_t>(si), q, mode, d_out, si->w_err.as<int>(), st)
+                : sig::upper_bounds<int32_t>(si->bws, view<int32_t>(si), q, mode, d_out, si->w_err.as<int>(), st);
+    if (r != SI_OK) return fail(r, "upper-bound kernel failed");
+    return SI_OK;
+}

@@ -146,10 +146,83 @@ def test_config4_scaled_int64(api, oracle, path):
     idx.close()
 
 
-def test_chunked_emit_matches_unchunked(api, oracle):
+UB_MODES = ["binary", "eytzinger", "learned"]
+
+
+def _ub_const(api, mode):
+    return {"binary": api.UB_BINARY, "eytzinger": api.UB_EYTZINGER, "learned": api.UB_LEARNED}[mode]
+
+
+@pytest.mark.parametrize("mode", UB_MODES)
+@pytest.mark.parametrize("name", ["config1_plain_small_int32", "nested_dups_int64", "edges_int32",
+                                  "edges_int64", "kat_single_int32", "presorted_int32"])
+def test_batched_upper_bound_modes(api, name, mode):
+    """Batched search_idxs is bit-identical whatever provider finds the upper bounds."""
+    g = load(name)
+    idx = _index(api, g["starts"], g["ends"], g["data"], path="batched")
+    idx.set_upper_bound(_ub_const(api, mode))
+    off, out = idx.search(g["q_starts"], g["q_ends"], order=api.ORDER_IDXS_CPP)
+    assert np.array_equal(off, g["ref_search_idxs_off"])
+    assert np.array_equal(out, g["ref_search_idxs"])
+    idx.close()
+
+
+def _device_ub(api, idx, qe, qc, mode):
+    import ctypes as C
+    lib = idx.lib
+    qe = np.ascontiguousarray(qe, dtype=idx.dtype)
+    n = qe.shape[0]
+    d_qe, d_qc, d_out = C.c_void_p(), C.c_void_p(), C.c_void_p()
+    api.check(lib.deviceMallocGpu(C.byref(d_qe), max(qe.nbytes, 1)))
+    api.check(lib.deviceMallocGpu(C.byref(d_out), max(4 * n, 1)))
+    api.check(lib.memcpyGpu(d_qe, C.c_void_p(qe.ctypes.data), qe.nbytes, idx.stream))
+    if qc is not None:
+        qc = np.ascontiguousarray(qc, dtype=np.int32)
+        api.check(lib.deviceMallocGpu(C.byref(d_qc), max(qc.nbytes, 1)))
+        api.check(lib.memcpyGpu(d_qc, C.c_void_p(qc.ctypes.data), qc.nbytes, idx.stream))
+    api.check(lib.upperBoundDeviceGpu(idx.h, d_qe, d_qc if qc is not None else None, n, mode, d_out,
+                                      idx.stream))
+    out = np.empty(n, np.int32)
+    api.check(lib.memcpyGpu(C.c_void_p(out.ctypes.data), d_out, 4 * n, idx.stream))
+    api.check(lib.streamSynchronizeGpu(idx.stream))
+    for p in (d_qe, d_qc, d_out):
+        if p.value:
+            lib.deviceFreeGpu(p)
+    return out
+
+
+@pytest.mark.parametrize("mode", UB_MODES)
+def test_upper_bound_providers_exact(api, mode):
+    """Every provider returns the reference's upper_bound (hpp:501-516) for every query,
+    including values before the first start, after the last one and on duplicates."""
+    from superintervals_gb300 import workloads as W
+    for wl in (W.config4(n=400_000, nq=100_000), W.config3(n=300_000, nq=100_000),
+               W.random_nested(41, 5000, 5000, dtype=np.int64)):
+        idx = _index(api, wl.starts, wl.ends, wl.data, seg=wl.seg if len(wl.seg) > 2 else None,
+                     path="batched")
+        idx.set_upper_bound(_ub_const(api, mode))
+        s, _, _, _ = idx.arrays()
+        qe = np.concatenate([wl.q_ends, s[:1000], s[:1000] - 1, [s.min() - 5, s.max() + 5]]).astype(idx.dtype)
+        qc = None
+        if wl.q_contig is not None:
+            qc = np.concatenate([wl.q_contig, np.zeros(2002, np.int32)])
+        got = _device_ub(api, idx, qe, qc, _ub_const(api, mode))
+        segs = wl.seg
+        exp = np.empty(qe.shape[0], np.int64)
+        cid = np.zeros(qe.shape[0], np.int64) if qc is None else qc
+        for gi in range(len(segs) - 1):
+            sel = cid == gi
+            ss = s[segs[gi]:segs[gi + 1]]
+            exp[sel] = np.searchsorted(ss, qe[sel], side="right") - 1
+        assert np.array_equal(got.astype(np.int64), exp)
+        idx.close()
+
+
+@pytest.mark.parametrize("path", PATHS)
+def test_chunked_emit_matches_unchunked(api, oracle, path):
     from superintervals_gb300 import workloads as W
     wl = W.random_nested(31, 20_000, 20_000, span=500_000, max_len=5_000)
-    idx = _index(api, wl.starts, wl.ends, wl.data)
+    idx = _index(api, wl.starts, wl.ends, wl.data, path=path)
     off1, out1 = idx.search(wl.q_starts, wl.q_ends)
     idx.set_output_budget(1 << 20)       # 1 MiB: forces many chunks
     off2, out2 = idx.search(wl.q_starts, wl.q_ends)
