@@ -109,6 +109,13 @@ int getIndexArraysGpu(const gSuperIntervals* si, void* starts, void* ends, int32
 /* ---- options (no reference counterpart) ------------------------------- */
 int setQueryPathGpu(gSuperIntervals* si, int path);
 int setUpperBoundModeGpu(gSuperIntervals* si, int mode);
+/* Tunables of the batched path: sorted queries per tile, candidate slots per
+ * tile (shared memory), and the query length above which a query takes the
+ * per-query walk.  0 keeps the current value. */
+int setBatchedParamsGpu(gSuperIntervals* si, int tile_queries, int tile_candidates,
+                        int64_t long_query_len);
+int getBatchedParamsGpu(const gSuperIntervals* si, int* tile_queries, int* tile_candidates,
+                        int64_t* long_query_len);
 /* Device bytes one search call may use for its result buffer; larger results
  * are emitted in query chunks against it. */
 int setOutputBudgetGpu(gSuperIntervals* si, size_t bytes);

@@ -222,6 +222,110 @@ __device__ void walk_query(const TileArgs<S>& a, S qs, int64_t u, int64_t lo, in
     }
 }
 
+// Block-wide exclusive scan of v[0, n) in place; the total goes to *s_sum.  Ends synchronized.
+__device__ void block_excl_scan(int32_t* v, int n, int* s_wsum, int* s_sum) {
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int per = (n + kThreads - 1) / kThreads;
+    const int beg = tid * per;
+    const int end = min(beg + per, n);
+    int local = 0;
+    for (int i = beg; i < end; ++i) local += v[i];
+    int inc = local;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const int y = __shfl_up_sync(kFull, inc, d);
+        if (lane >= d) inc += y;
+    }
+    if (lane == 31) s_wsum[warp] = inc;
+    __syncthreads();
+    int woff = 0;
+    for (int w = 0; w < warp; ++w) woff += s_wsum[w];
+    int run = woff + inc - local;
+    for (int i = beg; i < end; ++i) {
+        const int t = v[i];
+        v[i] = run;
+        run += t;
+    }
+    if (tid == kThreads - 1) *s_sum = woff + inc;
+    __syncthreads();
+}
+
+// Block-wide top-down gather of C = { k in [lo, umax] : ends[k] >= L } in DESCENDING position
+// order into (cpos, cend), one level of the max pyramid per round: every warp expands frontier
+// nodes (one coalesced 32-child load + ballot each), a block scan places the surviving children
+// in order.  Frontier lists ping-pong between cpos and lst.  Returns |C|, or -1 when a frontier
+// or C would exceed `cap`.  Block-uniform.
+template <typename S>
+__device__ int gather_bfs(const Pyr<S>& P, int64_t lo, int64_t umax, S L, int cap, int32_t* cpos, S* cend,
+                          int32_t* lst, int32_t* cnt, uint32_t* msk, int* s_wsum, int* s_n, int* s_sum) {
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    if (umax < lo) return 0;
+    const int H = P.H;
+    if (warp == 0) {
+        const int64_t nlo = lo >> (5 * H), nhi = umax >> (5 * H);
+        bool ok = lane >= nlo && lane <= nhi;
+        S v = Lim<S>::lo;
+        if (ok) v = (H == 0) ? P.ends[lane] : P.m[H - 1][lane];
+        ok = ok && v >= L;
+        const unsigned m = __ballot_sync(kFull, ok);
+        if (ok) {
+            const int idx = __popc(m & above_mask(lane));
+            ((H & 1) ? lst : cpos)[idx] = lane;
+            if (H == 0) cend[idx] = v;
+        }
+        if (lane == 0) *s_n = __popc(m);
+    }
+    __syncthreads();
+    int nf = *s_n;
+    for (int h = H; h >= 1; --h) {
+        const S* A = (h == 1) ? P.ends : P.m[h - 2];
+        const int sh = 5 * (h - 1);
+        const int64_t clo = lo >> sh, chi = umax >> sh;
+        const int32_t* in = (h & 1) ? lst : cpos;
+        int32_t* out = (h & 1) ? cpos : lst;
+        for (int f0 = warp; f0 < nf; f0 += 4 * kWarpsPerCta) {
+            // up to 4 frontier nodes per warp per round: the loads are independent
+            bool ok[4];
+            S v[4];
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const int f = f0 + k * kWarpsPerCta;
+                ok[k] = false;
+                if (f < nf) {
+                    const int64_t c = ((int64_t)in[f] << 5) + lane;
+                    ok[k] = c >= clo && c <= chi;
+                    v[k] = ok[k] ? A[c] : Lim<S>::lo;
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const int f = f0 + k * kWarpsPerCta;
+                const unsigned m = __ballot_sync(kFull, ok[k] && v[k] >= L);
+                if (f < nf && lane == 0) {
+                    msk[f] = m;
+                    cnt[f] = __popc(m);
+                }
+            }
+        }
+        __syncthreads();
+        block_excl_scan(cnt, nf, s_wsum, s_sum);
+        const int total = *s_sum;
+        if (total > cap) return -1;
+        for (int f = warp; f < nf; f += kWarpsPerCta) {
+            const unsigned m = msk[f];
+            if ((m >> lane) & 1u) {
+                const int64_t c = ((int64_t)in[f] << 5) + lane;
+                const int idx = cnt[f] + __popc(m & above_mask(lane));
+                out[idx] = (int32_t)c;
+                if (h == 1) cend[idx] = A[c];
+            }
+        }
+        __syncthreads();
+        nf = total;
+    }
+    return nf;
+}
+
 template <typename S, bool EMIT>
 __global__ void __launch_bounds__(kThreads) k_tiles(TileArgs<S> a) {
     extern __shared__ __align__(16) unsigned char smem[];
@@ -232,8 +336,13 @@ __global__ void __launch_bounds__(kThreads) k_tiles(TileArgs<S> a) {
     int32_t* q_u = reinterpret_cast<int32_t*>(q_s + T);
     uint32_t* q_c = reinterpret_cast<uint32_t*>(q_u + T);
     int32_t* q_id = reinterpret_cast<int32_t*>(q_c + T);
+    int32_t* lst = q_id + T;
+    int32_t* cnt = lst + cap;
+    uint32_t* msk = reinterpret_cast<uint32_t*>(cnt + cap);
     __shared__ int s_tile, s_nc, s_over;
+    __shared__ int s_wsum[kWarpsPerCta];
     __shared__ S s_red[kWarpsPerCta];
+    int s_nc_run = 0;
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     while (true) {
@@ -277,41 +386,16 @@ __global__ void __launch_bounds__(kThreads) k_tiles(TileArgs<S> a) {
                 }
                 if (lane == 0) s_red[warp] = mn;
                 __syncthreads();
-                if (warp == 0) {
-                    S L = s_red[lane < kWarpsPerCta ? lane : 0];
+                S L = s_red[0];
 #pragma unroll
-                    for (int d = 16; d > 0; d >>= 1) {
-                        const S o = __shfl_xor_sync(kFull, L, d);
-                        L = o < L ? o : L;
-                    }
-                    const int64_t umax = q_u[r1 - 1];
-                    int nc = 0;
-                    bool over = false;
-                    if (umax >= lo) {
-                        scan_desc(a.P, lo, umax, L, lane, [&](int64_t ch, unsigned hm, S v) {
-                            const int k = __popc(hm);
-                            if (nc + k > cap) {
-                                over = true;
-                                return false;
-                            }
-                            if ((hm >> lane) & 1u) {
-                                const int idx = nc + __popc(hm & above_mask(lane));
-                                cend[idx] = v;
-                                cpos[idx] = (int32_t)((ch << 5) + lane);
-                            }
-                            nc += k;
-                            return true;
-                        });
-                    }
-                    if (lane == 0) {
-                        s_nc = nc;
-                        s_over = over ? 1 : 0;
-                    }
-                }
-                __syncthreads();
-                per_query = s_over != 0;
+                for (int w = 1; w < kWarpsPerCta; ++w) L = s_red[w] < L ? s_red[w] : L;
+                const int64_t umax = q_u[r1 - 1];
+                const int got = gather_bfs<S>(a.P, lo, umax, L, cap, cpos, cend, lst, cnt, msk, s_wsum, &s_nc,
+                                              &s_over);
+                s_nc_run = got;
+                per_query = got < 0;
             }
-            const int nc = per_query ? 0 : s_nc;
+            const int nc = per_query ? 0 : s_nc_run;
             for (int i = r0 + warp; i < r1; i += kWarpsPerCta) {
                 const S qs = q_s[i];
                 const int64_t u = q_u[i];
@@ -659,7 +743,8 @@ UbView<S> make_ub(const BatchedWorkspace& ws, int mode) {
 }
 
 size_t tile_smem(const BatchedParams& p, size_t s) {
-    return (size_t)p.cap * (s + 4) + (size_t)p.tile_q * (s + 12) + 64;
+    // cend + cpos, the tile's query records, then frontier list + counts + masks
+    return (size_t)p.cap * (s + 4) + (size_t)p.tile_q * (s + 12) + (size_t)p.cap * 12 + 64;
 }
 
 #define SI_CU(call)                                    \

@@ -935,3 +935,26 @@ extern "C" int upperBoundDeviceGpu(gSuperIntervals* si, const void* d_qe, const 
     if (r != SI_OK) return fail(r, "upper-bound kernel failed");
     return SI_OK;
 }
+
+extern "C" int setBatchedParamsGpu(gSuperIntervals* si, int tile_q, int cap, int64_t long_len) {
+    if (!si) return fail(SI_ERR_INVALID, "null handle");
+    sig::BatchedParams p = si->bws.prm;
+    if (tile_q) p.tile_q = tile_q;
+    if (cap) p.cap = cap;
+    if (long_len) p.long_len = long_len;
+    if (p.tile_q < 32 || p.tile_q > 1024 || (p.tile_q & 31))
+        return fail(SI_ERR_INVALID, "tile_queries must be a multiple of 32 in [32, 1024]");
+    if (p.cap < 256 || p.cap > 8192 || (p.cap & 255))
+        return fail(SI_ERR_INVALID, "tile_candidates must be a multiple of 256 in [256, 8192]");
+    if (p.long_len < 1) return fail(SI_ERR_INVALID, "long_query_len must be positive");
+    si->bws.prm = p;
+    return SI_OK;
+}
+
+extern "C" int getBatchedParamsGpu(const gSuperIntervals* si, int* tile_q, int* cap, int64_t* long_len) {
+    if (!si) return fail(SI_ERR_INVALID, "null handle");
+    if (tile_q) *tile_q = si->bws.prm.tile_q;
+    if (cap) *cap = si->bws.prm.cap;
+    if (long_len) *long_len = si->bws.prm.long_len;
+    return SI_OK;
+}

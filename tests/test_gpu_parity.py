@@ -218,6 +218,31 @@ def test_upper_bound_providers_exact(api, mode):
         idx.close()
 
 
+@pytest.mark.parametrize("tile_q,cap,long_len", [(32, 256, 1 << 40), (64, 256, 50), (1024, 8192, 1 << 14),
+                                                 (128, 512, 2000)])
+def test_batched_params_and_overflow_walks(api, oracle, tile_q, cap, long_len):
+    """Small candidate capacity forces the per-query warp walk, a tiny long-query
+    threshold sends most queries there, large tiles stress the shared gather: every
+    setting returns the same bit-exact result."""
+    from superintervals_gb300 import workloads as W
+    wl = W.config3(n=200_000, nq=40_000, long_queries=True)
+    idx = _index(api, wl.starts, wl.ends, wl.data, seg=wl.seg, path="batched")
+    api.check(idx.lib.setBatchedParamsGpu(idx.h, tile_q, cap, long_len))
+    m = oracle.build(wl.starts, wl.ends, wl.data, seg=wl.seg)
+    rc = oracle.count_batch(m, wl.q_starts, wl.q_ends, wl.q_contig, nthreads=8)
+    assert np.array_equal(idx.count(wl.q_starts, wl.q_ends, wl.q_contig), rc)
+    for order in (0, 1):
+        off, out = idx.search(wl.q_starts, wl.q_ends, wl.q_contig, order=order)
+        ro, rv = oracle.search_batch(m, wl.q_starts, wl.q_ends, wl.q_contig, order=order, nthreads=8,
+                                     counts=rc)
+        assert np.array_equal(off, ro) and np.array_equal(out, rv)
+    offv, outv = idx.search(wl.q_starts, wl.q_ends, wl.q_contig, order=1, values=True)
+    _, rv = oracle.search_batch(m, wl.q_starts, wl.q_ends, wl.q_contig, order=1, values=True,
+                                nthreads=8, counts=rc)
+    assert np.array_equal(outv, rv)
+    idx.close()
+
+
 @pytest.mark.parametrize("path", PATHS)
 def test_chunked_emit_matches_unchunked(api, oracle, path):
     from superintervals_gb300 import workloads as W
