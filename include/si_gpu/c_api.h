@@ -110,12 +110,15 @@ int getIndexArraysGpu(const gSuperIntervals* si, void* starts, void* ends, int32
 int setQueryPathGpu(gSuperIntervals* si, int path);
 int setUpperBoundModeGpu(gSuperIntervals* si, int mode);
 /* Tunables of the batched path: sorted queries per tile, candidate slots per
- * tile (shared memory), and the query length above which a query takes the
- * per-query walk.  0 keeps the current value. */
+ * tile (shared memory), the query length above which a query takes the
+ * per-query walk, and the interval length from which a tile's candidate goes
+ * to its "long" list (scanned for every query) instead of being scanned only
+ * near each query.  0 keeps the current value (split_len: -1 keeps it, 0 is a
+ * valid length).  Results do not depend on these values. */
 int setBatchedParamsGpu(gSuperIntervals* si, int tile_queries, int tile_candidates,
-                        int64_t long_query_len);
+                        int64_t long_query_len, int64_t split_len);
 int getBatchedParamsGpu(const gSuperIntervals* si, int* tile_queries, int* tile_candidates,
-                        int64_t* long_query_len);
+                        int64_t* long_query_len, int64_t* split_len);
 /* Device bytes one search call may use for its result buffer; larger results
  * are emitted in query chunks against it. */
 int setOutputBudgetGpu(gSuperIntervals* si, size_t bytes);

@@ -74,8 +74,8 @@ SIGNATURES = {
     "setQueryPathGpu": (_I, [_H, _I]),
     "setUpperBoundModeGpu": (_I, [_H, _I]),
     "setOutputBudgetGpu": (_I, [_H, _SZ]),
-    "setBatchedParamsGpu": (_I, [_H, _I, _I, C.c_int64]),
-    "getBatchedParamsGpu": (_I, [_H, _P, _P, _P]),
+    "setBatchedParamsGpu": (_I, [_H, _I, _I, C.c_int64, C.c_int64]),
+    "getBatchedParamsGpu": (_I, [_H, _P, _P, _P, _P]),
     "setProfilingGpu": (_I, [_H, _I]),
     "getPhaseTimesGpu": (_I, [_H, _P, _P]),
     "setDeviceBudgetGpu": (_I, [_SZ]),

@@ -130,6 +130,8 @@ __device__ __forceinline__ unsigned above_mask(int lane) {
 template <typename S>
 struct TileArgs {
     Pyr<S> P;
+    const S* starts;
+    int64_t split_len;
     const int32_t* data;
     const int64_t* seg;
     int32_t G;
@@ -326,8 +328,43 @@ __device__ int gather_bfs(const Pyr<S>& P, int64_t lo, int64_t umax, S L, int ca
     return nf;
 }
 
+// First index in [0, n) whose value is <= key in a DESCENDING array (n when none).
+// Warp-cooperative 32-ary search: one round of 32 samples narrows the range 32-fold.
+__device__ __forceinline__ int warp_search_desc_le(const int32_t* arr, int n, int64_t key, int lane) {
+    int lo = 0, hi = n;  // answer in [lo, hi]
+    while (hi - lo > 32) {
+        const int step = (hi - lo + 31) >> 5;
+        const int idx = lo + lane * step;
+        const unsigned m = __ballot_sync(kFull, idx < hi && (int64_t)arr[idx] > key);
+        const int k = __popc(m);  // samples above key form a prefix
+        if (k == 0) return lo;
+        const int nlo = lo + (k - 1) * step + 1;
+        const int nhi = min(hi, lo + k * step);
+        lo = nlo;
+        hi = nhi;
+    }
+    const int idx = lo + lane;
+    const unsigned m = __ballot_sync(kFull, idx < hi && (int64_t)arr[idx] > key);
+    return lo + __popc(m);
+}
+
+// start >= qs - X, without overflow
+template <typename S>
+__device__ __forceinline__ bool near_start(S start, S qs, int64_t X) {
+    return start >= qs || (uint64_t)qs - (uint64_t)start <= (uint64_t)X;
+}
+
+// end - start >= X, without overflow
+template <typename S>
+__device__ __forceinline__ bool is_long_iv(S start, S end, int64_t X) {
+    return end >= start && (uint64_t)end - (uint64_t)start >= (uint64_t)X;
+}
+
+constexpr int kLnu = 128;        // long candidates ending before the tile's max qs
+constexpr int kMaxBlocks = 8192 / 32 + 1;
+
 template <typename S, bool EMIT>
-__global__ void __launch_bounds__(kThreads) k_tiles(TileArgs<S> a) {
+__global__ void __launch_bounds__(kThreads, 4) k_tiles(TileArgs<S> a) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int cap = a.cap, T = a.tile_q;
     S* cend = reinterpret_cast<S*>(smem);
@@ -336,15 +373,21 @@ __global__ void __launch_bounds__(kThreads) k_tiles(TileArgs<S> a) {
     int32_t* q_u = reinterpret_cast<int32_t*>(q_s + T);
     uint32_t* q_c = reinterpret_cast<uint32_t*>(q_u + T);
     int32_t* q_id = reinterpret_cast<int32_t*>(q_c + T);
-    int32_t* lst = q_id + T;
-    int32_t* cnt = lst + cap;
-    uint32_t* msk = reinterpret_cast<uint32_t*>(cnt + cap);
-    __shared__ int s_tile, s_nc, s_over;
+    int32_t* lst = q_id + T;                                   // BFS frontier, then long positions
+    int32_t* cnt = lst + cap;                                  // BFS counts  } then long ends
+    uint32_t* msk = reinterpret_cast<uint32_t*>(cnt + cap);   // BFS masks   }
+    int32_t* lpos = lst;
+    S* lend = reinterpret_cast<S*>(cnt);
+    __shared__ int s_tile, s_n, s_sum, s_nlnu;
     __shared__ int s_wsum[kWarpsPerCta];
-    __shared__ S s_red[kWarpsPerCta];
-    int s_nc_run = 0;
+    __shared__ S s_red[kWarpsPerCta], s_red2[kWarpsPerCta];
+    __shared__ uint32_t s_bmask[kMaxBlocks];
+    __shared__ int32_t s_boff[kMaxBlocks];
+    __shared__ int32_t s_lnu_pos[kLnu];
+    __shared__ S s_lnu_end[kLnu];
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int64_t X = a.split_len;
     while (true) {
         if (tid == 0) s_tile = atomicAdd(a.tile_counter, 1);
         __syncthreads();
@@ -375,27 +418,76 @@ __global__ void __launch_bounds__(kThreads) k_tiles(TileArgs<S> a) {
             if (g >= a.G) g = 0;  // reported by the prepare kernel
             const int64_t lo = a.seg[g];
             bool per_query = is_long;
+            int nc = 0, nl = 0, nlnu = 0;
             if (!is_long) {
-                // L = min qs over the run, umax = ub of the last query of the run
-                S mn = Lim<S>::hi;
-                for (int i = r0 + tid; i < r1; i += kThreads) mn = q_s[i] < mn ? q_s[i] : mn;
+                // L = min qs, Q = max qs over the run; umax = ub of the run's last query
+                S mn = Lim<S>::hi, mx = Lim<S>::lo;
+                for (int i = r0 + tid; i < r1; i += kThreads) {
+                    mn = q_s[i] < mn ? q_s[i] : mn;
+                    mx = q_s[i] > mx ? q_s[i] : mx;
+                }
 #pragma unroll
                 for (int d = 16; d > 0; d >>= 1) {
                     const S o = __shfl_xor_sync(kFull, mn, d);
                     mn = o < mn ? o : mn;
+                    const S p = __shfl_xor_sync(kFull, mx, d);
+                    mx = p > mx ? p : mx;
                 }
-                if (lane == 0) s_red[warp] = mn;
+                if (lane == 0) {
+                    s_red[warp] = mn;
+                    s_red2[warp] = mx;
+                }
+                if (tid == 0) s_nlnu = 0;
                 __syncthreads();
-                S L = s_red[0];
+                S L = s_red[0], Q = s_red2[0];
 #pragma unroll
-                for (int w = 1; w < kWarpsPerCta; ++w) L = s_red[w] < L ? s_red[w] : L;
+                for (int w = 1; w < kWarpsPerCta; ++w) {
+                    L = s_red[w] < L ? s_red[w] : L;
+                    Q = s_red2[w] > Q ? s_red2[w] : Q;
+                }
                 const int64_t umax = q_u[r1 - 1];
-                const int got = gather_bfs<S>(a.P, lo, umax, L, cap, cpos, cend, lst, cnt, msk, s_wsum, &s_nc,
-                                              &s_over);
-                s_nc_run = got;
-                per_query = got < 0;
+                nc = gather_bfs<S>(a.P, lo, umax, L, cap, cpos, cend, lst, cnt, msk, s_wsum, &s_n, &s_sum);
+                per_query = nc < 0;
+                if (!per_query && nc > 0) {
+                    // long candidates (end - start >= X) into (lpos, lend), in order; the ones
+                    // ending before Q (possible misses for some query) also into the lnu list
+                    const int nb = (nc + 31) >> 5;
+                    for (int b = warp; b < nb; b += kWarpsPerCta) {
+                        const int tt = (b << 5) + lane;
+                        bool isl = false;
+                        if (tt < nc) {
+                            isl = is_long_iv<S>(a.starts[cpos[tt]], cend[tt], X);
+                            if (isl && cend[tt] < Q) {
+                                const int slot = atomicAdd(&s_nlnu, 1);
+                                if (slot < kLnu) {
+                                    s_lnu_pos[slot] = cpos[tt];
+                                    s_lnu_end[slot] = cend[tt];
+                                }
+                            }
+                        }
+                        const unsigned m = __ballot_sync(kFull, isl);
+                        if (lane == 0) {
+                            s_bmask[b] = m;
+                            s_boff[b] = __popc(m);
+                        }
+                    }
+                    __syncthreads();
+                    block_excl_scan(s_boff, nb, s_wsum, &s_sum);
+                    nl = s_sum;
+                    for (int b = warp; b < nb; b += kWarpsPerCta) {
+                        const unsigned m = s_bmask[b];
+                        if ((m >> lane) & 1u) {
+                            const int tt = (b << 5) + lane;
+                            const int idx = s_boff[b] + __popc(m & lanemask_lt());
+                            lpos[idx] = cpos[tt];
+                            lend[idx] = cend[tt];
+                        }
+                    }
+                    __syncthreads();
+                    nlnu = s_nlnu;
+                }
+                if (per_query) nc = 0;
             }
-            const int nc = per_query ? 0 : s_nc_run;
             for (int i = r0 + warp; i < r1; i += kWarpsPerCta) {
                 const S qs = q_s[i];
                 const int64_t u = q_u[i];
@@ -404,14 +496,7 @@ __global__ void __launch_bounds__(kThreads) k_tiles(TileArgs<S> a) {
                     walk_query<S, EMIT>(a, qs, u, lo, id, lane);
                     continue;
                 }
-                // first candidate at or below u: C is sorted by position, descending
-                int b0 = 0, b1 = nc;
-                while (b0 < b1) {
-                    const int mid = (b0 + b1) >> 1;
-                    if (cpos[mid] > u) b0 = mid + 1;
-                    else b1 = mid;
-                }
-                const int t0 = b0;
+                const int t0 = warp_search_desc_le(cpos, nc, u, lane);  // first candidate <= u
                 if (!EMIT) {
                     int head = 0;
                     bool open = u >= lo;
@@ -426,13 +511,39 @@ __global__ void __launch_bounds__(kThreads) k_tiles(TileArgs<S> a) {
                             open = false;
                         }
                     }
-                    uint32_t cnt = 0;
+                    // part A: candidates whose start is within X of qs (all classes)
+                    uint32_t c = 0;
+                    int tsplit = nc;
                     for (int kk = t0; kk < nc; kk += 32) {
                         const int tt = kk + lane;
-                        cnt += __popc(__ballot_sync(kFull, tt < nc && cend[tt] >= qs));
+                        const bool in = tt < nc && near_start<S>(a.starts[cpos[tt]], qs, X);
+                        const unsigned mi = __ballot_sync(kFull, in);
+                        c += __popc(__ballot_sync(kFull, in && cend[tt] >= qs));
+                        if (mi != kFull) {
+                            tsplit = kk + __popc(mi);
+                            break;
+                        }
+                    }
+                    // part B: long candidates below the split are hits unless they end before qs
+                    if (tsplit < nc && nl > 0) {
+                        const int64_t psplit = cpos[tsplit];
+                        const int lb = warp_search_desc_le(lpos, nl, psplit, lane);
+                        if (nlnu <= kLnu) {
+                            int miss = 0;
+                            for (int k = lane; k < nlnu; k += 32)
+                                miss += (s_lnu_pos[k] <= psplit && s_lnu_end[k] < qs) ? 1 : 0;
+#pragma unroll
+                            for (int d = 16; d > 0; d >>= 1) miss += __shfl_xor_sync(kFull, miss, d);
+                            c += (uint32_t)(nl - lb - miss);
+                        } else {
+                            for (int kk = lb; kk < nl; kk += 32) {
+                                const int tt = kk + lane;
+                                c += __popc(__ballot_sync(kFull, tt < nl && lend[tt] >= qs));
+                            }
+                        }
                     }
                     if (lane == 0) {
-                        a.counts[id] = cnt;
+                        a.counts[id] = c;
                         a.heads[id] = head;
                     }
                 } else {
@@ -450,9 +561,14 @@ __global__ void __launch_bounds__(kThreads) k_tiles(TileArgs<S> a) {
                     }
                     int64_t w = h;
                     bool bad = false;
-                    for (int kk = t0 + (int)h; kk < nc; kk += 32) {
+                    // part A after the head
+                    const int ta = t0 + (int)(h < (int64_t)(nc - t0) ? h : (int64_t)(nc - t0));
+                    int tsplit = nc;
+                    for (int kk = ta; kk < nc; kk += 32) {
                         const int tt = kk + lane;
-                        const bool hit = tt < nc && cend[tt] >= qs;
+                        const bool in = tt < nc && near_start<S>(a.starts[cpos[tt]], qs, X);
+                        const unsigned mi = __ballot_sync(kFull, in);
+                        const bool hit = in && cend[tt] >= qs;
                         const unsigned m = __ballot_sync(kFull, hit);
                         const int k = __popc(m);
                         if (w + k > capq) {
@@ -464,6 +580,30 @@ __global__ void __launch_bounds__(kThreads) k_tiles(TileArgs<S> a) {
                             dst[w + __popc(m & lanemask_lt())] = a.values ? a.data[pos] : (int32_t)(pos - lo);
                         }
                         w += k;
+                        if (mi != kFull) {
+                            tsplit = kk + __popc(mi);
+                            break;
+                        }
+                    }
+                    // part B: long candidates at or below C index max(tsplit, ta)
+                    const int tb = max(tsplit, ta);
+                    if (!bad && tb < nc && nl > 0) {
+                        const int lb = warp_search_desc_le(lpos, nl, (int64_t)cpos[tb], lane);
+                        for (int kk = lb; kk < nl; kk += 32) {
+                            const int tt = kk + lane;
+                            const bool hit = tt < nl && lend[tt] >= qs;
+                            const unsigned m = __ballot_sync(kFull, hit);
+                            const int k = __popc(m);
+                            if (w + k > capq) {
+                                bad = true;
+                                break;
+                            }
+                            if (hit) {
+                                const int64_t pos = lpos[tt];
+                                dst[w + __popc(m & lanemask_lt())] = a.values ? a.data[pos] : (int32_t)(pos - lo);
+                            }
+                            w += k;
+                        }
                     }
                     if (bad && lane == 0) atomicCAS(a.d_err, kDevOk, kDevOverflow);
                 }
@@ -929,6 +1069,8 @@ static int run_tiles(BatchedWorkspace& ws, MapView<S> m, Levels<S> L, int H, int
     SI_CU(cudaMemsetAsync(ws.counters.p, 0, sizeof(int) * 4, st));
     TileArgs<S> a;
     a.P = make_pyr<S>(m, L, H);
+    a.starts = m.starts;
+    a.split_len = ws.prm.split_len;
     a.data = m.data;
     a.seg = m.seg;
     a.G = m.G;

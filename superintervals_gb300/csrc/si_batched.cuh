@@ -27,6 +27,7 @@ struct BatchedParams {
     int tile_q = 256;            // sorted queries per tile
     int cap = 2048;              // candidate slots per tile (shared memory)
     int64_t long_len = 16384;    // queries longer than this take the per-query walk
+    int64_t split_len = 2048;    // candidates at least this long form the tile's long list
     int eytz_depth = 0;          // 0: automatic
 };
 

@@ -936,12 +936,13 @@ extern "C" int upperBoundDeviceGpu(gSuperIntervals* si, const void* d_qe, const 
     return SI_OK;
 }
 
-extern "C" int setBatchedParamsGpu(gSuperIntervals* si, int tile_q, int cap, int64_t long_len) {
+extern "C" int setBatchedParamsGpu(gSuperIntervals* si, int tile_q, int cap, int64_t long_len, int64_t split_len) {
     if (!si) return fail(SI_ERR_INVALID, "null handle");
     sig::BatchedParams p = si->bws.prm;
     if (tile_q) p.tile_q = tile_q;
     if (cap) p.cap = cap;
     if (long_len) p.long_len = long_len;
+    if (split_len >= 0) p.split_len = split_len;
     if (p.tile_q < 32 || p.tile_q > 1024 || (p.tile_q & 31))
         return fail(SI_ERR_INVALID, "tile_queries must be a multiple of 32 in [32, 1024]");
     if (p.cap < 256 || p.cap > 8192 || (p.cap & 255))
@@ -951,10 +952,12 @@ extern "C" int setBatchedParamsGpu(gSuperIntervals* si, int tile_q, int cap, int
     return SI_OK;
 }
 
-extern "C" int getBatchedParamsGpu(const gSuperIntervals* si, int* tile_q, int* cap, int64_t* long_len) {
+extern "C" int getBatchedParamsGpu(const gSuperIntervals* si, int* tile_q, int* cap, int64_t* long_len,
+                                   int64_t* split_len) {
     if (!si) return fail(SI_ERR_INVALID, "null handle");
     if (tile_q) *tile_q = si->bws.prm.tile_q;
     if (cap) *cap = si->bws.prm.cap;
     if (long_len) *long_len = si->bws.prm.long_len;
+    if (split_len) *split_len = si->bws.prm.split_len;
     return SI_OK;
 }

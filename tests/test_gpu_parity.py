@@ -218,16 +218,17 @@ def test_upper_bound_providers_exact(api, mode):
         idx.close()
 
 
-@pytest.mark.parametrize("tile_q,cap,long_len", [(32, 256, 1 << 40), (64, 256, 50), (1024, 8192, 1 << 14),
-                                                 (128, 512, 2000)])
-def test_batched_params_and_overflow_walks(api, oracle, tile_q, cap, long_len):
+@pytest.mark.parametrize("tile_q,cap,long_len,split", [(32, 256, 1 << 40, 2048), (64, 256, 50, 0),
+                                                       (1024, 8192, 1 << 14, 1), (128, 512, 2000, 1 << 40),
+                                                       (256, 2048, 1 << 14, 300)])
+def test_batched_params_and_overflow_walks(api, oracle, tile_q, cap, long_len, split):
     """Small candidate capacity forces the per-query warp walk, a tiny long-query
     threshold sends most queries there, large tiles stress the shared gather: every
     setting returns the same bit-exact result."""
     from superintervals_gb300 import workloads as W
     wl = W.config3(n=200_000, nq=40_000, long_queries=True)
     idx = _index(api, wl.starts, wl.ends, wl.data, seg=wl.seg, path="batched")
-    api.check(idx.lib.setBatchedParamsGpu(idx.h, tile_q, cap, long_len))
+    api.check(idx.lib.setBatchedParamsGpu(idx.h, tile_q, cap, long_len, split))
     m = oracle.build(wl.starts, wl.ends, wl.data, seg=wl.seg)
     rc = oracle.count_batch(m, wl.q_starts, wl.q_ends, wl.q_contig, nthreads=8)
     assert np.array_equal(idx.count(wl.q_starts, wl.q_ends, wl.q_contig), rc)
