@@ -378,7 +378,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_tiles(TileArgs<S> a) {
     uint32_t* msk = reinterpret_cast<uint32_t*>(cnt + cap);   // BFS masks   }
     int32_t* lpos = lst;
     S* lend = reinterpret_cast<S*>(cnt);
-    __shared__ int s_tile, s_n, s_sum, s_nlnu;
+    __shared__ int s_tile, s_n, s_sum, s_nlnu, s_next;
     __shared__ int s_wsum[kWarpsPerCta];
     __shared__ S s_red[kWarpsPerCta], s_red2[kWarpsPerCta];
     __shared__ uint32_t s_bmask[kMaxBlocks];
@@ -391,8 +391,11 @@ __global__ void __launch_bounds__(kThreads, 4) k_tiles(TileArgs<S> a) {
     while (true) {
         if (tid == 0) s_tile = atomicAdd(a.tile_counter, 1);
         __syncthreads();
-        const int t = s_tile;
-        if (t >= a.n_tiles) return;
+        const int tc = s_tile;
+        if (tc >= a.n_tiles) return;
+        // heaviest first: long queries sort to the end of the batch, so tiles are handed
+        // out from the end and the per-query walks overlap the shared-candidate tiles
+        const int t = a.n_tiles - 1 - tc;
         const int64_t j0 = (int64_t)t * T;
         const int nt = (int)((a.nq - j0) < (int64_t)T ? (a.nq - j0) : (int64_t)T);
         for (int i = tid; i < nt; i += kThreads) {
@@ -488,14 +491,22 @@ __global__ void __launch_bounds__(kThreads, 4) k_tiles(TileArgs<S> a) {
                 }
                 if (per_query) nc = 0;
             }
-            for (int i = r0 + warp; i < r1; i += kWarpsPerCta) {
+            if (per_query) {
+                // per-query walks differ widely in length: warps claim queries one at a time
+                if (tid == 0) s_next = r0;
+                __syncthreads();
+                while (true) {
+                    int i = 0;
+                    if (lane == 0) i = atomicAdd(&s_next, 1);
+                    i = __shfl_sync(kFull, i, 0);
+                    if (i >= r1) break;
+                    walk_query<S, EMIT>(a, q_s[i], (int64_t)q_u[i], lo, q_id[i], lane);
+                }
+            }
+            for (int i = r0 + warp; !per_query && i < r1; i += kWarpsPerCta) {
                 const S qs = q_s[i];
                 const int64_t u = q_u[i];
                 const int32_t id = q_id[i];
-                if (per_query) {
-                    walk_query<S, EMIT>(a, qs, u, lo, id, lane);
-                    continue;
-                }
                 const int t0 = warp_search_desc_le(cpos, nc, u, lane);  // first candidate <= u
                 if (!EMIT) {
                     int head = 0;
