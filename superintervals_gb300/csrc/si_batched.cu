@@ -373,11 +373,15 @@ __global__ void __launch_bounds__(kThreads, 4) k_tiles(TileArgs<S> a) {
     int32_t* q_u = reinterpret_cast<int32_t*>(q_s + T);
     uint32_t* q_c = reinterpret_cast<uint32_t*>(q_u + T);
     int32_t* q_id = reinterpret_cast<int32_t*>(q_c + T);
-    int32_t* lst = q_id + T;                                   // BFS frontier, then long positions
+    int64_t* q_off = reinterpret_cast<int64_t*>(q_id + T);    // emit: output offset of the query
+    int32_t* q_cap = reinterpret_cast<int32_t*>(q_off + T);   // emit: its result count
+    int32_t* q_h = q_cap + T;                                  // emit: its head-run length
+    int32_t* lst = q_h + T;                                    // BFS frontier, then long positions
     int32_t* cnt = lst + cap;                                  // BFS counts  } then long ends
-    uint32_t* msk = reinterpret_cast<uint32_t*>(cnt + cap);   // BFS masks   }
+    uint32_t* msk = reinterpret_cast<uint32_t*>(cnt + cap);   // BFS masks   } (+ starts, 32-bit S)
     int32_t* lpos = lst;
     S* lend = reinterpret_cast<S*>(cnt);
+    S* cstart = (sizeof(S) == 4) ? reinterpret_cast<S*>(msk) : reinterpret_cast<S*>(msk + cap);
     __shared__ int s_tile, s_n, s_sum, s_nlnu, s_next;
     __shared__ int s_wsum[kWarpsPerCta];
     __shared__ S s_red[kWarpsPerCta], s_red2[kWarpsPerCta];
@@ -403,6 +407,14 @@ __global__ void __launch_bounds__(kThreads, 4) k_tiles(TileArgs<S> a) {
             q_u[i] = a.sq_u[j0 + i];
             q_c[i] = a.sq_c[j0 + i];
             q_id[i] = a.sq_id[j0 + i];
+            if (EMIT) {
+                // the tile's random per-query reads, issued together instead of per query
+                const int32_t id = q_id[i];
+                const int64_t o = a.offsets[id];
+                q_off[i] = o - a.out_base;
+                q_cap[i] = (int32_t)(a.offsets[id + 1] - o);
+                q_h[i] = a.heads_in[id];
+            }
         }
         __syncthreads();
         int r0 = 0;
@@ -459,7 +471,9 @@ __global__ void __launch_bounds__(kThreads, 4) k_tiles(TileArgs<S> a) {
                         const int tt = (b << 5) + lane;
                         bool isl = false;
                         if (tt < nc) {
-                            isl = is_long_iv<S>(a.starts[cpos[tt]], cend[tt], X);
+                            const S st = a.starts[cpos[tt]];
+                            cstart[tt] = st;
+                            isl = is_long_iv<S>(st, cend[tt], X);
                             if (isl && cend[tt] < Q) {
                                 const int slot = atomicAdd(&s_nlnu, 1);
                                 if (slot < kLnu) {
@@ -527,7 +541,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_tiles(TileArgs<S> a) {
                     int tsplit = nc;
                     for (int kk = t0; kk < nc; kk += 32) {
                         const int tt = kk + lane;
-                        const bool in = tt < nc && near_start<S>(a.starts[cpos[tt]], qs, X);
+                        const bool in = tt < nc && near_start<S>(cstart[tt], qs, X);
                         const unsigned mi = __ballot_sync(kFull, in);
                         c += __popc(__ballot_sync(kFull, in && cend[tt] >= qs));
                         if (mi != kFull) {
@@ -558,10 +572,9 @@ __global__ void __launch_bounds__(kThreads, 4) k_tiles(TileArgs<S> a) {
                         a.heads[id] = head;
                     }
                 } else {
-                    const int64_t h = a.heads_in[id];
-                    const int64_t base = a.offsets[id] - a.out_base;
-                    const int64_t capq = a.offsets[id + 1] - a.offsets[id];
-                    int32_t* dst = a.out + base;
+                    const int64_t h = q_h[i];
+                    const int64_t capq = q_cap[i];
+                    int32_t* dst = a.out + q_off[i];
                     if (h > capq) {
                         if (lane == 0) atomicCAS(a.d_err, kDevOk, kDevOverflow);
                         continue;
@@ -577,7 +590,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_tiles(TileArgs<S> a) {
                     int tsplit = nc;
                     for (int kk = ta; kk < nc; kk += 32) {
                         const int tt = kk + lane;
-                        const bool in = tt < nc && near_start<S>(a.starts[cpos[tt]], qs, X);
+                        const bool in = tt < nc && near_start<S>(cstart[tt], qs, X);
                         const unsigned mi = __ballot_sync(kFull, in);
                         const bool hit = in && cend[tt] >= qs;
                         const unsigned m = __ballot_sync(kFull, hit);
@@ -895,7 +908,9 @@ UbView<S> make_ub(const BatchedWorkspace& ws, int mode) {
 
 size_t tile_smem(const BatchedParams& p, size_t s) {
     // cend + cpos, the tile's query records, then frontier list + counts + masks
-    return (size_t)p.cap * (s + 4) + (size_t)p.tile_q * (s + 12) + (size_t)p.cap * 12 + 64;
+    // candidates (end, position), per-query records, BFS scratch / long list (+ 64-bit starts)
+    return (size_t)p.cap * (s + 4) + (size_t)p.tile_q * (s + 12 + 16) + (size_t)p.cap * 12 +
+           (s == 8 ? (size_t)p.cap * 8 : 0) + 64;
 }
 
 #define SI_CU(call)                                    \
