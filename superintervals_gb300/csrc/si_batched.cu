@@ -517,102 +517,131 @@ __global__ void __launch_bounds__(kThreads, 4) k_tiles(TileArgs<S> a) {
                     walk_query<S, EMIT>(a, q_s[i], (int64_t)q_u[i], lo, q_id[i], lane);
                 }
             }
-            for (int i = r0 + warp; !per_query && i < r1; i += kWarpsPerCta) {
-                const S qs = q_s[i];
-                const int64_t u = q_u[i];
-                const int32_t id = q_id[i];
-                const int t0 = warp_search_desc_le(cpos, nc, u, lane);  // first candidate <= u
-                if (!EMIT) {
-                    int head = 0;
-                    bool open = u >= lo;
-                    for (int kk = t0; open && kk < nc; kk += 32) {
-                        const int tt = kk + lane;
-                        const bool c = tt < nc && cpos[tt] == (int32_t)(u - (tt - t0)) && cend[tt] >= qs;
-                        const unsigned m = __ballot_sync(kFull, c);
-                        if (m == kFull) {
-                            head += 32;
-                        } else {
-                            head += __ffs(~m) - 1;
-                            open = false;
-                        }
-                    }
-                    // part A: candidates whose start is within X of qs (all classes)
+            if (!EMIT && !per_query) {
+                // count pass: one query per THREAD over the shared-memory lists
+                for (int i = r0 + tid; i < r1; i += kThreads) {
+                    const S qs = q_s[i];
+                    const int32_t u = q_u[i];
                     uint32_t c = 0;
-                    int tsplit = nc;
-                    for (int kk = t0; kk < nc; kk += 32) {
-                        const int tt = kk + lane;
-                        const bool in = tt < nc && near_start<S>(cstart[tt], qs, X);
-                        const unsigned mi = __ballot_sync(kFull, in);
-                        c += __popc(__ballot_sync(kFull, in && cend[tt] >= qs));
-                        if (mi != kFull) {
-                            tsplit = kk + __popc(mi);
-                            break;
+                    int head = 0;
+                    if (u >= lo && nc > 0) {
+                        int b0 = 0, b1 = nc;  // first candidate at or below u
+                        while (b0 < b1) {
+                            const int mid = (b0 + b1) >> 1;
+                            if (cpos[mid] > u) b0 = mid + 1;
+                            else b1 = mid;
                         }
-                    }
-                    // part B: long candidates below the split are hits unless they end before qs
-                    if (tsplit < nc && nl > 0) {
-                        const int64_t psplit = cpos[tsplit];
-                        const int lb = warp_search_desc_le(lpos, nl, psplit, lane);
-                        if (nlnu <= kLnu) {
-                            int miss = 0;
-                            for (int k = lane; k < nlnu; k += 32)
-                                miss += (s_lnu_pos[k] <= psplit && s_lnu_end[k] < qs) ? 1 : 0;
-#pragma unroll
-                            for (int d = 16; d > 0; d >>= 1) miss += __shfl_xor_sync(kFull, miss, d);
-                            c += (uint32_t)(nl - lb - miss);
-                        } else {
-                            for (int kk = lb; kk < nl; kk += 32) {
-                                const int tt = kk + lane;
-                                c += __popc(__ballot_sync(kFull, tt < nl && lend[tt] >= qs));
+                        const int t0 = b0;
+                        // part A and the head run: candidates whose start is within X of qs
+                        int t = t0;
+                        bool open = true;
+                        while (t < nc && near_start<S>(cstart[t], qs, X)) {
+                            const bool hit = cend[t] >= qs;
+                            c += hit ? 1u : 0u;
+                            if (open) {
+                                if (hit && cpos[t] == u - (t - t0)) ++head;
+                                else open = false;
+                            }
+                            ++t;
+                        }
+                        const int tsplit = t;
+                        for (; open && t < nc; ++t) {  // a head run reaching into the long candidates
+                            if (cpos[t] == u - (t - t0) && cend[t] >= qs) ++head;
+                            else open = false;
+                        }
+                        // part B: long candidates below the split are hits unless they end before qs
+                        if (tsplit < nc && nl > 0) {
+                            const int32_t psplit = cpos[tsplit];
+                            int l0 = 0, l1 = nl;
+                            while (l0 < l1) {
+                                const int mid = (l0 + l1) >> 1;
+                                if (lpos[mid] > psplit) l0 = mid + 1;
+                                else l1 = mid;
+                            }
+                            if (nlnu <= kLnu) {
+                                int miss = 0;
+                                for (int k = 0; k < nlnu; ++k)
+                                    miss += (s_lnu_pos[k] <= psplit && s_lnu_end[k] < qs) ? 1 : 0;
+                                c += (uint32_t)(nl - l0 - miss);
+                            } else {
+                                for (int k = l0; k < nl; ++k) c += lend[k] >= qs ? 1u : 0u;
                             }
                         }
                     }
-                    if (lane == 0) {
-                        a.counts[id] = c;
-                        a.heads[id] = head;
+                    a.counts[q_id[i]] = c;
+                    a.heads[q_id[i]] = head;
+                }
+            }
+            for (int i = r0 + warp; EMIT && !per_query && i < r1; i += kWarpsPerCta) {
+                // emit pass: one query per WARP, coalesced writes
+                const S qs = q_s[i];
+                const int64_t u = q_u[i];
+                const int t0 = warp_search_desc_le(cpos, nc, u, lane);  // first candidate <= u
+                const int64_t h = q_h[i];
+                const int64_t capq = q_cap[i];
+                int32_t* dst = a.out + q_off[i];
+                if (h > capq) {
+                    if (lane == 0) atomicCAS(a.d_err, kDevOk, kDevOverflow);
+                    continue;
+                }
+                for (int64_t r = lane; r < h; r += 32) {
+                    const int64_t pos = (a.order == kOrderIdxsCpp) ? (u - h + 1 + r) : (u - r);
+                    dst[r] = a.values ? a.data[pos] : (int32_t)(pos - lo);
+                }
+                int64_t w = h;
+                bool bad = false;
+                // part A after the head
+                const int ta = t0 + (int)(h < (int64_t)(nc - t0) ? h : (int64_t)(nc - t0));
+                int tsplit = nc;
+                for (int kk = ta; kk < nc; kk += 32) {
+                    const int tt = kk + lane;
+                    const bool in = tt < nc && near_start<S>(cstart[tt], qs, X);
+                    const unsigned mi = __ballot_sync(kFull, in);
+                    const bool hit = in && cend[tt] >= qs;
+                    const unsigned m = __ballot_sync(kFull, hit);
+                    const int k = __popc(m);
+                    if (w + k > capq) {
+                        bad = true;
+                        break;
                     }
-                } else {
-                    const int64_t h = q_h[i];
-                    const int64_t capq = q_cap[i];
-                    int32_t* dst = a.out + q_off[i];
-                    if (h > capq) {
-                        if (lane == 0) atomicCAS(a.d_err, kDevOk, kDevOverflow);
-                        continue;
+                    if (hit) {
+                        const int64_t pos = cpos[tt];
+                        dst[w + __popc(m & lanemask_lt())] = a.values ? a.data[pos] : (int32_t)(pos - lo);
                     }
-                    for (int64_t r = lane; r < h; r += 32) {
-                        const int64_t pos = (a.order == kOrderIdxsCpp) ? (u - h + 1 + r) : (u - r);
-                        dst[r] = a.values ? a.data[pos] : (int32_t)(pos - lo);
+                    w += k;
+                    if (mi != kFull) {
+                        tsplit = kk + __popc(mi);
+                        break;
                     }
-                    int64_t w = h;
-                    bool bad = false;
-                    // part A after the head
-                    const int ta = t0 + (int)(h < (int64_t)(nc - t0) ? h : (int64_t)(nc - t0));
-                    int tsplit = nc;
-                    for (int kk = ta; kk < nc; kk += 32) {
-                        const int tt = kk + lane;
-                        const bool in = tt < nc && near_start<S>(cstart[tt], qs, X);
-                        const unsigned mi = __ballot_sync(kFull, in);
-                        const bool hit = in && cend[tt] >= qs;
-                        const unsigned m = __ballot_sync(kFull, hit);
-                        const int k = __popc(m);
-                        if (w + k > capq) {
+                }
+                // part B: long candidates at or below C index max(tsplit, ta)
+                const int tb = max(tsplit, ta);
+                if (!bad && tb < nc && nl > 0) {
+                    const int32_t pb = cpos[tb];
+                    const int lb = warp_search_desc_le(lpos, nl, (int64_t)pb, lane);
+                    // only long candidates ending before the tile's max qs can miss
+                    int miss = 0;
+                    if (nlnu <= kLnu) {
+                        for (int k = lane; k < nlnu; k += 32)
+                            miss += (s_lnu_pos[k] <= pb && s_lnu_end[k] < qs) ? 1 : 0;
+#pragma unroll
+                        for (int d = 16; d > 0; d >>= 1) miss += __shfl_xor_sync(kFull, miss, d);
+                    } else {
+                        miss = 1;
+                    }
+                    if (miss == 0) {
+                        // every long candidate from lb on is a hit: straight copy
+                        const int len = nl - lb;
+                        if (w + len > capq) {
                             bad = true;
-                            break;
+                        } else {
+                            for (int k = lane; k < len; k += 32) {
+                                const int32_t pos = lpos[lb + k];
+                                dst[w + k] = a.values ? a.data[pos] : (int32_t)(pos - lo);
+                            }
+                            w += len;
                         }
-                        if (hit) {
-                            const int64_t pos = cpos[tt];
-                            dst[w + __popc(m & lanemask_lt())] = a.values ? a.data[pos] : (int32_t)(pos - lo);
-                        }
-                        w += k;
-                        if (mi != kFull) {
-                            tsplit = kk + __popc(mi);
-                            break;
-                        }
-                    }
-                    // part B: long candidates at or below C index max(tsplit, ta)
-                    const int tb = max(tsplit, ta);
-                    if (!bad && tb < nc && nl > 0) {
-                        const int lb = warp_search_desc_le(lpos, nl, (int64_t)cpos[tb], lane);
+                    } else {
                         for (int kk = lb; kk < nl; kk += 32) {
                             const int tt = kk + lane;
                             const bool hit = tt < nl && lend[tt] >= qs;
@@ -629,8 +658,8 @@ __global__ void __launch_bounds__(kThreads, 4) k_tiles(TileArgs<S> a) {
                             w += k;
                         }
                     }
-                    if (bad && lane == 0) atomicCAS(a.d_err, kDevOk, kDevOverflow);
                 }
+                if (bad && lane == 0) atomicCAS(a.d_err, kDevOk, kDevOverflow);
             }
             __syncthreads();
             r0 = r1;
