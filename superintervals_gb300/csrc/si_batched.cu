@@ -376,7 +376,10 @@ __global__ void __launch_bounds__(kThreads, 4) k_tiles(TileArgs<S> a) {
     int64_t* q_off = reinterpret_cast<int64_t*>(q_id + T);    // emit: output offset of the query
     int32_t* q_cap = reinterpret_cast<int32_t*>(q_off + T);   // emit: its result count
     int32_t* q_h = q_cap + T;                                  // emit: its head-run length
-    int32_t* lst = q_h + T;                                    // BFS frontier, then long positions
+    int32_t* q_ta = q_h + T;                                   // emit: first candidate after the head
+    int32_t* q_tsplit = q_ta + T;                              // emit: end of the near-qs candidates
+    int32_t* q_lb = q_tsplit + T;                              // emit: first long candidate (-1-x: misses)
+    int32_t* lst = q_lb + T;                                    // BFS frontier, then long positions
     int32_t* cnt = lst + cap;                                  // BFS counts  } then long ends
     uint32_t* msk = reinterpret_cast<uint32_t*>(cnt + cap);   // BFS masks   } (+ starts, 32-bit S)
     int32_t* lpos = lst;
@@ -572,11 +575,53 @@ __global__ void __launch_bounds__(kThreads, 4) k_tiles(TileArgs<S> a) {
                     a.heads[q_id[i]] = head;
                 }
             }
+            if (EMIT && !per_query) {
+                // emit, step 1: one query per THREAD finds where its hits lie in the lists
+                for (int i = r0 + tid; i < r1; i += kThreads) {
+                    const S qs = q_s[i];
+                    const int32_t u = q_u[i];
+                    int ta = nc, tsplit = nc, lb = nl, flags = 0;
+                    if (u >= lo && nc > 0) {
+                        int b0 = 0, b1 = nc;  // first candidate at or below u
+                        while (b0 < b1) {
+                            const int mid = (b0 + b1) >> 1;
+                            if (cpos[mid] > u) b0 = mid + 1;
+                            else b1 = mid;
+                        }
+                        const int t0 = b0;
+                        const int h = q_h[i];
+                        ta = t0 + (h < nc - t0 ? h : nc - t0);
+                        int t = ta;
+                        while (t < nc && near_start<S>(cstart[t], qs, X)) ++t;
+                        tsplit = t;
+                        const int tb = max(tsplit, ta);
+                        if (tb < nc && nl > 0) {
+                            const int32_t pb = cpos[tb];
+                            int l0 = 0, l1 = nl;
+                            while (l0 < l1) {
+                                const int mid = (l0 + l1) >> 1;
+                                if (lpos[mid] > pb) l0 = mid + 1;
+                                else l1 = mid;
+                            }
+                            lb = l0;
+                            if (nlnu > kLnu) {
+                                flags = 1;
+                            } else {
+                                for (int k = 0; k < nlnu; ++k)
+                                    if (s_lnu_pos[k] <= pb && s_lnu_end[k] < qs) flags = 1;
+                            }
+                        }
+                    }
+                    q_ta[i] = ta;
+                    q_tsplit[i] = tsplit;
+                    q_lb[i] = flags ? -1 - lb : lb;  // negative: some long candidate misses
+                }
+                __syncthreads();
+            }
             for (int i = r0 + warp; EMIT && !per_query && i < r1; i += kWarpsPerCta) {
-                // emit pass: one query per WARP, coalesced writes
+                // emit, step 2: one query per WARP writes its hits, coalesced
                 const S qs = q_s[i];
                 const int64_t u = q_u[i];
-                const int t0 = warp_search_desc_le(cpos, nc, u, lane);  // first candidate <= u
                 const int64_t h = q_h[i];
                 const int64_t capq = q_cap[i];
                 int32_t* dst = a.out + q_off[i];
@@ -590,14 +635,11 @@ __global__ void __launch_bounds__(kThreads, 4) k_tiles(TileArgs<S> a) {
                 }
                 int64_t w = h;
                 bool bad = false;
-                // part A after the head
-                const int ta = t0 + (int)(h < (int64_t)(nc - t0) ? h : (int64_t)(nc - t0));
-                int tsplit = nc;
-                for (int kk = ta; kk < nc; kk += 32) {
+                const int ta = q_ta[i], tsplit = q_tsplit[i];
+                // part A: candidates near qs after the head
+                for (int kk = ta; kk < tsplit; kk += 32) {
                     const int tt = kk + lane;
-                    const bool in = tt < nc && near_start<S>(cstart[tt], qs, X);
-                    const unsigned mi = __ballot_sync(kFull, in);
-                    const bool hit = in && cend[tt] >= qs;
+                    const bool hit = tt < tsplit && cend[tt] >= qs;
                     const unsigned m = __ballot_sync(kFull, hit);
                     const int k = __popc(m);
                     if (w + k > capq) {
@@ -605,39 +647,24 @@ __global__ void __launch_bounds__(kThreads, 4) k_tiles(TileArgs<S> a) {
                         break;
                     }
                     if (hit) {
-                        const int64_t pos = cpos[tt];
-                        dst[w + __popc(m & lanemask_lt())] = a.values ? a.data[pos] : (int32_t)(pos - lo);
+                        const int32_t pos = cpos[tt];
+                        dst[w + __popc(m & lanemask_lt())] = a.values ? a.data[pos] : pos - (int32_t)lo;
                     }
                     w += k;
-                    if (mi != kFull) {
-                        tsplit = kk + __popc(mi);
-                        break;
-                    }
                 }
-                // part B: long candidates at or below C index max(tsplit, ta)
-                const int tb = max(tsplit, ta);
-                if (!bad && tb < nc && nl > 0) {
-                    const int32_t pb = cpos[tb];
-                    const int lb = warp_search_desc_le(lpos, nl, (int64_t)pb, lane);
-                    // only long candidates ending before the tile's max qs can miss
-                    int miss = 0;
-                    if (nlnu <= kLnu) {
-                        for (int k = lane; k < nlnu; k += 32)
-                            miss += (s_lnu_pos[k] <= pb && s_lnu_end[k] < qs) ? 1 : 0;
-#pragma unroll
-                        for (int d = 16; d > 0; d >>= 1) miss += __shfl_xor_sync(kFull, miss, d);
-                    } else {
-                        miss = 1;
-                    }
-                    if (miss == 0) {
-                        // every long candidate from lb on is a hit: straight copy
+                // part B: the long candidates from lb on
+                const int lbf = q_lb[i];
+                const bool miss = lbf < 0;
+                const int lb = miss ? -1 - lbf : lbf;
+                if (!bad && lb < nl) {
+                    if (!miss) {
                         const int len = nl - lb;
                         if (w + len > capq) {
                             bad = true;
                         } else {
                             for (int k = lane; k < len; k += 32) {
                                 const int32_t pos = lpos[lb + k];
-                                dst[w + k] = a.values ? a.data[pos] : (int32_t)(pos - lo);
+                                dst[w + k] = a.values ? a.data[pos] : pos - (int32_t)lo;
                             }
                             w += len;
                         }
@@ -652,8 +679,8 @@ __global__ void __launch_bounds__(kThreads, 4) k_tiles(TileArgs<S> a) {
                                 break;
                             }
                             if (hit) {
-                                const int64_t pos = lpos[tt];
-                                dst[w + __popc(m & lanemask_lt())] = a.values ? a.data[pos] : (int32_t)(pos - lo);
+                                const int32_t pos = lpos[tt];
+                                dst[w + __popc(m & lanemask_lt())] = a.values ? a.data[pos] : pos - (int32_t)lo;
                             }
                             w += k;
                         }
@@ -938,7 +965,7 @@ UbView<S> make_ub(const BatchedWorkspace& ws, int mode) {
 size_t tile_smem(const BatchedParams& p, size_t s) {
     // cend + cpos, the tile's query records, then frontier list + counts + masks
     // candidates (end, position), per-query records, BFS scratch / long list (+ 64-bit starts)
-    return (size_t)p.cap * (s + 4) + (size_t)p.tile_q * (s + 12 + 16) + (size_t)p.cap * 12 +
+    return (size_t)p.cap * (s + 4) + (size_t)p.tile_q * (s + 12 + 16 + 12) + (size_t)p.cap * 12 +
            (s == 8 ? (size_t)p.cap * 8 : 0) + 64;
 }
 
