@@ -669,20 +669,33 @@ __global__ void __launch_bounds__(kThreads, 4) k_tiles(TileArgs<S> a) {
                             w += len;
                         }
                     } else {
-                        for (int kk = lb; kk < nl; kk += 32) {
-                            const int tt = kk + lane;
-                            const bool hit = tt < nl && lend[tt] >= qs;
-                            const unsigned m = __ballot_sync(kFull, hit);
-                            const int k = __popc(m);
-                            if (w + k > capq) {
+                        // 128 candidates per round as four independent 32-wide slices, so their
+                        // shared-memory reads and ballots overlap instead of chaining
+                        const unsigned lt = lanemask_lt();
+                        for (int kk = lb; kk < nl; kk += 128) {
+                            bool hit[4];
+                            int32_t pv[4];
+                            unsigned m[4];
+#pragma unroll
+                            for (int s = 0; s < 4; ++s) {
+                                const int tt = kk + 32 * s + lane;
+                                hit[s] = tt < nl && lend[tt] >= qs;
+                                pv[s] = hit[s] ? lpos[tt] : 0;
+                            }
+#pragma unroll
+                            for (int s = 0; s < 4; ++s) m[s] = __ballot_sync(kFull, hit[s]);
+                            const int c0 = __popc(m[0]), c1 = __popc(m[1]), c2 = __popc(m[2]), c3 = __popc(m[3]);
+                            if (w + c0 + c1 + c2 + c3 > capq) {
                                 bad = true;
                                 break;
                             }
-                            if (hit) {
-                                const int32_t pos = lpos[tt];
-                                dst[w + __popc(m & lanemask_lt())] = a.values ? a.data[pos] : pos - (int32_t)lo;
+                            const int64_t base[4] = {w, w + c0, w + c0 + c1, w + c0 + c1 + c2};
+#pragma unroll
+                            for (int s = 0; s < 4; ++s) {
+                                if (hit[s])
+                                    dst[base[s] + __popc(m[s] & lt)] = a.values ? a.data[pv[s]] : pv[s] - (int32_t)lo;
                             }
-                            w += k;
+                            w += c0 + c1 + c2 + c3;
                         }
                     }
                 }
