@@ -155,6 +155,9 @@ struct TileArgs {
     bool values;
     int32_t* out;
     int* d_err;
+    // per-tile candidate lists stored by the count pass and reloaded by the emit pass
+    unsigned char* cache;
+    int64_t cache_stride;
 };
 
 // ---- per-query walk (long queries, overflowing tiles): one warp, direct output ----
@@ -438,73 +441,138 @@ __global__ void __launch_bounds__(kThreads, 4) k_tiles(TileArgs<S> a) {
             bool per_query = is_long;
             int nc = 0, nl = 0, nlnu = 0;
             if (!is_long) {
-                // L = min qs, Q = max qs over the run; umax = ub of the run's last query
-                S mn = Lim<S>::hi, mx = Lim<S>::lo;
-                for (int i = r0 + tid; i < r1; i += kThreads) {
-                    mn = q_s[i] < mn ? q_s[i] : mn;
-                    mx = q_s[i] > mx ? q_s[i] : mx;
+                // a tile that is one run can reuse the candidate lists the count pass stored
+                const bool whole = (r0 == 0 && r1 == nt);
+                unsigned char* rec = (whole && a.cache) ? a.cache + (size_t)t * a.cache_stride : nullptr;
+                int32_t* g_cpos = reinterpret_cast<int32_t*>(rec + 16);
+                S* g_cend = reinterpret_cast<S*>(g_cpos + cap);
+                S* g_cstart = g_cend + cap;
+                int32_t* g_lpos = reinterpret_cast<int32_t*>(g_cstart + cap);
+                S* g_lend = reinterpret_cast<S*>(g_lpos + cap);
+                int32_t* g_lnu_pos = reinterpret_cast<int32_t*>(g_lend + cap);
+                S* g_lnu_end = reinterpret_cast<S*>(g_lnu_pos + kLnu);
+                bool cached = false;
+                if (EMIT && rec) {
+                    if (tid == 0) {
+                        const int32_t* hdr = reinterpret_cast<const int32_t*>(rec);
+                        s_n = hdr[3] == 1 ? hdr[0] : -1;
+                        s_sum = hdr[1];
+                        s_nlnu = hdr[2];
+                    }
+                    __syncthreads();
+                    if (s_n >= 0) {
+                        nc = s_n;
+                        nl = s_sum;
+                        nlnu = s_nlnu;
+                        for (int k = tid; k < nc; k += kThreads) {
+                            cpos[k] = g_cpos[k];
+                            cend[k] = g_cend[k];
+                            cstart[k] = g_cstart[k];
+                        }
+                        for (int k = tid; k < nl; k += kThreads) {
+                            lpos[k] = g_lpos[k];
+                            lend[k] = g_lend[k];
+                        }
+                        for (int k = tid; k < nlnu && k < kLnu; k += kThreads) {
+                            s_lnu_pos[k] = g_lnu_pos[k];
+                            s_lnu_end[k] = g_lnu_end[k];
+                        }
+                        __syncthreads();
+                        cached = true;
+                    }
                 }
-#pragma unroll
-                for (int d = 16; d > 0; d >>= 1) {
-                    const S o = __shfl_xor_sync(kFull, mn, d);
-                    mn = o < mn ? o : mn;
-                    const S p = __shfl_xor_sync(kFull, mx, d);
-                    mx = p > mx ? p : mx;
-                }
-                if (lane == 0) {
-                    s_red[warp] = mn;
-                    s_red2[warp] = mx;
-                }
-                if (tid == 0) s_nlnu = 0;
-                __syncthreads();
-                S L = s_red[0], Q = s_red2[0];
-#pragma unroll
-                for (int w = 1; w < kWarpsPerCta; ++w) {
-                    L = s_red[w] < L ? s_red[w] : L;
-                    Q = s_red2[w] > Q ? s_red2[w] : Q;
-                }
-                const int64_t umax = q_u[r1 - 1];
-                nc = gather_bfs<S>(a.P, lo, umax, L, cap, cpos, cend, lst, cnt, msk, s_wsum, &s_n, &s_sum);
-                per_query = nc < 0;
-                if (!per_query && nc > 0) {
-                    // long candidates (end - start >= X) into (lpos, lend), in order; the ones
-                    // ending before Q (possible misses for some query) also into the lnu list
-                    const int nb = (nc + 31) >> 5;
-                    for (int b = warp; b < nb; b += kWarpsPerCta) {
-                        const int tt = (b << 5) + lane;
-                        bool isl = false;
-                        if (tt < nc) {
-                            const S st = a.starts[cpos[tt]];
-                            cstart[tt] = st;
-                            isl = is_long_iv<S>(st, cend[tt], X);
-                            if (isl && cend[tt] < Q) {
-                                const int slot = atomicAdd(&s_nlnu, 1);
-                                if (slot < kLnu) {
-                                    s_lnu_pos[slot] = cpos[tt];
-                                    s_lnu_end[slot] = cend[tt];
+                if (!cached) {
+                    // L = min qs, Q = max qs over the run; umax = ub of the run's last query
+                    S mn = Lim<S>::hi, mx = Lim<S>::lo;
+                    for (int i = r0 + tid; i < r1; i += kThreads) {
+                        mn = q_s[i] < mn ? q_s[i] : mn;
+                        mx = q_s[i] > mx ? q_s[i] : mx;
+                    }
+    #pragma unroll
+                    for (int d = 16; d > 0; d >>= 1) {
+                        const S o = __shfl_xor_sync(kFull, mn, d);
+                        mn = o < mn ? o : mn;
+                        const S p = __shfl_xor_sync(kFull, mx, d);
+                        mx = p > mx ? p : mx;
+                    }
+                    if (lane == 0) {
+                        s_red[warp] = mn;
+                        s_red2[warp] = mx;
+                    }
+                    if (tid == 0) s_nlnu = 0;
+                    __syncthreads();
+                    S L = s_red[0], Q = s_red2[0];
+    #pragma unroll
+                    for (int w = 1; w < kWarpsPerCta; ++w) {
+                        L = s_red[w] < L ? s_red[w] : L;
+                        Q = s_red2[w] > Q ? s_red2[w] : Q;
+                    }
+                    const int64_t umax = q_u[r1 - 1];
+                    nc = gather_bfs<S>(a.P, lo, umax, L, cap, cpos, cend, lst, cnt, msk, s_wsum, &s_n, &s_sum);
+                    per_query = nc < 0;
+                    if (!per_query && nc > 0) {
+                        // long candidates (end - start >= X) into (lpos, lend), in order; the ones
+                        // ending before Q (possible misses for some query) also into the lnu list
+                        const int nb = (nc + 31) >> 5;
+                        for (int b = warp; b < nb; b += kWarpsPerCta) {
+                            const int tt = (b << 5) + lane;
+                            bool isl = false;
+                            if (tt < nc) {
+                                const S st = a.starts[cpos[tt]];
+                                cstart[tt] = st;
+                                isl = is_long_iv<S>(st, cend[tt], X);
+                                if (isl && cend[tt] < Q) {
+                                    const int slot = atomicAdd(&s_nlnu, 1);
+                                    if (slot < kLnu) {
+                                        s_lnu_pos[slot] = cpos[tt];
+                                        s_lnu_end[slot] = cend[tt];
+                                    }
                                 }
                             }
+                            const unsigned m = __ballot_sync(kFull, isl);
+                            if (lane == 0) {
+                                s_bmask[b] = m;
+                                s_boff[b] = __popc(m);
+                            }
                         }
-                        const unsigned m = __ballot_sync(kFull, isl);
-                        if (lane == 0) {
-                            s_bmask[b] = m;
-                            s_boff[b] = __popc(m);
+                        __syncthreads();
+                        block_excl_scan(s_boff, nb, s_wsum, &s_sum);
+                        nl = s_sum;
+                        for (int b = warp; b < nb; b += kWarpsPerCta) {
+                            const unsigned m = s_bmask[b];
+                            if ((m >> lane) & 1u) {
+                                const int tt = (b << 5) + lane;
+                                const int idx = s_boff[b] + __popc(m & lanemask_lt());
+                                lpos[idx] = cpos[tt];
+                                lend[idx] = cend[tt];
+                            }
+                        }
+                        __syncthreads();
+                        nlnu = s_nlnu;
+                    }
+                    if (!EMIT && rec) {
+                        // store the lists for the emit pass (header last field: 1 = usable)
+                        for (int k = tid; k < nc; k += kThreads) {
+                            g_cpos[k] = cpos[k];
+                            g_cend[k] = cend[k];
+                            g_cstart[k] = cstart[k];
+                        }
+                        for (int k = tid; k < nl; k += kThreads) {
+                            g_lpos[k] = lpos[k];
+                            g_lend[k] = lend[k];
+                        }
+                        for (int k = tid; k < nlnu && k < kLnu; k += kThreads) {
+                            g_lnu_pos[k] = s_lnu_pos[k];
+                            g_lnu_end[k] = s_lnu_end[k];
+                        }
+                        if (tid == 0) {
+                            int32_t* hdr = reinterpret_cast<int32_t*>(rec);
+                            hdr[0] = per_query ? -1 : nc;
+                            hdr[1] = nl;
+                            hdr[2] = nlnu;
+                            hdr[3] = per_query ? 0 : 1;
                         }
                     }
-                    __syncthreads();
-                    block_excl_scan(s_boff, nb, s_wsum, &s_sum);
-                    nl = s_sum;
-                    for (int b = warp; b < nb; b += kWarpsPerCta) {
-                        const unsigned m = s_bmask[b];
-                        if ((m >> lane) & 1u) {
-                            const int tt = (b << 5) + lane;
-                            const int idx = s_boff[b] + __popc(m & lanemask_lt());
-                            lpos[idx] = cpos[tt];
-                            lend[idx] = cend[tt];
-                        }
-                    }
-                    __syncthreads();
-                    nlnu = s_nlnu;
                 }
                 if (per_query) nc = 0;
             }
@@ -1159,7 +1227,8 @@ int batched_prepare_queries(BatchedWorkspace& ws, MapView<S> m, const QueryBatch
 template <typename S>
 static int run_tiles(BatchedWorkspace& ws, MapView<S> m, Levels<S> L, int H, int64_t nq, bool emit,
                      uint32_t* counts, int32_t* heads, const int32_t* heads_in, const int64_t* offsets,
-                     int64_t out_base, int order, bool values, int32_t* out, int* d_err, cudaStream_t st) {
+                     int64_t out_base, int order, bool values, int32_t* out, int* d_err, bool use_cache,
+                     cudaStream_t st) {
     SI_OKR(ws.counters.reserve(sizeof(int) * 4));
     SI_CU(cudaMemsetAsync(ws.counters.p, 0, sizeof(int) * 4, st));
     TileArgs<S> a;
@@ -1187,6 +1256,8 @@ static int run_tiles(BatchedWorkspace& ws, MapView<S> m, Levels<S> L, int H, int
     a.values = values;
     a.out = out;
     a.d_err = d_err;
+    a.cache = (use_cache && ws.cache_ok) ? ws.tile_cache.as<unsigned char>() : nullptr;
+    a.cache_stride = ws.cache_stride;
     const size_t sm = tile_smem(ws.prm, sizeof(S));
     int dev = 0, nsm = 152, per_sm = 1;
     cudaGetDevice(&dev);
@@ -1214,8 +1285,16 @@ int batched_count(BatchedWorkspace& ws, MapView<S> m, Levels<S> L, int H, const 
     if (ws.prepared_nq != nq || ws.prepared_qs != q.qs) return SI_ERR_INVALID;
     SI_OKR(ws.heads.reserve(sizeof(int32_t) * nq));
     ws.n_heads = nq;
+    // room for every tile's candidate lists, so that the emit pass need not gather again;
+    // without room (device budget) the emit pass simply gathers again
+    ws.cache_stride = (int64_t)round_up(16 + (int64_t)ws.prm.cap * (8 + 3 * (int64_t)sizeof(S)) +
+                                            (int64_t)kLnu * (4 + (int64_t)sizeof(S)), 256);
+    const int64_t n_tiles = ceil_div(nq, ws.prm.tile_q);
+    ws.cache_ok = ws.tile_cache.reserve((size_t)(n_tiles * ws.cache_stride)) == SI_OK;
+    ws.cache_prm_tile = ws.prm.tile_q;
+    ws.cache_prm_cap = ws.prm.cap;
     return run_tiles<S>(ws, m, L, H, nq, false, counts, ws.heads.as<int32_t>(), nullptr, nullptr, 0, 0, false,
-                        nullptr, d_err, st);
+                        nullptr, d_err, true, st);
 }
 
 template <typename S>
@@ -1227,9 +1306,10 @@ int batched_emit(BatchedWorkspace& ws, MapView<S> m, Levels<S> L, int H, const Q
     if (q_offset < 0 || q_offset + nq > ws.n_heads) return SI_ERR_INVALID;
     const bool same = (q_offset == 0 && ws.prepared_nq == nq && ws.prepared_qs == q.qs);
     if (!same) SI_OKR(batched_prepare_queries<S>(ws, m, q, d_err, ub_mode, st));
+    const bool cache = same && ws.cache_ok && ws.cache_prm_tile == ws.prm.tile_q && ws.cache_prm_cap == ws.prm.cap;
     // sorted ids are relative to q; heads / offsets are shifted to the slice
     return run_tiles<S>(ws, m, L, H, nq, true, nullptr, nullptr, ws.heads.as<int32_t>() + q_offset, offsets,
-                        out_base, order, values, out, d_err, st);
+                        out_base, order, values, out, d_err, cache, st);
 }
 
 template <typename S>

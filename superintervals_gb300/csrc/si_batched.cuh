@@ -64,6 +64,11 @@ struct BatchedWorkspace {
     int prepared_mode = -1;
     int64_t n_heads = 0;
     long long launches = 0;      // kernels launched by this path
+    // candidate lists of every tile, written by the count pass, read by the emit pass
+    DBuf tile_cache;
+    bool cache_ok = false;
+    int64_t cache_stride = 0;
+    int cache_prm_tile = 0, cache_prm_cap = 0;
 };
 
 template <typename S>
