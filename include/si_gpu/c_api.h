@@ -173,6 +173,22 @@ int searchDeviceGpu(gSuperIntervals* si, const void* d_qs, const void* d_qe,
                     int64_t* d_offsets, int32_t* d_values, size_t capacity, size_t* total,
                     void* stream);
 
+/* Allocation-free search.  No counterpart in the reference: it exists for callers
+ * that cannot allocate device memory while they query (a host whose device memory
+ * belongs to another allocator or a fixed pool, or a query thread that must not
+ * call cudaMalloc).  Same result as searchDeviceGpu with values_not_idxs = 0 (the
+ * plain one-query-per-thread path), into caller-provided device buffers; the
+ * scratch it needs sits in one fixed device array inside the library (about
+ * 16.1 MiB, held on every device that loads the library until exit), so the call
+ * performs no cudaMalloc / cudaFree.  Limit: at most 4,194,304 queries per call
+ * (larger batches return SI_ERR_TOO_LARGE).  All calls share that array: calls
+ * that overlap on the GPU race and must be serialized by the caller.  The first
+ * call on a device looks the array up on that device; make it before any stream
+ * capture.  The index must already be built. */
+int searchIdxsNoAllocGpu(gSuperIntervals* si, const void* d_qs, const void* d_qe,
+                         const int32_t* d_qcontig, size_t nq, int order, int64_t* d_offsets,
+                         int32_t* d_values, size_t capacity, size_t* total, void* stream);
+
 /* Upper bound of every query end: contig-local position of the last interval
  * whose start <= qe, or -1.  upperBound (c_superintervals.h:195, 537-568) /
  * IntervalMap::upper_bound (superintervals.hpp:501-516), computed with the

@@ -92,6 +92,7 @@ SIGNATURES = {
     "countOverlapsDeviceGpu": (_I, [_H, _P, _P, _P, _SZ, _P, _P]),
     "searchDeviceGpu": (_I, [_H, _P, _P, _P, _SZ, _I, _I, _P, _P, _SZ, C.POINTER(_SZ), _P]),
     "upperBoundDeviceGpu": (_I, [_H, _P, _P, _SZ, _I, _P, _P]),
+    "searchIdxsNoAllocGpu": (_I, [_H, _P, _P, _P, _SZ, _I, _P, _P, _SZ, C.POINTER(_SZ), _P]),
     "createCsrResult": (cCsrResult, []),
     "clearCsrResult": (None, [C.POINTER(cCsrResult)]),
     "destroyCsrResult": (None, [C.POINTER(cCsrResult)]),

@@ -961,3 +961,105 @@ extern "C" int getBatchedParamsGpu(const gSuperIntervals* si, int* tile_q, int* 
     if (split_len) *split_len = si->bws.prm.split_len;
     return SI_OK;
 }
+
+// =====================================================================================
+// Allocation-free search (searchIdxsNoAllocGpu).
+//
+// Some callers cannot allocate device memory while they query: a host whose device memory is
+// owned by another allocator or a fixed pool, a query thread that must not grow its memory
+// footprint, or code that is not allowed to call cudaMalloc at that point.  For them this entry
+// point runs the count -> scan -> emit search without allocating anything: the caller passes
+// device buffers for the queries, the offsets and the results, and the scratch the search needs
+// (per-query counts, scan partials, a device error word) lives in one file-scope device array of
+// fixed size.  The index must already be built (building allocates).
+//
+// Limits:
+//   * at most kNoAllocMaxQueries queries per call; larger batches are rejected (SI_ERR_TOO_LARGE);
+//   * the array is part of the library image, so every device that loads the library holds it
+//     (about 16.1 MiB) until the process exits;
+//   * every call shares the array and it keeps the last call's contents: calls that overlap on
+//     the GPU (other streams, threads or handles) race on it, so the caller serializes them;
+//   * the first call on a device looks up the array's device address with that device current;
+//     make that first call before any stream capture.
+// =====================================================================================
+namespace {
+
+constexpr size_t kNoAllocMaxQueries = (size_t)1 << 22;
+constexpr size_t kNoAllocHeader = 256;        // device error word
+constexpr size_t kNoAllocScanBytes = 64 << 10;  // scan partials for up to kNoAllocMaxQueries
+constexpr size_t kNoAllocBytes = kNoAllocHeader + kNoAllocScanBytes + kNoAllocMaxQueries * sizeof(uint32_t);
+
+__device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
+
+std::mutex g_noalloc_mu;
+void* g_noalloc_addr[64] = {nullptr};
+
+// Device address of the scratch array on the current device (looked up once per device).
+int noalloc_scratch(int device, unsigned char** out) {
+    if (device < 0 || device >= 64) return fail(SI_ERR_INVALID, "device id %d out of range", device);
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_noalloc_addr[device]) {
+        void* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess || !p) {
+            cudaGetLastError();
+            return fail(SI_ERR_CUDA, "cudaGetSymbolAddress(scratch) failed: %s", cudaGetErrorString(e));
+        }
+        g_noalloc_addr[device] = p;
+    }
+    *out = static_cast<unsigned char*>(g_noalloc_addr[device]);
+    return SI_OK;
+}
+
+template <typename S>
+int search_noalloc(gSuperIntervals* si, const sig::QueryBatch& q, int order, int64_t* d_offsets, int32_t* d_out,
+                   size_t capacity, size_t* total, cudaStream_t st) {
+    unsigned char* base = nullptr;
+    SI_TRY(noalloc_scratch(si->device, &base));
+    int* d_err = reinterpret_cast<int*>(base);
+    void* scan_tmp = base + kNoAllocHeader;
+    uint32_t* counts = reinterpret_cast<uint32_t*>(base + kNoAllocHeader + kNoAllocScanBytes);
+    if (sig::scan_temp_bytes(q.nq) > kNoAllocScanBytes)
+        return fail(SI_ERR_TOO_LARGE, "scan scratch too small for %lld queries", (long long)q.nq);
+    SI_CK(cudaMemsetAsync(d_err, 0, sizeof(int), st));  // the error word starts at zero
+    if (si->n == 0 || q.nq == 0) {
+        SI_CK(cudaMemsetAsync(d_offsets, 0, sizeof(int64_t) * (q.nq + 1), st));
+        SI_CK(cudaStreamSynchronize(st));
+        if (total) *total = 0;
+        return SI_OK;
+    }
+    SI_CK(sig::launch_count_plain<S>(view<S>(si), q, counts, d_err, st));
+    SI_CK(sig::exclusive_scan_u32_to_i64(counts, d_offsets, q.nq, scan_tmp, st));
+    int64_t P = 0;
+    SI_CK(cudaMemcpyAsync(&P, d_offsets + q.nq, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+    SI_CK(cudaStreamSynchronize(st));
+    if (total) *total = (size_t)P;
+    int e = 0;
+    if ((size_t)P <= capacity) {
+        SI_CK(sig::launch_emit_plain<S>(view<S>(si), q, d_offsets, 0, order, false, d_out, d_err, st));
+    }
+    SI_CK(cudaMemcpyAsync(&e, d_err, sizeof(int), cudaMemcpyDeviceToHost, st));
+    SI_CK(cudaStreamSynchronize(st));
+    if (e == sig::kDevBadContig) return fail(SI_ERR_INVALID, "a query names a contig outside [0, %d)", si->G);
+    if (e != 0) return fail(SI_ERR_CUDA, "device error word %d", e);
+    if ((size_t)P > capacity) return fail(SI_ERR_CAPACITY, "output needs %lld values, capacity %zu", (long long)P, capacity);
+    return SI_OK;
+}
+
+}  // namespace
+
+extern "C" int searchIdxsNoAllocGpu(gSuperIntervals* si, const void* d_qs, const void* d_qe,
+                                    const int32_t* d_qcontig, size_t nq, int order, int64_t* d_offsets,
+                                    int32_t* d_values, size_t capacity, size_t* total, void* stream) {
+    SI_TRY(check_built(si));
+    if (order != SI_ORDER_IDXS_CPP && order != SI_ORDER_DESC) return fail(SI_ERR_INVALID, "unknown order");
+    if (nq > kNoAllocMaxQueries)
+        return fail(SI_ERR_TOO_LARGE, "the allocation-free search takes at most %zu queries per call, got %zu",
+                    kNoAllocMaxQueries, nq);
+    if (!d_offsets || (nq && (!d_qs || !d_qe))) return fail(SI_ERR_INVALID, "null device buffer");
+    SI_TRY(set_dev(si));
+    cudaStream_t st = stream ? (cudaStream_t)stream : si->st;
+    sig::QueryBatch q{d_qs, d_qe, d_qcontig, (int64_t)nq};
+    if (si->bits == 64) return search_noalloc<int64_t>(si, q, order, d_offsets, d_values, capacity, total, st);
+    return search_noalloc<int32_t>(si, q, order, d_offsets, d_values, capacity, total, st);
+}
