@@ -41,7 +41,7 @@ PEAK_FALLBACK_GBS = 6800.0
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=8)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", default="config3",
@@ -102,7 +102,7 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "100"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
@@ -197,13 +197,15 @@ def run_gpu(args, rank, world, dist):
     for e in ev:
         _capi.check(lib.eventCreateGpu(C.byref(e)))
 
-    def timed(k, w, fn):
+    def timed(k, w, fn, on_start=None):
         for _ in range(w):
             _capi.check(lib.flushL2Gpu(st))
             fn()
         _capi.check(lib.streamSynchronizeGpu(st))
         if dist:
             dist.barrier()
+        if on_start:
+            on_start()
         total_ms = 0.0
         for _ in range(k):
             _capi.check(lib.flushL2Gpu(st))
@@ -218,8 +220,14 @@ def run_gpu(args, rank, world, dist):
             dist.barrier()
         return total_ms
 
+    launches = {}
+
+    def counted():
+        launches["before"] = lib.getLaunchCountGpu()
+
     with ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) as clk:
-        total_ms = timed(args.steps, args.warmup, step)
+        total_ms = timed(args.steps, args.warmup, step, on_start=counted)
+    launches_timed = lib.getLaunchCountGpu() - launches["before"]
     if dist:
         import torch
         t = torch.tensor([total_ms], dtype=torch.float64)
@@ -227,6 +235,7 @@ def run_gpu(args, rank, world, dist):
         total_ms = float(t.item())
     ms_per_step = total_ms / args.steps
     res = {"wl": wl, "P": P, "nq": nq, "ms_per_step": ms_per_step, "build_s": build_s,
+           "launches": launches_timed,
            "clocks": clk.summary(), "s_bytes": s_bytes}
     if args.profile_only:
         return res
@@ -250,6 +259,8 @@ def run_gpu(args, rank, world, dist):
         idx.set_path(path)
         idx.set_upper_bound(ub)
 
+    lib.deviceFreeGpu(d_out)       # the e2e leg below stages its own result buffer
+    d_out = None
     # e2e through the C-ABI with pinned host buffers
     if not args.no_e2e:
         def pinned(nbytes):
@@ -401,7 +412,7 @@ def main():
                         "peak_kind": peak_kind, "algorithmic_bytes": algo,
                         "phase_ms": {"count": ph[0], "scan": ph[1], "emit": ph[2], "prepare": ph[3]},
                         "whole_step_frac": (algo / (ms / 1000.0) / 1e9) / peak}
-    line["gpu_launches"] = None
+    line["gpu_launches"] = res["launches"]
     if "plain_ms" in res:
         line["plain_gpu"] = {"ms_per_step": res["plain_ms"], "queries_per_s": nq / (res["plain_ms"] / 1e3),
                              "speedup_vs_plain": res["plain_ms"] / ms}

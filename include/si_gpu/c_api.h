@@ -217,6 +217,8 @@ int eventCreateGpu(void** ev);
 int eventDestroyGpu(void* ev);
 int eventRecordGpu(void* ev, void* stream);
 int eventElapsedMsGpu(void* start, void* stop, float* ms);
+/* Number of kernels this library has launched in this process. */
+long long getLaunchCountGpu(void);
 /* L2 flush: writes a device buffer larger than L2 on the stream. */
 int flushL2Gpu(void* stream);
 

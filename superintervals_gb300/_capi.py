@@ -110,6 +110,7 @@ SIGNATURES = {
     "eventRecordGpu": (_I, [_P, _P]),
     "eventElapsedMsGpu": (_I, [_P, _P, C.POINTER(C.c_float)]),
     "flushL2Gpu": (_I, [_P]),
+    "getLaunchCountGpu": (C.c_longlong, []),
 }
 
 _lib = None

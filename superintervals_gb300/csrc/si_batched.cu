@@ -331,26 +331,6 @@ __device__ int gather_bfs(const Pyr<S>& P, int64_t lo, int64_t umax, S L, int ca
     return nf;
 }
 
-// First index in [0, n) whose value is <= key in a DESCENDING array (n when none).
-// Warp-cooperative 32-ary search: one round of 32 samples narrows the range 32-fold.
-__device__ __forceinline__ int warp_search_desc_le(const int32_t* arr, int n, int64_t key, int lane) {
-    int lo = 0, hi = n;  // answer in [lo, hi]
-    while (hi - lo > 32) {
-        const int step = (hi - lo + 31) >> 5;
-        const int idx = lo + lane * step;
-        const unsigned m = __ballot_sync(kFull, idx < hi && (int64_t)arr[idx] > key);
-        const int k = __popc(m);  // samples above key form a prefix
-        if (k == 0) return lo;
-        const int nlo = lo + (k - 1) * step + 1;
-        const int nhi = min(hi, lo + k * step);
-        lo = nlo;
-        hi = nhi;
-    }
-    const int idx = lo + lane;
-    const unsigned m = __ballot_sync(kFull, idx < hi && (int64_t)arr[idx] > key);
-    return lo + __popc(m);
-}
-
 // start >= qs - X, without overflow
 template <typename S>
 __device__ __forceinline__ bool near_start(S start, S qs, int64_t X) {
@@ -1089,6 +1069,7 @@ int build_learned(BatchedWorkspace& ws, MapView<S> m, cudaStream_t st) {
     SI_CU(cudaMemsetAsync(acc.p, 0, sizeof(double) * 2 * G, st));
     dim3 grid(64, (unsigned)std::min(G, 65535));
     k_root_sums<S><<<grid, kThreads, 0, st>>>(m.starts, m.seg, G, nullptr, acc.as<double>(), 0);
+    note_launch();
     SI_CU(cudaGetLastError());
     std::vector<double> a(2 * G), mean(G);
     SI_CU(cudaMemcpyAsync(a.data(), acc.p, sizeof(double) * 2 * G, cudaMemcpyDeviceToHost, st));
@@ -1101,6 +1082,7 @@ int build_learned(BatchedWorkspace& ws, MapView<S> m, cudaStream_t st) {
     // pass 2: centred products -> root slope; root maps key to leaf coordinate
     SI_CU(cudaMemsetAsync(acc.p, 0, sizeof(double) * 2 * G, st));
     k_root_sums<S><<<grid, kThreads, 0, st>>>(m.starts, m.seg, G, ws.ub.key_mean.as<double>(), acc.as<double>(), 1);
+    note_launch();
     SI_CU(cudaGetLastError());
     SI_CU(cudaMemcpyAsync(a.data(), acc.p, sizeof(double) * 2 * G, cudaMemcpyDeviceToHost, st));
     SI_CU(cudaStreamSynchronize(st));
@@ -1118,6 +1100,7 @@ int build_learned(BatchedWorkspace& ws, MapView<S> m, cudaStream_t st) {
     k_leaf_bounds<S><<<dim3(256, G), kThreads, 0, st>>>(m.starts, m.seg, G, ws.ub.root.as<double2>(),
                                                         ws.ub.key_mean.as<double>(), ws.ub.leaf_base.as<int32_t>(),
                                                         bnd.as<int32_t>());
+    note_launch();
     SI_CU(cudaGetLastError());
     // leaves never reached by any key keep INT32_MAX-ish: clamp to the contig size on the host
     std::vector<int32_t> hb(total);
@@ -1132,6 +1115,7 @@ int build_learned(BatchedWorkspace& ws, MapView<S> m, cudaStream_t st) {
     k_leaf_fit<S><<<(unsigned)std::min(total, 152 * 32), kThreads, 0, st>>>(
         m.starts, m.seg, lc.as<int32_t>(), ws.ub.leaf_base.as<int32_t>(), bnd.as<int32_t>(),
         ws.ub.key_mean.as<double>(), ws.ub.leaves.as<LeafModel>(), total);
+    note_launch();
     SI_CU(cudaGetLastError());
     SI_CU(cudaStreamSynchronize(st));
     ws.launches += 5;
@@ -1153,6 +1137,7 @@ int build_eytz(BatchedWorkspace& ws, MapView<S> m, cudaStream_t st) {
     ws.ub.eytz_n = K + 1;
     SI_OKR(ws.ub.eytz_keys.reserve(sizeof(S) * (size_t)G * (K + 1)));
     k_eytz_build<S><<<dim3(nblk(K + 1), G), kThreads, 0, st>>>(m.starts, m.seg, G, K, ws.ub.eytz_keys.as<S>());
+    note_launch();
     SI_CU(cudaGetLastError());
     SI_CU(cudaStreamSynchronize(st));
     ws.launches += 1;
@@ -1204,6 +1189,7 @@ int batched_prepare_queries(BatchedWorkspace& ws, MapView<S> m, const QueryBatch
     k_qkeys<S><<<nblk(nq), kThreads, 0, st>>>(static_cast<const S*>(q.qs), static_cast<const S*>(q.qe), q.qc, nq,
                                               ws.prm.long_len, kp[0], K == 3 ? kp[1] : nullptr, wc,
                                               ws.pay.as<uint32_t>());
+    note_launch();
     SI_CU(cudaGetLastError());
     bool in_alt = false;
     int passes = 0;
@@ -1216,6 +1202,7 @@ int batched_prepare_queries(BatchedWorkspace& ws, MapView<S> m, const QueryBatch
     k_qprep<S><<<nblk(nq), kThreads, sm, st>>>(spay, swc, static_cast<const S*>(q.qs), static_cast<const S*>(q.qe),
                                               nq, m, U, ws.sq_s.as<S>(), ws.sq_u.as<int32_t>(),
                                               ws.sq_c.as<uint32_t>(), ws.sq_id.as<int32_t>(), d_err);
+    note_launch();
     SI_CU(cudaGetLastError());
     ws.launches += 2 + 3 * passes + 1;
     ws.prepared_qs = q.qs;
@@ -1272,6 +1259,7 @@ static int run_tiles(BatchedWorkspace& ws, MapView<S> m, Levels<S> L, int H, int
     const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)nsm * std::max(per_sm, 1), a.n_tiles));
     if (emit) k_tiles<S, true><<<grid, kThreads, sm, st>>>(a);
     else k_tiles<S, false><<<grid, kThreads, sm, st>>>(a);
+    note_launch();
     SI_CU(cudaGetLastError());
     ws.launches += 1;
     return SI_OK;
@@ -1318,6 +1306,7 @@ int upper_bounds(BatchedWorkspace& ws, MapView<S> m, const QueryBatch& q, int ub
     if (q.nq <= 0) return SI_OK;
     UbView<S> U = make_ub<S>(ws, ub_mode);
     k_ub_plain<S><<<nblk(q.nq), kThreads, 0, st>>>(static_cast<const S*>(q.qe), q.qc, q.nq, m, U, out, d_err);
+    note_launch();
     SI_CU(cudaGetLastError());
     ws.launches += 1;
     return SI_OK;

@@ -203,6 +203,7 @@ cudaError_t launch_check_sorted(const S* s, const S* e, int64_t n, const int64_t
     if (err != cudaSuccess || n <= 1) return err;
     const unsigned blocks = (unsigned)std::min<int64_t>(ceil_div(n, kThreads), 152 * 16);
     k_check_sorted<S><<<blocks, kThreads, 0, st>>>(s, e, n, seg, G, d_flag);
+    note_launch();
     return cudaGetLastError();
 }
 
@@ -220,6 +221,7 @@ cudaError_t launch_make_keys(const S* s, const S* e, int64_t n, const int64_t* s
     for (int k = 0; k < K; ++k) w[k] = kw[k];
     k_make_keys<S><<<blocks_for(n), kThreads, 0, st>>>(s, e, n, seg, G, w[0], w[1], w[2], w[3],
                                                       w[4], payload);
+    note_launch();
     return cudaGetLastError();
 }
 
@@ -232,6 +234,7 @@ cudaError_t launch_decode(const uint32_t* const* kw, const uint32_t* perm, const
     const uint32_t* w3 = sizeof(S) == 8 ? kw[3] : nullptr;
     k_decode<S><<<blocks_for(n_pad), kThreads, 0, st>>>(kw[0], kw[1], w2, w3, perm, data_in, n,
                                                        n_pad, starts, ends, data);
+    note_launch();
     return cudaGetLastError();
 }
 
@@ -242,6 +245,7 @@ cudaError_t launch_copy_pad(const S* s_in, const S* e_in, const int32_t* d_in, i
     if (n_pad <= 0) return cudaSuccess;
     k_copy_pad<S><<<blocks_for(n_pad), kThreads, 0, st>>>(s_in, e_in, d_in, n, n_pad, starts, ends,
                                                          data, perm);
+    note_launch();
     return cudaGetLastError();
 }
 
@@ -267,6 +271,7 @@ cudaError_t launch_pyramid(const S* ends, const int64_t* sizes, int H, S* const*
     for (int h = 1; h <= H; ++h) {
         const int64_t nodes = ceil_div(m, 32);
         k_level_max<S><<<blocks_for(sizes[h]), kThreads, 0, st>>>(in, nodes, sizes[h], lvl[h - 1]);
+        note_launch();
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) return e;
         in = lvl[h - 1];
@@ -280,6 +285,7 @@ cudaError_t launch_branch(const S* ends, int64_t n, int64_t n_pad, Levels<S> L, 
                           const int64_t* seg, int G, int32_t* branch, cudaStream_t st) {
     if (n <= 0) return cudaSuccess;
     k_branch<S><<<blocks_for(n_pad), kThreads, 0, st>>>(ends, n, n_pad, L, H, seg, G, branch);
+    note_launch();
     return cudaGetLastError();
 }
 

@@ -1063,3 +1063,12 @@ extern "C" int searchIdxsNoAllocGpu(gSuperIntervals* si, const void* d_qs, const
     if (si->bits == 64) return search_noalloc<int64_t>(si, q, order, d_offsets, d_values, capacity, total, st);
     return search_noalloc<int32_t>(si, q, order, d_offsets, d_values, capacity, total, st);
 }
+
+namespace {
+std::atomic<long long> g_launches{0};
+}
+namespace sig {
+void note_launch(int n) { g_launches += n; }
+}  // namespace sig
+
+extern "C" long long getLaunchCountGpu(void) { return g_launches.load(); }

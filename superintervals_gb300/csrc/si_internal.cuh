@@ -38,6 +38,9 @@ __device__ __forceinline__ uint32_t lanemask_lt() {
 }
 
 inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
+
+// Counts the library's own kernel launches (reported by getLaunchCountGpu).
+void note_launch(int n = 1);
 inline int64_t round_up(int64_t a, int64_t b) { return ceil_div(a, b) * b; }
 
 // Device-side error word written by kernels that detect bad input or give up

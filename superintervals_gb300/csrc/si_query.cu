@@ -158,6 +158,7 @@ cudaError_t launch_count_plain(MapView<S> m, QueryBatch q, uint32_t* counts, int
     if (q.nq <= 0) return cudaSuccess;
     k_count_plain<S><<<blocks_for(q.nq), kThreads, 0, st>>>(
         m, static_cast<const S*>(q.qs), static_cast<const S*>(q.qe), q.qc, q.nq, counts, d_err);
+    note_launch();
     return cudaGetLastError();
 }
 
@@ -168,6 +169,7 @@ cudaError_t launch_emit_plain(MapView<S> m, QueryBatch q, const int64_t* offsets
     k_emit_plain<S><<<blocks_for(q.nq), kThreads, 0, st>>>(
         m, static_cast<const S*>(q.qs), static_cast<const S*>(q.qe), q.qc, q.nq, offsets, out_base,
         order, values, out, d_err);
+    note_launch();
     return cudaGetLastError();
 }
 
@@ -177,6 +179,7 @@ cudaError_t launch_any_plain(MapView<S> m, QueryBatch q, uint8_t* out, int* d_er
     if (q.nq <= 0) return cudaSuccess;
     k_any_plain<S><<<blocks_for(q.nq), kThreads, 0, st>>>(
         m, static_cast<const S*>(q.qs), static_cast<const S*>(q.qe), q.qc, q.nq, out, d_err);
+    note_launch();
     return cudaGetLastError();
 }
 

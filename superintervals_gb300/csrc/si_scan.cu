@@ -94,17 +94,20 @@ cudaError_t scan_impl(const Tin* in, Tout* out, int64_t n, char* temp, cudaStrea
     const int64_t tiles = ceil_div(n, kTile);
     if (tiles == 1) {
         k_tile_scan<Tin, Tout><<<1, kThreads, 0, st>>>(in, n, (const Tout*)nullptr, out);
+        note_launch();
         return cudaGetLastError();
     }
     Tout* totals = reinterpret_cast<Tout*>(temp);
     Tout* tprefix = totals + round_up(tiles, 64);
     char* next = reinterpret_cast<char*>(tprefix + round_up(tiles + 1, 64));
     k_tile_totals<Tin, Tout><<<(unsigned)tiles, kThreads, 0, st>>>(in, n, totals);
+    note_launch();
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     e = scan_impl<Tout, Tout>(totals, tprefix, tiles, next, st);
     if (e != cudaSuccess) return e;
     k_tile_scan<Tin, Tout><<<(unsigned)tiles, kThreads, 0, st>>>(in, n, tprefix, out);
+    note_launch();
     return cudaGetLastError();
 }
 

@@ -193,6 +193,7 @@ cudaError_t radix_sort(uint32_t* const* keys, uint32_t* const* alt_keys, uint32_
     for (int w = 0; w < K; ++w) kp.w[w] = keys[w];
     int gblocks = (int)std::min<int64_t>(ceil_div(n, kThreads), 152 * 8);
     k_global_hist<<<gblocks, kThreads, 0, st>>>(kp, K, n, ghist);
+    note_launch();
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     uint32_t hh[kMaxKeyWords * 4 * kRadix];
     e = cudaMemcpyAsync(hh, ghist, sizeof(uint32_t) * K * 4 * kRadix, cudaMemcpyDeviceToHost, st);
@@ -217,6 +218,7 @@ cudaError_t radix_sort(uint32_t* const* keys, uint32_t* const* alt_keys, uint32_
                 if (hb[d] == (uint32_t)n) constant = true;
             if (constant) continue;
             k_pass_hist<<<(unsigned)tiles, kThreads, 0, st>>>(cur_k[w], 8 * b, n, H, tiles);
+            note_launch();
             if ((e = cudaGetLastError()) != cudaSuccess) return e;
             e = exclusive_scan_u32_to_u32(H, O, kRadix * tiles, scan_tmp, st);
             if (e != cudaSuccess) return e;
@@ -228,6 +230,7 @@ cudaError_t radix_sort(uint32_t* const* keys, uint32_t* const* alt_keys, uint32_
             }
             k_pass_scatter<<<(unsigned)tiles, kThreads, 0, st>>>(in, out, K, cur_p, oth_p, w, 8 * b,
                                                                  n, O, tiles);
+            note_launch();
             if ((e = cudaGetLastError()) != cudaSuccess) return e;
             for (int ww = 0; ww < K; ++ww) {
                 uint32_t* tmp = cur_k[ww];

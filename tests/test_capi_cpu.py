@@ -13,8 +13,8 @@ HEADER = os.path.join(ROOT, "include", "si_gpu", "c_api.h")
 def declared_functions():
     src = open(HEADER).read()
     src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
-    names = re.findall(r"^\s*(?:const\s+)?[A-Za-z_][A-Za-z0-9_]*\s*\**\s+\**([A-Za-z_][A-Za-z0-9_]*)\s*\(",
-                       src, flags=re.M)
+    names = re.findall(r"^\s*(?:const\s+)?(?:[A-Za-z_][A-Za-z0-9_]*\s+)*[A-Za-z_][A-Za-z0-9_]*\s*\**\s+\**"
+                       r"([A-Za-z_][A-Za-z0-9_]*)\s*\(", src, flags=re.M)
     return sorted(set(names))
 
 
