@@ -492,6 +492,18 @@ int search_host(gSuperIntervals* si, const S* qs, const S* qe, const int32_t* qc
         return fail(SI_ERR_CAPACITY, "output needs %lld values, capacity %zu", (long long)P, cap);
     }
     if (P == 0) return read_dev_err(si);
+    // A pinned (page-locked) result buffer is written by the emit kernel directly over the
+    // host link, so the transfer overlaps the emit instead of following it.
+    {
+        cudaPointerAttributes attr;
+        if (cudaPointerGetAttributes(&attr, h_out) == cudaSuccess && attr.type == cudaMemoryTypeHost &&
+            attr.devicePointer != nullptr) {
+            SI_TRY(run_emit<S>(si, q, 0, d_off, 0, order, values, static_cast<int32_t*>(attr.devicePointer), st));
+            SI_CK(cudaStreamSynchronize(st));
+            return read_dev_err(si);
+        }
+        cudaGetLastError();
+    }
     // chunked emit against the device output budget
     const int64_t budget = std::max<int64_t>((int64_t)(si->out_budget / sizeof(int32_t)), 1 << 20);
     const int64_t buf = std::min<int64_t>(P, budget);

@@ -326,3 +326,31 @@ def test_python_intervalmap_dropin(api):
         imap.at(3)
     with pytest.raises(ValueError):
         imap.count_batch(array("i", [1, 2]), array("i", [3]))
+
+
+@pytest.mark.parametrize("path", PATHS)
+def test_pinned_host_output_matches(api, oracle, path):
+    """searchBatchIntoGpu into pinned host buffers (written directly by the emit kernel)
+    gives the same CSR as into pageable buffers."""
+    import ctypes as C
+    from superintervals_gb300 import workloads as W
+    wl = W.config3(n=200_000, nq=50_000)
+    idx = _index(api, wl.starts, wl.ends, wl.data, seg=wl.seg, path=path)
+    off, out = idx.search(wl.q_starts, wl.q_ends, wl.q_contig)
+    lib = idx.lib
+    P, nq = int(off[-1]), wl.nq
+    h_off, h_out = C.c_void_p(), C.c_void_p()
+    api.check(lib.hostMallocPinnedGpu(C.byref(h_off), 8 * (nq + 1)))
+    api.check(lib.hostMallocPinnedGpu(C.byref(h_out), 4 * P))
+    qs, qe, qc = (np.ascontiguousarray(a) for a in (wl.q_starts, wl.q_ends, wl.q_contig))
+    tot = C.c_size_t()
+    for order in (0, 1):
+        api.check(lib.searchBatchIntoGpu(idx.h, C.c_void_p(qs.ctypes.data), C.c_void_p(qe.ctypes.data),
+                                         C.c_void_p(qc.ctypes.data), nq, order, 0, h_off, h_out, P, C.byref(tot)))
+        got_off = np.ctypeslib.as_array(C.cast(h_off, C.POINTER(C.c_int64)), shape=(nq + 1,)).copy()
+        got_out = np.ctypeslib.as_array(C.cast(h_out, C.POINTER(C.c_int32)), shape=(P,)).copy()
+        ro, rv = idx.search(wl.q_starts, wl.q_ends, wl.q_contig, order=order)
+        assert np.array_equal(got_off, ro) and np.array_equal(got_out, rv)
+    lib.hostFreePinnedGpu(h_off)
+    lib.hostFreePinnedGpu(h_out)
+    idx.close()
