@@ -130,6 +130,8 @@ __device__ __forceinline__ unsigned above_mask(int lane) {
 template <typename S>
 struct TileArgs {
     Pyr<S> P;
+    Pyr<S> PL;               // pyramid over the ends of intervals >= long_split long
+    int64_t long_split;
     const S* starts;
     int64_t split_len;
     const int32_t* data;
@@ -346,6 +348,133 @@ __device__ __forceinline__ bool is_long_iv(S start, S end, int64_t X) {
 constexpr int kLnu = 128;        // long candidates ending before the tile's max qs
 constexpr int kMaxBlocks = 8192 / 32 + 1;
 
+// First position p in [a, b] with start[p] >= qs - X (starts ascending; b means none).
+// Warp-cooperative 32-ary search over global memory.  Warp-uniform.
+template <typename S>
+__device__ __forceinline__ int64_t warp_first_near(const S* __restrict__ starts, int64_t a, int64_t b, S qs,
+                                                   int64_t X, int lane) {
+    while (b - a > 32) {
+        const int64_t step = (b - a + 31) >> 5;
+        const int64_t idx = a + lane * step;
+        const unsigned m = __ballot_sync(kFull, idx < b && near_start<S>(starts[idx], qs, X));
+        if (!m) {
+            const int64_t last = min((int64_t)31, (b - 1 - a) / step);  // every valid sample is below
+            a = a + last * step + 1;
+        } else {
+            const int k = __ffs(m) - 1;
+            if (k == 0) return a;
+            const int64_t na = a + (int64_t)(k - 1) * step + 1, nb = a + (int64_t)k * step;
+            a = na;
+            b = nb;
+        }
+    }
+    const int64_t idx = a + lane;
+    const unsigned m = __ballot_sync(kFull, idx < b && near_start<S>(starts[idx], qs, X));
+    return m ? a + __ffs(m) - 1 : b;
+}
+
+// First index of a DESCENDING position list whose position is < key (n when none).
+__device__ __forceinline__ int first_below(const int32_t* __restrict__ pos, int n, int64_t key) {
+    int b0 = 0, b1 = n;
+    while (b0 < b1) {
+        const int mid = (b0 + b1) >> 1;
+        if ((int64_t)pos[mid] >= key) b0 = mid + 1;
+        else b1 = mid;
+    }
+    return b0;
+}
+
+// One long query, one warp.  Hits are the window [plo, u] of intervals starting at or after
+// qs - X (read directly, 32 positions per step) plus, below the window, the tile's shared
+// long candidates (intervals at least X long; shorter ones below the window cannot reach qs).
+template <typename S, bool EMIT>
+__device__ void long_query(const TileArgs<S>& a, S qs, int64_t u, int64_t lo, int32_t id,
+                           const int32_t* __restrict__ cpos, const S* __restrict__ cend, int nc, int64_t h_in,
+                           int64_t out_off, int64_t capq, int lane) {
+    if (u < lo) {
+        if (!EMIT && lane == 0) {
+            a.counts[id] = 0;
+            a.heads[id] = 0;
+        }
+        return;
+    }
+    const int64_t X = a.long_split;
+    const S* __restrict__ ends = a.P.ends;
+    const int64_t plo = warp_first_near<S>(a.starts, lo, u + 1, qs, X, lane);
+    if (!EMIT) {
+        uint32_t cnt = 0;
+        int64_t head = 0;
+        bool open = true;
+        for (int64_t top = u; top >= plo; top -= 32) {
+            const int64_t p = top - lane;
+            const unsigned m = __ballot_sync(kFull, p >= plo && ends[p] >= qs);
+            cnt += __popc(m);
+            if (open) {
+                const int run = (m == kFull) ? 32 : __ffs(~m) - 1;
+                head += run;
+                if (run < 32 && top - run >= plo) open = false;  // a miss inside the window ends it
+            }
+        }
+        // a head run covering the whole window may continue into longer intervals below it
+        for (int64_t top = plo - 1; open && top >= lo; top -= 32) {
+            const int64_t p = top - lane;
+            const unsigned m = __ballot_sync(kFull, p >= lo && ends[p] >= qs);
+            const int run = (m == kFull) ? 32 : __ffs(~m) - 1;
+            head += run;
+            if (run < 32) open = false;
+        }
+        for (int kk = first_below(cpos, nc, plo); kk < nc; kk += 32) {
+            const int tt = kk + lane;
+            cnt += __popc(__ballot_sync(kFull, tt < nc && cend[tt] >= qs));
+        }
+        if (lane == 0) {
+            a.counts[id] = cnt;
+            a.heads[id] = (int32_t)head;
+        }
+        return;
+    }
+    const int64_t h = h_in;
+    if (h > capq) {
+        if (lane == 0) atomicCAS(a.d_err, kDevOk, kDevOverflow);
+        return;
+    }
+    int32_t* dst = a.out + out_off;
+    for (int64_t r = lane; r < h; r += 32) {
+        const int64_t pos = (a.order == kOrderIdxsCpp) ? (u - h + 1 + r) : (u - r);
+        dst[r] = a.values ? a.data[pos] : (int32_t)(pos - lo);
+    }
+    int64_t w = h;
+    const unsigned lt = lanemask_lt();
+    for (int64_t top = u - h; top >= plo; top -= 32) {  // the window below the head run
+        const int64_t p = top - lane;
+        const bool hit = p >= plo && ends[p] >= qs;
+        const unsigned m = __ballot_sync(kFull, hit);
+        const int k = __popc(m);
+        if (w + k > capq) {
+            if (lane == 0) atomicCAS(a.d_err, kDevOk, kDevOverflow);
+            return;
+        }
+        if (hit) dst[w + __popc(m & lt)] = a.values ? a.data[p] : (int32_t)(p - lo);
+        w += k;
+    }
+    const int64_t below = plo < u - h + 1 ? plo : u - h + 1;  // long candidates under both
+    for (int kk = first_below(cpos, nc, below); kk < nc; kk += 32) {
+        const int tt = kk + lane;
+        const bool hit = tt < nc && cend[tt] >= qs;
+        const unsigned m = __ballot_sync(kFull, hit);
+        const int k = __popc(m);
+        if (w + k > capq) {
+            if (lane == 0) atomicCAS(a.d_err, kDevOk, kDevOverflow);
+            return;
+        }
+        if (hit) {
+            const int32_t pos = cpos[tt];
+            dst[w + __popc(m & lt)] = a.values ? a.data[pos] : pos - (int32_t)lo;
+        }
+        w += k;
+    }
+}
+
 template <typename S, bool EMIT>
 __global__ void __launch_bounds__(kThreads, 4) k_tiles(TileArgs<S> a) {
     extern __shared__ __align__(16) unsigned char smem[];
@@ -418,7 +547,8 @@ __global__ void __launch_bounds__(kThreads, 4) k_tiles(TileArgs<S> a) {
             int g = (int)(cw & 0x7fffffffu);
             if (g >= a.G) g = 0;  // reported by the prepare kernel
             const int64_t lo = a.seg[g];
-            bool per_query = is_long;
+            bool per_query = is_long && a.PL.ends == nullptr;
+            const bool long_run = is_long && !per_query;
             int nc = 0, nl = 0, nlnu = 0;
             if (!is_long) {
                 // a tile that is one run can reuse the candidate lists the count pass stored
@@ -556,8 +686,29 @@ __global__ void __launch_bounds__(kThreads, 4) k_tiles(TileArgs<S> a) {
                 }
                 if (per_query) nc = 0;
             }
-            if (per_query) {
-                // per-query walks differ widely in length: warps claim queries one at a time
+            if (long_run) {
+                // long queries share the tile's long-interval candidates (long pyramid)
+                S mn = Lim<S>::hi;
+                for (int i = r0 + tid; i < r1; i += kThreads) mn = q_s[i] < mn ? q_s[i] : mn;
+#pragma unroll
+                for (int d = 16; d > 0; d >>= 1) {
+                    const S o = __shfl_xor_sync(kFull, mn, d);
+                    mn = o < mn ? o : mn;
+                }
+                if (lane == 0) s_red[warp] = mn;
+                __syncthreads();
+                S L = s_red[0];
+#pragma unroll
+                for (int w = 1; w < kWarpsPerCta; ++w) L = s_red[w] < L ? s_red[w] : L;
+                nc = gather_bfs<S>(a.PL, lo, (int64_t)q_u[r1 - 1], L, cap, cpos, cend, lst, cnt, msk, s_wsum,
+                                   &s_n, &s_sum);
+                if (nc < 0) {
+                    per_query = true;
+                    nc = 0;
+                }
+            }
+            if (per_query || long_run) {
+                // per-query work differs widely in length: warps claim queries one at a time
                 if (tid == 0) s_next = r0;
                 __syncthreads();
                 while (true) {
@@ -565,10 +716,15 @@ __global__ void __launch_bounds__(kThreads, 4) k_tiles(TileArgs<S> a) {
                     if (lane == 0) i = atomicAdd(&s_next, 1);
                     i = __shfl_sync(kFull, i, 0);
                     if (i >= r1) break;
-                    walk_query<S, EMIT>(a, q_s[i], (int64_t)q_u[i], lo, q_id[i], lane);
+                    if (per_query)
+                        walk_query<S, EMIT>(a, q_s[i], (int64_t)q_u[i], lo, q_id[i], lane);
+                    else
+                        long_query<S, EMIT>(a, q_s[i], (int64_t)q_u[i], lo, q_id[i], cpos, cend, nc,
+                                            EMIT ? (int64_t)q_h[i] : 0, EMIT ? q_off[i] : 0,
+                                            EMIT ? (int64_t)q_cap[i] : 0, lane);
                 }
             }
-            if (!EMIT && !per_query) {
+            if (!EMIT && !per_query && !long_run) {
                 // count pass: one query per THREAD over the shared-memory lists
                 for (int i = r0 + tid; i < r1; i += kThreads) {
                     const S qs = q_s[i];
@@ -623,7 +779,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_tiles(TileArgs<S> a) {
                     a.heads[q_id[i]] = head;
                 }
             }
-            if (EMIT && !per_query) {
+            if (EMIT && !per_query && !long_run) {
                 // emit, step 1: one query per THREAD finds where its hits lie in the lists
                 for (int i = r0 + tid; i < r1; i += kThreads) {
                     const S qs = q_s[i];
@@ -666,7 +822,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_tiles(TileArgs<S> a) {
                 }
                 __syncthreads();
             }
-            for (int i = r0 + warp; EMIT && !per_query && i < r1; i += kWarpsPerCta) {
+            for (int i = r0 + warp; EMIT && !per_query && !long_run && i < r1; i += kWarpsPerCta) {
                 // emit, step 2: one query per WARP writes its hits, coalesced
                 const S qs = q_s[i];
                 const int64_t u = q_u[i];
@@ -1220,6 +1376,10 @@ static int run_tiles(BatchedWorkspace& ws, MapView<S> m, Levels<S> L, int H, int
     SI_CU(cudaMemsetAsync(ws.counters.p, 0, sizeof(int) * 4, st));
     TileArgs<S> a;
     a.P = make_pyr<S>(m, L, H);
+    a.PL.ends = static_cast<const S*>(ws.long_ends);
+    for (int h = 0; h < kMaxLevels; ++h) a.PL.m[h] = static_cast<const S*>(ws.long_lvl[h]);
+    a.PL.H = H;
+    a.long_split = ws.long_split;
     a.starts = m.starts;
     a.split_len = ws.prm.split_len;
     a.data = m.data;

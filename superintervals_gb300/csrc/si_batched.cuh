@@ -69,7 +69,14 @@ struct BatchedWorkspace {
     bool cache_ok = false;
     int64_t cache_stride = 0;
     int cache_prm_tile = 0, cache_prm_cap = 0;
+    // pyramid over the ends of intervals at least long_split long (long-query tiles)
+    const void* long_ends = nullptr;
+    const void* long_lvl[kMaxLevels] = {nullptr};
+    int64_t long_split = 0;
 };
+
+// Interval length from which an interval enters the long-interval pyramid.
+constexpr int64_t kLongIntervalSplit = 65536;
 
 template <typename S>
 int batched_prepare(BatchedWorkspace& ws, MapView<S> m, Levels<S> L, int H, const int64_t* lvl_sizes,

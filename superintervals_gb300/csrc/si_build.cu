@@ -132,6 +132,19 @@ __global__ void k_level_max(const S* __restrict__ in, int64_t n_out, int64_t n_o
 }
 
 template <typename S>
+__global__ void k_long_ends(const S* __restrict__ starts, const S* __restrict__ ends, int64_t n, int64_t n_pad,
+                            int64_t X, S* __restrict__ out) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_pad) return;
+    S v = Lim<S>::lo;
+    if (i < n) {
+        const S s = starts[i], e = ends[i];
+        if (e >= s && (uint64_t)e - (uint64_t)s >= (uint64_t)X) v = e;
+    }
+    out[i] = v;
+}
+
+template <typename S>
 __global__ void __launch_bounds__(kThreads) k_branch(const S* __restrict__ ends, int64_t n,
                                                      int64_t n_pad, Levels<S> L, int H,
                                                      const int64_t* __restrict__ seg, int G,
@@ -281,6 +294,15 @@ cudaError_t launch_pyramid(const S* ends, const int64_t* sizes, int H, S* const*
 }
 
 template <typename S>
+cudaError_t launch_long_ends(const S* starts, const S* ends, int64_t n, int64_t n_pad, int64_t X, S* out,
+                             cudaStream_t st) {
+    if (n_pad <= 0) return cudaSuccess;
+    k_long_ends<S><<<blocks_for(n_pad), kThreads, 0, st>>>(starts, ends, n, n_pad, X, out);
+    note_launch();
+    return cudaGetLastError();
+}
+
+template <typename S>
 cudaError_t launch_branch(const S* ends, int64_t n, int64_t n_pad, Levels<S> L, int H,
                           const int64_t* seg, int G, int32_t* branch, cudaStream_t st) {
     if (n <= 0) return cudaSuccess;
@@ -300,6 +322,7 @@ cudaError_t launch_branch(const S* ends, int64_t n, int64_t n_pad, Levels<S> L, 
     template cudaError_t launch_copy_pad<S>(const S*, const S*, const int32_t*, int64_t, int64_t, \
                                             S*, S*, int32_t*, uint32_t*, cudaStream_t);          \
     template cudaError_t launch_pyramid<S>(const S*, const int64_t*, int, S* const*, cudaStream_t); \
+    template cudaError_t launch_long_ends<S>(const S*, const S*, int64_t, int64_t, int64_t, S*, cudaStream_t); \
     template cudaError_t launch_branch<S>(const S*, int64_t, int64_t, Levels<S>, int,           \
                                           const int64_t*, int, int32_t*, cudaStream_t);
 SIG_INST(int32_t)

@@ -135,6 +135,8 @@ struct gSuperIntervals {
     int64_t lvl_sizes[sig::kMaxLevels + 1] = {0};
     DevBuf starts, ends, data, branch, seg, perm;
     DevBuf lvl[sig::kMaxLevels];
+    DevBuf ends_long;                  // ends of intervals >= kLongIntervalSplit long, else S_MIN
+    DevBuf lvl_long[sig::kMaxLevels];  // their max pyramid
     int sort_passes = 0;
     bool input_was_sorted = false;
     // query workspace
@@ -256,6 +258,7 @@ int build_impl(gSuperIntervals* si) {
     for (int g = 0; g < G; ++g)
         if (segv[g + 1] < segv[g]) return fail(SI_ERR_INVALID, "contig offsets decrease at %d", g);
     si->built = false;
+    si->bws.long_ends = nullptr;  // set again once the long-interval pyramid exists
     si->n = n;
     si->G = G;
     si->n_pad = sig::round_up(std::max<int64_t>(n, 1), 32);
@@ -326,6 +329,17 @@ int build_impl(gSuperIntervals* si) {
     SI_CK(sig::launch_pyramid<S>(ends, si->lvl_sizes, si->H, lp, st));
     SI_CK(sig::launch_branch<S>(ends, n, n_pad, levels<S>(si), si->H, si->seg.as<int64_t>(), G,
                                 si->branch.as<int32_t>(), st));
+    // long-interval pyramid (long-query tiles of the batched path)
+    SI_TRY(si->ends_long.reserve(sizeof(S) * n_pad));
+    for (int h = 1; h <= si->H; ++h) SI_TRY(si->lvl_long[h - 1].reserve(sizeof(S) * si->lvl_sizes[h]));
+    SI_CK(sig::launch_long_ends<S>(si->starts.as<S>(), ends, n, n_pad, sig::kLongIntervalSplit,
+                                   si->ends_long.as<S>(), st));
+    S* lpl[sig::kMaxLevels];
+    for (int h = 0; h < sig::kMaxLevels; ++h) lpl[h] = si->lvl_long[h].as<S>();
+    SI_CK(sig::launch_pyramid<S>(si->ends_long.as<S>(), si->lvl_sizes, si->H, lpl, st));
+    si->bws.long_ends = si->ends_long.p;
+    for (int h = 0; h < sig::kMaxLevels; ++h) si->bws.long_lvl[h] = si->lvl_long[h].p;
+    si->bws.long_split = sig::kLongIntervalSplit;
     SI_TRY(sig::batched_prepare<S>(si->bws, view<S>(si), levels<S>(si), si->H, si->lvl_sizes,
                                    si->ub_mode, st));
     SI_CK(cudaStreamSynchronize(st));
@@ -492,18 +506,9 @@ int search_host(gSuperIntervals* si, const S* qs, const S* qe, const int32_t* qc
         return fail(SI_ERR_CAPACITY, "output needs %lld values, capacity %zu", (long long)P, cap);
     }
     if (P == 0) return read_dev_err(si);
-    // A pinned (page-locked) result buffer is written by the emit kernel directly over the
-    // host link, so the transfer overlaps the emit instead of following it.
-    {
-        cudaPointerAttributes attr;
-        if (cudaPointerGetAttributes(&attr, h_out) == cudaSuccess && attr.type == cudaMemoryTypeHost &&
-            attr.devicePointer != nullptr) {
-            SI_TRY(run_emit<S>(si, q, 0, d_off, 0, order, values, static_cast<int32_t*>(attr.devicePointer), st));
-            SI_CK(cudaStreamSynchronize(st));
-            return read_dev_err(si);
-        }
-        cudaGetLastError();
-    }
+    // Results are staged in device memory and copied in bulk: the emit writes every query's
+    // list at a scattered place, and such writes over the host link run several times slower
+    // than one large copy.
     // chunked emit against the device output budget
     const int64_t budget = std::max<int64_t>((int64_t)(si->out_budget / sizeof(int32_t)), 1 << 20);
     const int64_t buf = std::min<int64_t>(P, budget);

@@ -124,6 +124,11 @@ int pyramid_levels(int64_t n_pad, int64_t* sizes);
 template <typename S>
 cudaError_t launch_pyramid(const S* ends, const int64_t* sizes, int H, S* const* lvl,
                            cudaStream_t st);
+// ends of intervals at least X long (end - start >= X), S_MIN for the others: the base of
+// the long-interval pyramid used by the batched path's long-query tiles.
+template <typename S>
+cudaError_t launch_long_ends(const S* starts, const S* ends, int64_t n, int64_t n_pad, int64_t X, S* out,
+                             cudaStream_t st);
 template <typename S>
 cudaError_t launch_branch(const S* ends, int64_t n, int64_t n_pad, Levels<S> L, int H,
                           const int64_t* seg, int G, int32_t* branch, cudaStream_t st);
