@@ -500,6 +500,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_tiles(TileArgs<S> a) {
     __shared__ int s_tile, s_n, s_sum, s_nlnu, s_next;
     __shared__ int s_wsum[kWarpsPerCta];
     __shared__ S s_red[kWarpsPerCta], s_red2[kWarpsPerCta];
+    __shared__ int32_t s_red3[kWarpsPerCta];
     __shared__ uint32_t s_bmask[kMaxBlocks];
     __shared__ int32_t s_boff[kMaxBlocks];
     __shared__ int32_t s_lnu_pos[kLnu];
@@ -543,9 +544,10 @@ __global__ void __launch_bounds__(kThreads, 4) k_tiles(TileArgs<S> a) {
                 else hi_i = mid;
             }
             const int r1 = lo_i;
-            const bool is_long = (cw >> 31) != 0;
-            int g = (int)(cw & 0x7fffffffu);
-            if (g >= a.G) g = 0;  // reported by the prepare kernel
+            // class code: g for short queries of contig g, G + g for long ones (query_code)
+            const bool is_long = cw >= (uint32_t)a.G && cw < 2u * (uint32_t)a.G;
+            int g = (int)(is_long ? cw - (uint32_t)a.G : cw);
+            if (g >= a.G) g = 0;  // invalid contigs are reported by the prepare kernel
             const int64_t lo = a.seg[g];
             bool per_query = is_long && a.PL.ends == nullptr;
             const bool long_run = is_long && !per_query;
@@ -593,10 +595,13 @@ __global__ void __launch_bounds__(kThreads, 4) k_tiles(TileArgs<S> a) {
                 }
                 if (!cached) {
                     // L = min qs, Q = max qs over the run; umax = ub of the run's last query
+                    // queries are only roughly ordered inside a run: reduce max ub as well
                     S mn = Lim<S>::hi, mx = Lim<S>::lo;
+                    int32_t um = INT32_MIN;
                     for (int i = r0 + tid; i < r1; i += kThreads) {
                         mn = q_s[i] < mn ? q_s[i] : mn;
                         mx = q_s[i] > mx ? q_s[i] : mx;
+                        um = q_u[i] > um ? q_u[i] : um;
                     }
     #pragma unroll
                     for (int d = 16; d > 0; d >>= 1) {
@@ -604,20 +609,24 @@ __global__ void __launch_bounds__(kThreads, 4) k_tiles(TileArgs<S> a) {
                         mn = o < mn ? o : mn;
                         const S p = __shfl_xor_sync(kFull, mx, d);
                         mx = p > mx ? p : mx;
+                        um = max(um, __shfl_xor_sync(kFull, um, d));
                     }
                     if (lane == 0) {
                         s_red[warp] = mn;
                         s_red2[warp] = mx;
+                        s_red3[warp] = um;
                     }
                     if (tid == 0) s_nlnu = 0;
                     __syncthreads();
                     S L = s_red[0], Q = s_red2[0];
+                    int32_t umx = s_red3[0];
     #pragma unroll
                     for (int w = 1; w < kWarpsPerCta; ++w) {
                         L = s_red[w] < L ? s_red[w] : L;
                         Q = s_red2[w] > Q ? s_red2[w] : Q;
+                        umx = max(umx, s_red3[w]);
                     }
-                    const int64_t umax = q_u[r1 - 1];
+                    const int64_t umax = umx;
                     nc = gather_bfs<S>(a.P, lo, umax, L, cap, cpos, cend, lst, cnt, msk, s_wsum, &s_n, &s_sum);
                     per_query = nc < 0;
                     if (!per_query && nc > 0) {
@@ -689,19 +698,31 @@ __global__ void __launch_bounds__(kThreads, 4) k_tiles(TileArgs<S> a) {
             if (long_run) {
                 // long queries share the tile's long-interval candidates (long pyramid)
                 S mn = Lim<S>::hi;
-                for (int i = r0 + tid; i < r1; i += kThreads) mn = q_s[i] < mn ? q_s[i] : mn;
+                int32_t um = INT32_MIN;
+                for (int i = r0 + tid; i < r1; i += kThreads) {
+                    mn = q_s[i] < mn ? q_s[i] : mn;
+                    um = q_u[i] > um ? q_u[i] : um;
+                }
 #pragma unroll
                 for (int d = 16; d > 0; d >>= 1) {
                     const S o = __shfl_xor_sync(kFull, mn, d);
                     mn = o < mn ? o : mn;
+                    um = max(um, __shfl_xor_sync(kFull, um, d));
                 }
-                if (lane == 0) s_red[warp] = mn;
+                if (lane == 0) {
+                    s_red[warp] = mn;
+                    s_red3[warp] = um;
+                }
                 __syncthreads();
                 S L = s_red[0];
+                int32_t umx = s_red3[0];
 #pragma unroll
-                for (int w = 1; w < kWarpsPerCta; ++w) L = s_red[w] < L ? s_red[w] : L;
-                nc = gather_bfs<S>(a.PL, lo, (int64_t)q_u[r1 - 1], L, cap, cpos, cend, lst, cnt, msk, s_wsum,
-                                   &s_n, &s_sum);
+                for (int w = 1; w < kWarpsPerCta; ++w) {
+                    L = s_red[w] < L ? s_red[w] : L;
+                    umx = max(umx, s_red3[w]);
+                }
+                nc = gather_bfs<S>(a.PL, lo, (int64_t)umx, L, cap, cpos, cend, lst, cnt, msk, s_wsum, &s_n,
+                                   &s_sum);
                 if (nc < 0) {
                     per_query = true;
                     nc = 0;
@@ -914,23 +935,33 @@ __global__ void __launch_bounds__(kThreads, 4) k_tiles(TileArgs<S> a) {
 // ---- query keys: (class|contig, end) -------------------------------------------------
 template <typename S>
 __global__ void k_qkeys(const S* __restrict__ qs, const S* __restrict__ qe, const int32_t* __restrict__ qc,
-                        int64_t nq, int64_t long_len, uint32_t* w0, uint32_t* w1, uint32_t* wc,
+                        int64_t nq, int64_t long_len, int G, uint32_t* w0, uint32_t* w1, uint32_t* wc,
                         uint32_t* __restrict__ pay) {
     const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= nq) return;
     const int32_t g = qc ? qc[q] : 0;
     const bool is_long = ((double)qe[q] - (double)qs[q] + 1.0) > (double)long_len;
+    // The end key drops its lowest byte: tiles need queries grouped by class and contig and
+    // close in position, not exactly ordered, and a constant digit costs no sort pass.
     if constexpr (sizeof(S) == 4) {
-        w0[q] = (uint32_t)qe[q] ^ 0x80000000u;
+        w0[q] = ((uint32_t)qe[q] ^ 0x80000000u) & ~0xffu;
     } else {
         const uint64_t b = (uint64_t)qe[q] ^ 0x8000000000000000ull;
-        w0[q] = (uint32_t)b;
+        w0[q] = (uint32_t)b & ~0xffu;
         w1[q] = (uint32_t)(b >> 32);
     }
-    wc[q] = ((uint32_t)g & 0x7fffffffu) | (is_long ? 0x80000000u : 0u);
+    // class code: short queries of contig g -> g, long ones -> G + g, bad contig ids -> 2G
+    wc[q] = (g < 0 || g >= G) ? 2u * (uint32_t)G : (uint32_t)g + (is_long ? (uint32_t)G : 0u);
     pay[q] = (uint32_t)q;
 }
 
+constexpr int kPrepWindow = 2048;  // starts staged per block by the cooperative search
+
+// Prepare the sorted batch: gather each query's record and find its upper bound.  A block
+// holds 256 consecutive sorted queries; when they share one class/contig code (the usual
+// case) the block searches only its smallest and largest end with the index's accelerator,
+// stages the starts between the two answers in shared memory and resolves every query
+// there.  Otherwise each query searches on its own.
 template <typename S>
 __global__ void __launch_bounds__(kThreads) k_qprep(const uint32_t* __restrict__ pay,
                                                     const uint32_t* __restrict__ wc,
@@ -939,33 +970,82 @@ __global__ void __launch_bounds__(kThreads) k_qprep(const uint32_t* __restrict__
                                                     S* __restrict__ sq_s, int32_t* __restrict__ sq_u,
                                                     uint32_t* __restrict__ sq_c, int32_t* __restrict__ sq_id,
                                                     int* d_err) {
-    extern __shared__ __align__(16) unsigned char smem[];
-    S* tree = reinterpret_cast<S*>(smem);
-    const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    int g0 = -1;
-    if (U.mode == 1 && U.eytz_n > 1) {
-        const int64_t jb = (int64_t)blockIdx.x * blockDim.x;
-        g0 = (int)(wc[jb < nq ? jb : nq - 1] & 0x7fffffffu);
-        if (g0 >= m.G) g0 = 0;
-        for (int i = threadIdx.x; i < U.eytz_n; i += blockDim.x) tree[i] = U.eytz_keys[(int64_t)g0 * U.eytz_n + i];
-        __syncthreads();
+    __shared__ S win[kPrepWindow];
+    __shared__ S s_mn[kWarpsPerCta], s_mx[kWarpsPerCta];
+    __shared__ int64_t s_a, s_b;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int64_t jb = (int64_t)blockIdx.x * kThreads;
+    const int64_t j = jb + tid;
+    const int64_t jl = (jb + kThreads < nq ? jb + kThreads : nq) - 1;  // last query of the block
+    const bool valid = j < nq;
+    uint32_t orig = 0, cw = 0;
+    S v = 0;
+    if (valid) {
+        orig = pay[j];
+        cw = wc[j];
+        v = qe[orig];
     }
-    if (j >= nq) return;
-    const uint32_t orig = pay[j];
-    const uint32_t cw = wc[j];
-    int g = (int)(cw & 0x7fffffffu);
+    const uint32_t cfirst = wc[jb], clast = wc[jl];
+    const bool uniform = cfirst == clast && cfirst < 2u * (uint32_t)m.G;  // sorted: one code
+    int g = (int)(cw >= (uint32_t)m.G ? cw - (uint32_t)m.G : cw);
     bool bad = false;
-    if (g >= m.G) {
+    if (valid && cw >= 2u * (uint32_t)m.G) {
         atomicCAS(d_err, kDevOk, kDevBadContig);
         g = 0;
         bad = true;
     }
+    if (!valid) g = (int)(cfirst >= (uint32_t)m.G ? cfirst - (uint32_t)m.G : cfirst);
+    if (g >= m.G) g = 0;
     const int64_t lo = m.seg[g];
     const int64_t n = m.seg[g + 1] - lo;
     int64_t u = -1;
-    if (!bad && n > 0) {
-        const S* tr = (U.mode == 1) ? ((g == g0) ? tree : U.eytz_keys + (int64_t)g * U.eytz_n) : nullptr;
-        u = ub_search(U, g, m.starts + lo, n, qe[orig], tr);
+    bool done = false;
+    if (uniform) {
+        S mn = valid ? v : Lim<S>::hi, mx = valid ? v : Lim<S>::lo;
+#pragma unroll
+        for (int d = 16; d > 0; d >>= 1) {
+            const S o = __shfl_xor_sync(kFull, mn, d);
+            mn = o < mn ? o : mn;
+            const S p = __shfl_xor_sync(kFull, mx, d);
+            mx = p > mx ? p : mx;
+        }
+        if (lane == 0) {
+            s_mn[warp] = mn;
+            s_mx[warp] = mx;
+        }
+        __syncthreads();
+        if (tid < 2 && n > 0) {
+            S x = tid == 0 ? s_mn[0] : s_mx[0];  // thread 0: smallest end, thread 1: largest
+            for (int w = 1; w < kWarpsPerCta; ++w)
+                x = tid == 0 ? (s_mn[w] < x ? s_mn[w] : x) : (s_mx[w] > x ? s_mx[w] : x);
+            const S* tr = (U.mode == 1) ? U.eytz_keys + (int64_t)g * U.eytz_n : nullptr;
+            const int64_t r = ub_search(U, g, m.starts + lo, n, x, tr);
+            if (tid == 0) s_a = r;
+            else s_b = r;
+        }
+        __syncthreads();
+        if (n > 0) {
+            const int64_t a0 = s_a < 0 ? 0 : s_a, b0 = s_b;
+            if (b0 < a0) {
+                done = true;  // every end of the block precedes the contig's first start
+                u = -1;
+            } else if (b0 - a0 + 1 <= kPrepWindow) {
+                for (int64_t k = a0 + tid; k <= b0; k += kThreads) win[k - a0] = m.starts[lo + k];
+                __syncthreads();
+                if (valid && !bad) u = a0 + ub_range(win, (int64_t)0, b0 - a0, v);
+                done = true;
+            } else if (valid && !bad) {
+                u = ub_range(m.starts + lo, a0, b0, v);  // answer lies between the block's two
+                done = true;
+            }
+        } else {
+            done = true;
+        }
+    }
+    if (!valid) return;
+    if (!done && !bad && n > 0) {
+        const S* tr = (U.mode == 1) ? U.eytz_keys + (int64_t)g * U.eytz_n : nullptr;
+        u = ub_search(U, g, m.starts + lo, n, v, tr);
     }
     sq_s[j] = qs[orig];
     sq_u[j] = (int32_t)(lo + u);
@@ -973,10 +1053,18 @@ __global__ void __launch_bounds__(kThreads) k_qprep(const uint32_t* __restrict__
     sq_id[j] = (int32_t)orig;
 }
 
-// upper bounds in the original query order (plain path with an accelerator, tests)
+// upper bounds in the original query order (plain path with an accelerator, tests).  With
+// one contig and the Eytzinger provider, each block first stages the tree in shared memory.
 template <typename S>
 __global__ void k_ub_plain(const S* __restrict__ qe, const int32_t* __restrict__ qc, int64_t nq,
                            MapView<S> m, UbView<S> U, int32_t* __restrict__ out, int* d_err) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    S* tree = reinterpret_cast<S*>(smem);
+    const bool staged = U.mode == 1 && m.G == 1 && U.eytz_n > 1;
+    if (staged) {
+        for (int i = threadIdx.x; i < U.eytz_n; i += blockDim.x) tree[i] = U.eytz_keys[i];
+        __syncthreads();
+    }
     const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= nq) return;
     int g = qc ? qc[q] : 0;
@@ -986,7 +1074,7 @@ __global__ void k_ub_plain(const S* __restrict__ qe, const int32_t* __restrict__
         return;
     }
     const int64_t lo = m.seg[g], n = m.seg[g + 1] - lo;
-    const S* tr = (U.mode == 1) ? U.eytz_keys + (int64_t)g * U.eytz_n : nullptr;
+    const S* tr = (U.mode == 1) ? (staged ? tree : U.eytz_keys + (int64_t)g * U.eytz_n) : nullptr;
     out[q] = (int32_t)ub_search(U, g, m.starts + lo, n, qe[q], tr);
 }
 
@@ -1343,7 +1431,7 @@ int batched_prepare_queries(BatchedWorkspace& ws, MapView<S> m, const QueryBatch
     SI_OKR(ws.sq_id.reserve(sizeof(int32_t) * nq));
     uint32_t* wc = kp[K - 1];
     k_qkeys<S><<<nblk(nq), kThreads, 0, st>>>(static_cast<const S*>(q.qs), static_cast<const S*>(q.qe), q.qc, nq,
-                                              ws.prm.long_len, kp[0], K == 3 ? kp[1] : nullptr, wc,
+                                              ws.prm.long_len, m.G, kp[0], K == 3 ? kp[1] : nullptr, wc,
                                               ws.pay.as<uint32_t>());
     note_launch();
     SI_CU(cudaGetLastError());
@@ -1354,8 +1442,7 @@ int batched_prepare_queries(BatchedWorkspace& ws, MapView<S> m, const QueryBatch
     const uint32_t* spay = in_alt ? ws.palt.as<uint32_t>() : ws.pay.as<uint32_t>();
     const uint32_t* swc = in_alt ? ka[K - 1] : kp[K - 1];
     UbView<S> U = make_ub<S>(ws, ub_mode);
-    const size_t sm = (U.mode == 1) ? sizeof(S) * (size_t)U.eytz_n : 0;
-    k_qprep<S><<<nblk(nq), kThreads, sm, st>>>(spay, swc, static_cast<const S*>(q.qs), static_cast<const S*>(q.qe),
+    k_qprep<S><<<nblk(nq), kThreads, 0, st>>>(spay, swc, static_cast<const S*>(q.qs), static_cast<const S*>(q.qe),
                                               nq, m, U, ws.sq_s.as<S>(), ws.sq_u.as<int32_t>(),
                                               ws.sq_c.as<uint32_t>(), ws.sq_id.as<int32_t>(), d_err);
     note_launch();
@@ -1465,7 +1552,10 @@ int upper_bounds(BatchedWorkspace& ws, MapView<S> m, const QueryBatch& q, int ub
                  cudaStream_t st) {
     if (q.nq <= 0) return SI_OK;
     UbView<S> U = make_ub<S>(ws, ub_mode);
-    k_ub_plain<S><<<nblk(q.nq), kThreads, 0, st>>>(static_cast<const S*>(q.qe), q.qc, q.nq, m, U, out, d_err);
+    const size_t sm = (U.mode == 1 && m.G == 1 && U.eytz_n > 1) ? sizeof(S) * (size_t)U.eytz_n : 0;
+    if (sm > 48 * 1024)
+        SI_CU(cudaFuncSetAttribute(k_ub_plain<S>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    k_ub_plain<S><<<nblk(q.nq), kThreads, sm, st>>>(static_cast<const S*>(q.qe), q.qc, q.nq, m, U, out, d_err);
     note_launch();
     SI_CU(cudaGetLastError());
     ws.launches += 1;
