@@ -119,6 +119,14 @@ int setBatchedParamsGpu(gSuperIntervals* si, int tile_queries, int tile_candidat
                         int64_t long_query_len, int64_t split_len);
 int getBatchedParamsGpu(const gSuperIntervals* si, int* tile_queries, int* tile_candidates,
                         int64_t* long_query_len, int64_t* split_len);
+/* Autotuner of the batched path: times full searches on the first `sample`
+ * queries of a device-resident batch and keeps the fastest upper-bound provider,
+ * tile size, candidate capacity and length split (coordinate descent from the
+ * current values).  The choice stays set on the handle and is also written to
+ * `report` as a JSON object (may be NULL).  Results never depend on it. */
+int autotuneBatchedGpu(gSuperIntervals* si, const void* d_qs, const void* d_qe,
+                       const int32_t* d_qcontig, size_t nq, size_t sample, char* report,
+                       size_t report_len);
 /* Device bytes one search call may use for its result buffer; larger results
  * are emitted in query chunks against it. */
 int setOutputBudgetGpu(gSuperIntervals* si, size_t bytes);
@@ -196,6 +204,15 @@ int searchIdxsNoAllocGpu(gSuperIntervals* si, const void* d_qs, const void* d_qe
  * SI_UB_BINARY.  Device buffers. */
 int upperBoundDeviceGpu(gSuperIntervals* si, const void* d_qe, const int32_t* d_qcontig, size_t nq,
                         int mode, int32_t* d_out, void* stream);
+
+/* Same result as searchDeviceGpu (values_not_idxs = 0, plain path), replayed from a CUDA
+ * graph: count -> scan -> emit are captured on the first call of a given shape (buffers,
+ * size, order, capacity, stream) and replayed by later calls with that shape -- for
+ * repeated small batches, where launch overhead dominates.  Never writes past `capacity`;
+ * a larger result returns SI_ERR_CAPACITY with *total set. */
+int searchDeviceGraphGpu(gSuperIntervals* si, const void* d_qs, const void* d_qe,
+                         const int32_t* d_qcontig, size_t nq, int order, int64_t* d_offsets,
+                         int32_t* d_values, size_t capacity, size_t* total, void* stream);
 
 /* ---- result helpers: createIndexResult / clearIndexResult /
  *      destroyIndexResult (c_superintervals.h:339-343, 1070-1075) --------- */

@@ -76,6 +76,7 @@ SIGNATURES = {
     "setOutputBudgetGpu": (_I, [_H, _SZ]),
     "setBatchedParamsGpu": (_I, [_H, _I, _I, C.c_int64, C.c_int64]),
     "getBatchedParamsGpu": (_I, [_H, _P, _P, _P, _P]),
+    "autotuneBatchedGpu": (_I, [_H, _P, _P, _P, _SZ, _SZ, C.c_char_p, _SZ]),
     "setProfilingGpu": (_I, [_H, _I]),
     "getPhaseTimesGpu": (_I, [_H, _P, _P]),
     "setDeviceBudgetGpu": (_I, [_SZ]),
@@ -92,6 +93,7 @@ SIGNATURES = {
     "countOverlapsDeviceGpu": (_I, [_H, _P, _P, _P, _SZ, _P, _P]),
     "searchDeviceGpu": (_I, [_H, _P, _P, _P, _SZ, _I, _I, _P, _P, _SZ, C.POINTER(_SZ), _P]),
     "upperBoundDeviceGpu": (_I, [_H, _P, _P, _SZ, _I, _P, _P]),
+    "searchDeviceGraphGpu": (_I, [_H, _P, _P, _P, _SZ, _I, _P, _P, _SZ, C.POINTER(_SZ), _P]),
     "searchIdxsNoAllocGpu": (_I, [_H, _P, _P, _P, _SZ, _I, _P, _P, _SZ, C.POINTER(_SZ), _P]),
     "createCsrResult": (cCsrResult, []),
     "clearCsrResult": (None, [C.POINTER(cCsrResult)]),

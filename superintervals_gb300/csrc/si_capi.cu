@@ -146,6 +146,11 @@ struct gSuperIntervals {
     int path = SI_PATH_AUTO;
     int ub_mode = SI_UB_BINARY;
     size_t out_budget = (size_t)4 << 30;
+    // captured count -> scan -> emit graph and the call it was captured for
+    cudaGraphExec_t gexec = nullptr;
+    const void* gkey[8] = {nullptr};
+    size_t gkey_n[3] = {0, 0, 0};
+    long long g_kernels = 0;  // kernels inside the captured graph
     // phase profiling (count, scan, emit, prepare)
     bool prof = false;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -259,6 +264,10 @@ int build_impl(gSuperIntervals* si) {
         if (segv[g + 1] < segv[g]) return fail(SI_ERR_INVALID, "contig offsets decrease at %d", g);
     si->built = false;
     si->bws.long_ends = nullptr;  // set again once the long-interval pyramid exists
+    if (si->gexec) {              // a captured graph holds the old buffers
+        cudaGraphExecDestroy(si->gexec);
+        si->gexec = nullptr;
+    }
     si->n = n;
     si->G = G;
     si->n_pad = sig::round_up(std::max<int64_t>(n, 1), 32);
@@ -635,6 +644,7 @@ void destroySuperIntervalsGpu(gSuperIntervals* si) {
     cudaStreamSynchronize(si->st);
     if (si->ev0) cudaEventDestroy(si->ev0);
     if (si->ev1) cudaEventDestroy(si->ev1);
+    if (si->gexec) cudaGraphExecDestroy(si->gexec);
     cudaStream_t st = si->st;
     delete si;  // releases device buffers
     cudaStreamDestroy(st);
@@ -1089,3 +1099,214 @@ void note_launch(int n) { g_launches += n; }
 }  // namespace sig
 
 extern "C" long long getLaunchCountGpu(void) { return g_launches.load(); }
+
+// =====================================================================================
+// Autotuner for the batched path: times full searches (count -> scan -> emit) on a sample of
+// the caller's own device-resident queries and keeps the fastest upper-bound provider, tile
+// size, candidate capacity and length split, by coordinate descent from the current values.
+// The chosen values stay set on the handle; `report` receives them as one JSON object.
+// =====================================================================================
+extern "C" int autotuneBatchedGpu(gSuperIntervals* si, const void* d_qs, const void* d_qe, const int32_t* d_qc,
+                                  size_t nq, size_t sample, char* report, size_t report_len) {
+    SI_TRY(check_built(si));
+    SI_TRY(set_dev(si));
+    if (!d_qs || !d_qe || nq == 0) return fail(SI_ERR_INVALID, "autotune needs a non-empty device query batch");
+    const size_t ns = std::min(nq, std::max<size_t>(sample, 4096));
+    cudaStream_t st = si->st;
+    const int saved_path = si->path;
+    si->path = SI_PATH_BATCHED;
+    DevBuf off, out;
+    SI_TRY(off.reserve(sizeof(int64_t) * (ns + 1)));
+    sig::QueryBatch q{d_qs, d_qe, d_qc, (int64_t)ns};
+    size_t P = 0;
+    auto run = [&](int& status) -> double {
+        cudaEvent_t a, b;
+        cudaEventCreate(&a);
+        cudaEventCreate(&b);
+        double best = 1e30;
+        for (int rep = 0; rep < 2; ++rep) {
+            size_t t = 0;
+            cudaEventRecord(a, st);
+            status = si->bits == 64 ? search_device<int64_t>(si, q, SI_ORDER_IDXS_CPP, false, off.as<int64_t>(),
+                                                              out.as<int32_t>(), out.bytes / 4, &t, st)
+                                    : search_device<int32_t>(si, q, SI_ORDER_IDXS_CPP, false, off.as<int64_t>(),
+                                                              out.as<int32_t>(), out.bytes / 4, &t, st);
+            cudaEventRecord(b, st);
+            cudaEventSynchronize(b);
+            float ms = 0;
+            cudaEventElapsedTime(&ms, a, b);
+            if (status != SI_OK) break;
+            best = std::min(best, (double)ms);
+        }
+        cudaEventDestroy(a);
+        cudaEventDestroy(b);
+        return best;
+    };
+    // size the output on the sample
+    {
+        size_t t = 0;
+        int r = si->bits == 64 ? search_device<int64_t>(si, q, SI_ORDER_IDXS_CPP, false, off.as<int64_t>(), nullptr, 0,
+                                                        &t, st)
+                               : search_device<int32_t>(si, q, SI_ORDER_IDXS_CPP, false, off.as<int64_t>(), nullptr, 0,
+                                                        &t, st);
+        if (r != SI_OK && r != SI_ERR_CAPACITY) {
+            si->path = saved_path;
+            return r;
+        }
+        P = t;
+        int rr = out.reserve(sizeof(int32_t) * std::max<size_t>(P, 1));
+        if (rr != SI_OK) {
+            si->path = saved_path;
+            return rr;
+        }
+    }
+    sig::BatchedParams best = si->bws.prm;
+    int best_ub = si->ub_mode;
+    int status = SI_OK;
+    double best_ms = run(status);
+    if (status != SI_OK) {
+        si->path = saved_path;
+        return status;
+    }
+    int trials = 1;
+    auto try_params = [&](const sig::BatchedParams& p, int ub) {
+        const sig::BatchedParams keep = si->bws.prm;
+        const int keep_ub = si->ub_mode;
+        si->bws.prm = p;
+        if (ub != si->ub_mode && setUpperBoundModeGpu(si, ub) != SI_OK) {
+            si->bws.prm = keep;
+            return;
+        }
+        int s = SI_OK;
+        const double ms = run(s);
+        ++trials;
+        if (s == SI_OK && ms < best_ms) {
+            best_ms = ms;
+            best = p;
+            best_ub = ub;
+        } else {
+            si->bws.prm = keep;
+            if (si->ub_mode != keep_ub) setUpperBoundModeGpu(si, keep_ub);
+        }
+    };
+    for (int ub : {SI_UB_BINARY, SI_UB_EYTZINGER, SI_UB_LEARNED})
+        if (ub != best_ub) try_params(best, ub);
+    for (int t : {128, 256, 384, 512})
+        if (t != best.tile_q) {
+            sig::BatchedParams p = best;
+            p.tile_q = t;
+            try_params(p, best_ub);
+        }
+    for (int c : {1024, 2048, 3072})
+        if (c != best.cap) {
+            sig::BatchedParams p = best;
+            p.cap = c;
+            try_params(p, best_ub);
+        }
+    for (int64_t x : {(int64_t)512, (int64_t)2048, (int64_t)8192})
+        if (x != best.split_len) {
+            sig::BatchedParams p = best;
+            p.split_len = x;
+            try_params(p, best_ub);
+        }
+    si->bws.prm = best;
+    if (si->ub_mode != best_ub) SI_TRY(setUpperBoundModeGpu(si, best_ub));
+    si->path = saved_path;
+    if (report && report_len) {
+        snprintf(report, report_len,
+                 "{\"upper_bound\": %d, \"tile_queries\": %d, \"tile_candidates\": %d, \"split_len\": %lld, "
+                 "\"long_query_len\": %lld, \"sample_queries\": %zu, \"sample_ms\": %.4f, \"trials\": %d}",
+                 best_ub, best.tile_q, best.cap, (long long)best.split_len, (long long)best.long_len, ns, best_ms,
+                 trials);
+    }
+    return SI_OK;
+}
+
+// =====================================================================================
+// Graph-replayed search: the plain path's count -> scan -> emit captured once per call
+// shape (buffers, size, order, capacity, stream) as a CUDA graph and replayed afterwards, so
+// that repeated small batches (a serving loop) pay one graph launch instead of several kernel
+// launches.  The emit kernel never writes past `capacity`; a larger result is reported with
+// SI_ERR_CAPACITY and the required size.  The index must not be rebuilt between calls with the
+// same shape (a rebuild drops the captured graph).
+// =====================================================================================
+namespace {
+
+template <typename S>
+int capture_plain(gSuperIntervals* si, const sig::QueryBatch& q, int order, int64_t* d_offsets, int32_t* d_values,
+                  size_t capacity, cudaStream_t st) {
+    cudaGraph_t graph = nullptr;
+    const long long k0 = g_launches.load();
+    SI_CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    cudaError_t e = cudaMemsetAsync(si->w_err.p, 0, sizeof(int), st);
+    if (e == cudaSuccess) e = sig::launch_count_plain<S>(view<S>(si), q, si->w_counts.as<uint32_t>(), si->w_err.as<int>(), st);
+    if (e == cudaSuccess)
+        e = sig::exclusive_scan_u32_to_i64(si->w_counts.as<uint32_t>(), d_offsets, q.nq, si->w_tmp.p, st);
+    if (e == cudaSuccess)
+        e = sig::launch_emit_plain<S>(view<S>(si), q, d_offsets, 0, order, false, d_values, si->w_err.as<int>(), st,
+                                      (int64_t)capacity);
+    cudaError_t e2 = cudaStreamEndCapture(st, &graph);
+    si->g_kernels = g_launches.load() - k0;
+    g_launches -= si->g_kernels;  // counted when the graph runs, not when it is recorded
+    if (e != cudaSuccess || e2 != cudaSuccess) {
+        if (graph) cudaGraphDestroy(graph);
+        cudaGetLastError();
+        return fail(SI_ERR_CUDA, "graph capture failed: %s", cudaGetErrorString(e != cudaSuccess ? e : e2));
+    }
+    if (si->gexec) cudaGraphExecDestroy(si->gexec);
+    si->gexec = nullptr;
+    e = cudaGraphInstantiate(&si->gexec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) {
+        si->gexec = nullptr;
+        return fail(SI_ERR_CUDA, "cudaGraphInstantiate: %s", cudaGetErrorString(e));
+    }
+    return SI_OK;
+}
+
+}  // namespace
+
+extern "C" int searchDeviceGraphGpu(gSuperIntervals* si, const void* d_qs, const void* d_qe, const int32_t* d_qc,
+                                    size_t nq, int order, int64_t* d_offsets, int32_t* d_values, size_t capacity,
+                                    size_t* total, void* stream) {
+    SI_TRY(check_built(si));
+    SI_TRY(set_dev(si));
+    if (order != SI_ORDER_IDXS_CPP && order != SI_ORDER_DESC) return fail(SI_ERR_INVALID, "unknown order");
+    if (!d_offsets || (nq && (!d_qs || !d_qe))) return fail(SI_ERR_INVALID, "null device buffer");
+    cudaStream_t st = stream ? (cudaStream_t)stream : si->st;
+    if (si->n == 0 || nq == 0) {
+        SI_CK(cudaMemsetAsync(d_offsets, 0, sizeof(int64_t) * (nq + 1), st));
+        SI_CK(cudaStreamSynchronize(st));
+        if (total) *total = 0;
+        return SI_OK;
+    }
+    // workspace first: nothing may be allocated while a capture is open
+    SI_TRY(si->w_err.reserve(sizeof(int)));
+    SI_TRY(si->w_counts.reserve(sizeof(uint32_t) * nq));
+    SI_TRY(si->w_tmp.reserve(sig::scan_temp_bytes((int64_t)nq)));
+    const void* key[8] = {d_qs, d_qe, d_qc, d_offsets, d_values, (const void*)st, si->w_counts.p, si->w_tmp.p};
+    const size_t key_n[3] = {nq, capacity, (size_t)order};
+    bool same = si->gexec != nullptr;
+    for (int k = 0; k < 8 && same; ++k) same = key[k] == si->gkey[k];
+    for (int k = 0; k < 3 && same; ++k) same = key_n[k] == si->gkey_n[k];
+    if (!same) {
+        sig::QueryBatch q{d_qs, d_qe, d_qc, (int64_t)nq};
+        const int r = si->bits == 64 ? capture_plain<int64_t>(si, q, order, d_offsets, d_values, capacity, st)
+                                     : capture_plain<int32_t>(si, q, order, d_offsets, d_values, capacity, st);
+        if (r != SI_OK) return r;
+        for (int k = 0; k < 8; ++k) si->gkey[k] = key[k];
+        for (int k = 0; k < 3; ++k) si->gkey_n[k] = key_n[k];
+    }
+    SI_CK(cudaGraphLaunch(si->gexec, st));
+    int64_t P = 0;
+    int e = 0;
+    SI_CK(cudaMemcpyAsync(&P, d_offsets + nq, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+    SI_CK(cudaMemcpyAsync(&e, si->w_err.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+    SI_CK(cudaStreamSynchronize(st));
+    if (total) *total = (size_t)P;
+    if ((size_t)P > capacity) return fail(SI_ERR_CAPACITY, "output needs %lld values, capacity %zu", (long long)P, capacity);
+    if (e == sig::kDevBadContig) return fail(SI_ERR_INVALID, "a query names a contig outside [0, %d)", si->G);
+    if (e != 0) return fail(SI_ERR_CUDA, "device error word %d", e);
+    sig::note_launch((int)si->g_kernels);
+    return SI_OK;
+}

@@ -160,7 +160,8 @@ cudaError_t launch_count_plain(MapView<S> m, QueryBatch q, uint32_t* counts, int
                                cudaStream_t st);
 template <typename S>
 cudaError_t launch_emit_plain(MapView<S> m, QueryBatch q, const int64_t* offsets, int64_t out_base,
-                              int order, bool values, int32_t* out, int* d_err, cudaStream_t st);
+                              int order, bool values, int32_t* out, int* d_err, cudaStream_t st,
+                              int64_t total_cap = INT64_MAX);
 template <typename S>
 cudaError_t launch_any_plain(MapView<S> m, QueryBatch q, uint8_t* out, int* d_err,
                              cudaStream_t st);

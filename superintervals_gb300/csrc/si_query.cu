@@ -88,7 +88,8 @@ __global__ void __launch_bounds__(kThreads) k_emit_plain(MapView<S> m, const S* 
                                                          int64_t nq,
                                                          const int64_t* __restrict__ offsets,
                                                          int64_t out_base, int order, bool values,
-                                                         int32_t* __restrict__ out, int* d_err) {
+                                                         int32_t* __restrict__ out, int* d_err,
+                                                         int64_t total_cap) {
     const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= nq) return;
     int64_t lo, len;
@@ -96,6 +97,10 @@ __global__ void __launch_bounds__(kThreads) k_emit_plain(MapView<S> m, const S* 
     const S s = qs[q];
     const int64_t u = ub_halving(m.starts + lo, len, qe[q]);
     if (u < 0) return;
+    if (offsets[q + 1] - out_base > total_cap) {  // the caller's buffer ends before this query's list
+        atomicCAS(d_err, kDevOk, kDevOverflow);
+        return;
+    }
     int32_t* dst = out + (offsets[q] - out_base);
     const int64_t cap = offsets[q + 1] - offsets[q];
     int64_t w = 0;
@@ -164,11 +169,12 @@ cudaError_t launch_count_plain(MapView<S> m, QueryBatch q, uint32_t* counts, int
 
 template <typename S>
 cudaError_t launch_emit_plain(MapView<S> m, QueryBatch q, const int64_t* offsets, int64_t out_base,
-                              int order, bool values, int32_t* out, int* d_err, cudaStream_t st) {
+                              int order, bool values, int32_t* out, int* d_err, cudaStream_t st,
+                              int64_t total_cap) {
     if (q.nq <= 0) return cudaSuccess;
     k_emit_plain<S><<<blocks_for(q.nq), kThreads, 0, st>>>(
         m, static_cast<const S*>(q.qs), static_cast<const S*>(q.qe), q.qc, q.nq, offsets, out_base,
-        order, values, out, d_err);
+        order, values, out, d_err, total_cap);
     note_launch();
     return cudaGetLastError();
 }
@@ -187,7 +193,7 @@ cudaError_t launch_any_plain(MapView<S> m, QueryBatch q, uint8_t* out, int* d_er
     template cudaError_t launch_count_plain<S>(MapView<S>, QueryBatch, uint32_t*, int*,          \
                                                cudaStream_t);                                   \
     template cudaError_t launch_emit_plain<S>(MapView<S>, QueryBatch, const int64_t*, int64_t,   \
-                                              int, bool, int32_t*, int*, cudaStream_t);          \
+                                              int, bool, int32_t*, int*, cudaStream_t, int64_t); \
     template cudaError_t launch_any_plain<S>(MapView<S>, QueryBatch, uint8_t*, int*, cudaStream_t);
 SIG_QINST(int32_t)
 SIG_QINST(int64_t)

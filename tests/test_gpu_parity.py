@@ -354,3 +354,90 @@ def test_pinned_host_output_matches(api, oracle, path):
     lib.hostFreePinnedGpu(h_off)
     lib.hostFreePinnedGpu(h_out)
     idx.close()
+
+
+class _Dev:
+    """Device copies of a query batch plus result buffers, through the C-ABI helpers."""
+
+    def __init__(self, api, idx, wl):
+        import ctypes as C
+        self.C, self.api, self.lib, self.idx = C, api, idx.lib, idx
+        self.ptrs = []
+        dt = idx.dtype
+        self.nq = wl.nq
+        self.qs = self.put(np.ascontiguousarray(wl.q_starts, dt))
+        self.qe = self.put(np.ascontiguousarray(wl.q_ends, dt))
+        self.qc = None if wl.q_contig is None else self.put(np.ascontiguousarray(wl.q_contig, np.int32))
+        self.off = self.alloc(8 * (self.nq + 1))
+
+    def alloc(self, nbytes):
+        p = self.C.c_void_p()
+        self.api.check(self.lib.deviceMallocGpu(self.C.byref(p), max(int(nbytes), 1)))
+        self.ptrs.append(p)
+        return p
+
+    def put(self, arr):
+        p = self.alloc(arr.nbytes)
+        self.api.check(self.lib.memcpyGpu(p, self.C.c_void_p(arr.ctypes.data), arr.nbytes, self.idx.stream))
+        return p
+
+    def get(self, p, n, dtype):
+        out = np.empty(n, dtype)
+        if n:
+            self.api.check(self.lib.memcpyGpu(self.C.c_void_p(out.ctypes.data), p, out.nbytes, self.idx.stream))
+        self.api.check(self.lib.streamSynchronizeGpu(self.idx.stream))
+        return out
+
+    def close(self):
+        for p in self.ptrs:
+            self.lib.deviceFreeGpu(p)
+
+
+def test_autotuner_keeps_results_exact(api, oracle):
+    import ctypes as C
+    import json
+    from superintervals_gb300 import workloads as W
+    wl = W.config3(n=400_000, nq=120_000)
+    idx = _index(api, wl.starts, wl.ends, wl.data, seg=wl.seg, path="batched")
+    d = _Dev(api, idx, wl)
+    rep = C.create_string_buffer(512)
+    api.check(idx.lib.autotuneBatchedGpu(idx.h, d.qs, d.qe, d.qc, d.nq, 50_000, rep, 512))
+    tuned = json.loads(rep.value.decode())
+    assert tuned["trials"] >= 10 and tuned["upper_bound"] in (0, 1, 2)
+    m = oracle.build(wl.starts, wl.ends, wl.data, seg=wl.seg)
+    off, out = idx.search(wl.q_starts, wl.q_ends, wl.q_contig)
+    ro, rv = oracle.search_batch(m, wl.q_starts, wl.q_ends, wl.q_contig, nthreads=8)
+    assert np.array_equal(off, ro) and np.array_equal(out, rv)
+    d.close()
+    idx.close()
+
+
+def test_graph_replay_matches_and_respects_capacity(api):
+    import ctypes as C
+    from superintervals_gb300 import workloads as W
+    wl = W.config3(n=200_000, nq=30_000)
+    idx = _index(api, wl.starts, wl.ends, wl.data, seg=wl.seg, path="plain")
+    d = _Dev(api, idx, wl)
+    off_ref, out_ref = idx.search(wl.q_starts, wl.q_ends, wl.q_contig)
+    P = int(off_ref[-1])
+    d_out = d.alloc(4 * P)
+    tot = C.c_size_t()
+    launches0 = idx.lib.getLaunchCountGpu()
+    for _ in range(3):   # first call captures, the others replay
+        api.check(idx.lib.searchDeviceGraphGpu(idx.h, d.qs, d.qe, d.qc, d.nq, 0, d.off, d_out, P, C.byref(tot),
+                                               None))
+        assert int(tot.value) == P
+        assert np.array_equal(d.get(d.off, d.nq + 1, np.int64), off_ref)
+        assert np.array_equal(d.get(d_out, P, np.int32), out_ref)
+    assert idx.lib.getLaunchCountGpu() > launches0
+    # too small an output: reported, nothing written past the end
+    small = P // 2
+    guard = d.alloc(4 * (small + 1024))
+    sentinel = np.full(small + 1024, -9, np.int32)
+    api.check(idx.lib.memcpyGpu(guard, C.c_void_p(sentinel.ctypes.data), sentinel.nbytes, idx.stream))
+    st = idx.lib.searchDeviceGraphGpu(idx.h, d.qs, d.qe, d.qc, d.nq, 0, d.off, guard, small, C.byref(tot), None)
+    assert st == 5 and int(tot.value) == P
+    tail = d.get(guard, small + 1024, np.int32)[small:]
+    assert (tail == -9).all()
+    d.close()
+    idx.close()
