@@ -49,6 +49,7 @@ def parse():
     ap.add_argument("--scale", type=float, default=1.0, help="shrink N and Q (tests only)")
     ap.add_argument("--path", default="batched", choices=["batched", "plain", "auto"])
     ap.add_argument("--ub", default="learned", choices=["learned", "eytzinger", "binary"])
+    ap.add_argument("--no-autotune", action="store_true", help="keep the default batched-path tunables")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
@@ -187,6 +188,12 @@ def run_gpu(args, rank, world, dist):
     if st_ not in (_capi.SI_OK, _capi.SI_ERR_CAPACITY):
         _capi.check(st_)
     P = int(total.value)
+    tuned = None
+    if path == _capi.PATH_BATCHED and not args.no_autotune:
+        from superintervals_gb300 import autotune
+        # the requested upper-bound provider stays fixed (the metric compares it with plain)
+        tuned = autotune.tune(idx, d_qs, d_qe, d_qc, nq, sample=min(nq, 2_000_000), use_cache=False,
+                              keep_upper_bound=True)
     d_out = dalloc(4 * max(P, 1))
 
     def step():
@@ -235,7 +242,7 @@ def run_gpu(args, rank, world, dist):
         total_ms = float(t.item())
     ms_per_step = total_ms / args.steps
     res = {"wl": wl, "P": P, "nq": nq, "ms_per_step": ms_per_step, "build_s": build_s,
-           "launches": launches_timed,
+           "launches": launches_timed, "tuned": tuned,
            "clocks": clk.summary(), "s_bytes": s_bytes}
     if args.profile_only:
         return res
@@ -394,7 +401,8 @@ def main():
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "int32" if s == 4 else "int64", "data": "synthetic (seeded)",
-            "config": dict(workload_desc(cfg, wl), path=args.path, upper_bound=args.ub),
+            "config": dict(workload_desc(cfg, wl), path=args.path, upper_bound=args.ub,
+                           autotuned=res.get("tuned")),
             "pairs_per_s": pps, "result_pairs_per_step": P,
             "build_s": res["build_s"], "clocks": res["clocks"]}
     if args.profile_only:

@@ -122,10 +122,12 @@ int getBatchedParamsGpu(const gSuperIntervals* si, int* tile_queries, int* tile_
 /* Autotuner of the batched path: times full searches on the first `sample`
  * queries of a device-resident batch and keeps the fastest upper-bound provider,
  * tile size, candidate capacity and length split (coordinate descent from the
- * current values).  The choice stays set on the handle and is also written to
- * `report` as a JSON object (may be NULL).  Results never depend on it. */
+ * current values).  flags & SI_TUNE_KEEP_UPPER_BOUND keeps the current upper-bound
+ * provider.  The choice stays set on the handle and is also written to `report`
+ * as a JSON object (may be NULL).  Results never depend on it. */
+#define SI_TUNE_KEEP_UPPER_BOUND 1
 int autotuneBatchedGpu(gSuperIntervals* si, const void* d_qs, const void* d_qe,
-                       const int32_t* d_qcontig, size_t nq, size_t sample, char* report,
+                       const int32_t* d_qcontig, size_t nq, size_t sample, int flags, char* report,
                        size_t report_len);
 /* Device bytes one search call may use for its result buffer; larger results
  * are emitted in query chunks against it. */

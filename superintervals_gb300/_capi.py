@@ -25,6 +25,8 @@ SI_ERR_TOO_LARGE = 7
 ORDER_IDXS_CPP = 0
 ORDER_DESC = 1
 
+TUNE_KEEP_UPPER_BOUND = 1
+
 PATH_AUTO = 0
 PATH_PLAIN = 1
 PATH_BATCHED = 2
@@ -76,7 +78,7 @@ SIGNATURES = {
     "setOutputBudgetGpu": (_I, [_H, _SZ]),
     "setBatchedParamsGpu": (_I, [_H, _I, _I, C.c_int64, C.c_int64]),
     "getBatchedParamsGpu": (_I, [_H, _P, _P, _P, _P]),
-    "autotuneBatchedGpu": (_I, [_H, _P, _P, _P, _SZ, _SZ, C.c_char_p, _SZ]),
+    "autotuneBatchedGpu": (_I, [_H, _P, _P, _P, _SZ, _SZ, _I, C.c_char_p, _SZ]),
     "setProfilingGpu": (_I, [_H, _I]),
     "getPhaseTimesGpu": (_I, [_H, _P, _P]),
     "setDeviceBudgetGpu": (_I, [_SZ]),

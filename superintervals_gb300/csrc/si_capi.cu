@@ -1107,7 +1107,7 @@ extern "C" long long getLaunchCountGpu(void) { return g_launches.load(); }
 // The chosen values stay set on the handle; `report` receives them as one JSON object.
 // =====================================================================================
 extern "C" int autotuneBatchedGpu(gSuperIntervals* si, const void* d_qs, const void* d_qe, const int32_t* d_qc,
-                                  size_t nq, size_t sample, char* report, size_t report_len) {
+                                  size_t nq, size_t sample, int flags, char* report, size_t report_len) {
     SI_TRY(check_built(si));
     SI_TRY(set_dev(si));
     if (!d_qs || !d_qe || nq == 0) return fail(SI_ERR_INVALID, "autotune needs a non-empty device query batch");
@@ -1189,8 +1189,9 @@ extern "C" int autotuneBatchedGpu(gSuperIntervals* si, const void* d_qs, const v
             if (si->ub_mode != keep_ub) setUpperBoundModeGpu(si, keep_ub);
         }
     };
-    for (int ub : {SI_UB_BINARY, SI_UB_EYTZINGER, SI_UB_LEARNED})
-        if (ub != best_ub) try_params(best, ub);
+    if (!(flags & SI_TUNE_KEEP_UPPER_BOUND))
+        for (int ub : {SI_UB_BINARY, SI_UB_EYTZINGER, SI_UB_LEARNED})
+            if (ub != best_ub) try_params(best, ub);
     for (int t : {128, 256, 384, 512})
         if (t != best.tile_q) {
             sig::BatchedParams p = best;

@@ -401,7 +401,7 @@ def test_autotuner_keeps_results_exact(api, oracle):
     idx = _index(api, wl.starts, wl.ends, wl.data, seg=wl.seg, path="batched")
     d = _Dev(api, idx, wl)
     rep = C.create_string_buffer(512)
-    api.check(idx.lib.autotuneBatchedGpu(idx.h, d.qs, d.qe, d.qc, d.nq, 50_000, rep, 512))
+    api.check(idx.lib.autotuneBatchedGpu(idx.h, d.qs, d.qe, d.qc, d.nq, 50_000, 0, rep, 512))
     tuned = json.loads(rep.value.decode())
     assert tuned["trials"] >= 10 and tuned["upper_bound"] in (0, 1, 2)
     m = oracle.build(wl.starts, wl.ends, wl.data, seg=wl.seg)
