@@ -9,6 +9,7 @@ reference's published timings use BED files that are not available here).
   python bench.py [--gpus N] [--steps K] [--warmup W] [--config config3]
                   [--path batched|plain] [--ub learned|eytzinger|binary]
   python bench.py --impl reference ...   # the reference algorithm on the host cores
+  python bench.py --config config4       # --op upper_bound: learned vs Eytzinger vs binary
 
 Prints one JSON line.  `value` = queries/s with inputs resident in HBM;
 `e2e` = the same through the C-ABI with pinned host buffers (H2D of the
@@ -35,6 +36,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = ("overlap queries/s + result pairs/s on 1 GB300; % HBM peak; batched+learned vs plain")
+METRIC_UB = "upper-bound queries/s on 1 GB300: learned two-stage index vs binary search, bit-identical"
 PEAK_FALLBACK_GBS = 6800.0
 
 
@@ -49,6 +51,9 @@ def parse():
     ap.add_argument("--scale", type=float, default=1.0, help="shrink N and Q (tests only)")
     ap.add_argument("--path", default="batched", choices=["batched", "plain", "auto"])
     ap.add_argument("--ub", default="learned", choices=["learned", "eytzinger", "binary"])
+    ap.add_argument("--op", default=None, choices=["search_idxs", "upper_bound"],
+                    help="search_idxs (default) or upper_bound (default for config4, whose "
+                         "full-size result, ~2.9e13 pairs, cannot be materialised)")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default batched-path tunables")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
@@ -149,6 +154,16 @@ def measured_peak():
 
 
 # ----------------------------------------------------------------------------- GPU arm
+def max_over_ranks(x: float, dist) -> float:
+    """The slowest rank's time (the whole job ends when it does); x itself at N = 1."""
+    if not dist:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def run_gpu(args, rank, world, dist):
     from superintervals_gb300 import _capi
     from superintervals_gb300.interval_map import GpuIndex
@@ -191,9 +206,9 @@ def run_gpu(args, rank, world, dist):
     tuned = None
     if path == _capi.PATH_BATCHED and not args.no_autotune:
         from superintervals_gb300 import autotune
-        # the requested upper-bound provider stays fixed (the metric compares it with plain)
-        tuned = autotune.tune(idx, d_qs, d_qe, d_qc, nq, sample=min(nq, 2_000_000), use_cache=False,
-                              keep_upper_bound=True)
+        # timed on the whole batch: a prefix of unsorted queries is sparser along the genome and
+        # favours smaller tiles.  The requested upper-bound provider stays fixed.
+        tuned = autotune.tune(idx, d_qs, d_qe, d_qc, nq, sample=0, use_cache=False, keep_upper_bound=True)
     d_out = dalloc(4 * max(P, 1))
 
     def step():
@@ -235,11 +250,7 @@ def run_gpu(args, rank, world, dist):
     with ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) as clk:
         total_ms = timed(args.steps, args.warmup, step, on_start=counted)
     launches_timed = lib.getLaunchCountGpu() - launches["before"]
-    if dist:
-        import torch
-        t = torch.tensor([total_ms], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = max_over_ranks(total_ms, dist)
     ms_per_step = total_ms / args.steps
     res = {"wl": wl, "P": P, "nq": nq, "ms_per_step": ms_per_step, "build_s": build_s,
            "launches": launches_timed, "tuned": tuned,
@@ -297,12 +308,7 @@ def run_gpu(args, rank, world, dist):
         for _ in range(k):
             e2e_step()
         e2e_s = (time.perf_counter() - t0) / k
-        if dist:
-            import torch
-            t = torch.tensor([e2e_s], dtype=torch.float64)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            e2e_s = float(t.item())
-        res["e2e_s"] = e2e_s
+        res["e2e_s"] = max_over_ranks(e2e_s, dist)
         res["h2d_bytes"] = wl.q_starts.nbytes + wl.q_ends.nbytes + (wl.q_contig.nbytes if hq_c else 0)
         res["d2h_bytes"] = 8 * (nq + 1) + 4 * P
         for p in (hq_s, hq_e, hq_c, h_off, h_out):
@@ -313,6 +319,176 @@ def run_gpu(args, rank, world, dist):
             lib.deviceFreeGpu(p)
     idx.close()
     return res
+
+
+# ----------------------------------------------------------------------------- upper bound
+UB_MODES = (("binary", 0), ("eytzinger", 1), ("learned", 2))
+
+
+def run_gpu_ub(args, rank, world, dist):
+    """Upper bound of every query end (upperBoundDeviceGpu) with each provider over the
+    same device-resident batch; every provider's output must equal binary search's."""
+    from superintervals_gb300 import _capi
+    from superintervals_gb300.interval_map import GpuIndex
+    lib = _capi.load()
+    wl = make_workload(args.config, args.scale, rank)
+    s_bytes = wl.dtype.itemsize
+    idx = GpuIndex(64 if s_bytes == 8 else 32, 0)
+    idx.add_arrays(wl.starts, wl.ends, wl.data, seg=wl.seg if len(wl.seg) > 2 else None)
+    t0 = time.perf_counter()
+    idx.build()
+    build_s = time.perf_counter() - t0
+    st = idx.stream
+    nq = wl.nq
+
+    def dalloc(nbytes):
+        p = C.c_void_p()
+        _capi.check(lib.deviceMallocGpu(C.byref(p), max(int(nbytes), 1)))
+        return p
+
+    qe = np.ascontiguousarray(wl.q_ends)
+    qc = None if wl.q_contig is None else np.ascontiguousarray(wl.q_contig)
+    d_qe, d_out = dalloc(qe.nbytes), dalloc(4 * nq)
+    _capi.check(lib.memcpyGpu(d_qe, C.c_void_p(qe.ctypes.data), qe.nbytes, st))
+    d_qc = None
+    if qc is not None:
+        d_qc = dalloc(qc.nbytes)
+        _capi.check(lib.memcpyGpu(d_qc, C.c_void_p(qc.ctypes.data), qc.nbytes, st))
+    ev = [C.c_void_p(), C.c_void_p()]
+    for e in ev:
+        _capi.check(lib.eventCreateGpu(C.byref(e)))
+    host = np.empty(nq, dtype=np.int32)
+    ref = None
+    res = {"wl": wl, "nq": nq, "s_bytes": s_bytes, "build_s": build_s, "modes": {}}
+    for name, mode in UB_MODES:
+        t0 = time.perf_counter()
+        idx.set_upper_bound(mode)          # builds the provider's structure (model / tree)
+        prep_s = time.perf_counter() - t0
+
+        def step():
+            _capi.check(lib.upperBoundDeviceGpu(idx.h, d_qe, d_qc, nq, mode, d_out, st))
+        for _ in range(args.warmup):
+            _capi.check(lib.flushL2Gpu(st))
+            step()
+        _capi.check(lib.streamSynchronizeGpu(st))
+        if dist:
+            dist.barrier()
+        k0 = lib.getLaunchCountGpu()
+        total_ms = 0.0
+        with ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) as clk:
+            for _ in range(args.steps):
+                _capi.check(lib.flushL2Gpu(st))
+                _capi.check(lib.eventRecordGpu(ev[0], st))
+                step()
+                _capi.check(lib.eventRecordGpu(ev[1], st))
+                _capi.check(lib.streamSynchronizeGpu(st))
+                ms = C.c_float()
+                _capi.check(lib.eventElapsedMsGpu(ev[0], ev[1], C.byref(ms)))
+                total_ms += ms.value
+        launches = lib.getLaunchCountGpu() - k0 - args.steps   # minus the L2 flushes
+        total_ms = max_over_ranks(total_ms, dist)
+        _capi.check(lib.memcpyGpu(C.c_void_p(host.ctypes.data), d_out, host.nbytes, st))
+        _capi.check(lib.streamSynchronizeGpu(st))
+        if ref is None:
+            ref = host.copy()
+            same = True
+        else:
+            same = bool(np.array_equal(host, ref))
+        res["modes"][name] = {"ms_per_step": total_ms / args.steps, "prepare_s": prep_s,
+                              "identical_to_binary": same, "launches": launches,
+                              "clocks": clk.summary()}
+    # the oracle's upper bound on a sample (sanity check of the binary result itself)
+    from oracle.oracle import Oracle
+    o = Oracle()
+    m = o.build(wl.starts, wl.ends, wl.data, seg=wl.seg)
+    k = min(nq, 1_000_000)
+    want = o.upper_bound_batch(m, qe[:k], None if qc is None else qc[:k], nthreads=host_threads())
+    res["oracle_sample_ok"] = bool(np.array_equal(ref[:k].astype(np.int64), want))
+    res["oracle_map"] = (o, m)
+    # e2e: H2D of the query ends, the learned upper bound and D2H of the result, all
+    # through the C-ABI from pinned host memory
+    if not args.no_e2e:
+        mode = dict(UB_MODES)[args.ub]
+        idx.set_upper_bound(mode)
+        hp, ho = C.c_void_p(), C.c_void_p()
+        _capi.check(lib.hostMallocPinnedGpu(C.byref(hp), qe.nbytes))
+        _capi.check(lib.hostMallocPinnedGpu(C.byref(ho), 4 * nq))
+        C.memmove(hp, qe.ctypes.data, qe.nbytes)
+
+        def e2e_step():
+            _capi.check(lib.memcpyGpu(d_qe, hp, qe.nbytes, st))
+            _capi.check(lib.upperBoundDeviceGpu(idx.h, d_qe, d_qc, nq, mode, d_out, st))
+            _capi.check(lib.memcpyGpu(ho, d_out, 4 * nq, st))
+            _capi.check(lib.streamSynchronizeGpu(st))
+        for _ in range(max(1, args.warmup)):
+            e2e_step()
+        if dist:
+            dist.barrier()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            e2e_step()
+        res["e2e_s"] = max_over_ranks((time.perf_counter() - t0) / args.steps, dist)
+        res["h2d_bytes"] = qe.nbytes
+        res["d2h_bytes"] = 4 * nq
+        lib.hostFreePinnedGpu(hp)
+        lib.hostFreePinnedGpu(ho)
+    for p in (d_qe, d_qc, d_out):
+        if p:
+            lib.deviceFreeGpu(p)
+    idx.close()
+    return res
+
+
+def cpu_run_ub(o, m, wl, seconds, nthreads):
+    """The reference's upper_bound (oracle port) over a bounded query sample."""
+    qc = wl.q_contig
+    probe = min(wl.nq, 200_000)
+    t0 = time.perf_counter()
+    o.upper_bound_batch(m, wl.q_ends[:probe], None if qc is None else qc[:probe], nthreads=nthreads)
+    dt = max(time.perf_counter() - t0, 1e-6)
+    k = int(min(wl.nq, max(probe, probe * seconds / dt)))
+    t0 = time.perf_counter()
+    o.upper_bound_batch(m, wl.q_ends[:k], None if qc is None else qc[:k], nthreads=nthreads)
+    dt = time.perf_counter() - t0
+    return {"q_per_s": k / dt, "sample_q": k, "seconds": dt}
+
+
+def ub_line(args, res, world):
+    wl, nq, s = res["wl"], res["nq"], res["s_bytes"]
+    modes = res["modes"]
+    main = modes[args.ub]
+    ms = main["ms_per_step"]
+    peak, peak_kind = measured_peak()
+    # algorithmic bytes per query: the query end, the int32 result and one 32-byte sector
+    # of the starts array (the least a verified search reads)
+    algo = nq * (s + 4 + 32)
+    line = {"metric": METRIC_UB, "value": world * nq / (ms / 1e3), "unit": "queries/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "int64" if s == 8 else "int32",
+            "data": "synthetic (seeded)",
+            "config": dict(workload_desc(args.config, wl), op="upper_bound", upper_bound=args.ub),
+            "build_s": res["build_s"], "clocks": main["clocks"],
+            "providers": {k: {"queries_per_s": nq / (v["ms_per_step"] / 1e3), "ms_per_step": v["ms_per_step"],
+                              "prepare_s": v["prepare_s"], "identical_to_binary": v["identical_to_binary"]}
+                          for k, v in modes.items()},
+            "speedup_vs_binary": modes["binary"]["ms_per_step"] / ms,
+            "oracle_sample_identical": res["oracle_sample_ok"],
+            "roofline": {"bound": "hbm", "achieved": algo / (ms / 1e3) / 1e9, "peak": peak, "unit": "GB/s",
+                         "frac": algo / (ms / 1e3) / 1e9 / peak, "traffic": None, "kernel": "k_ub_plain",
+                         "peak_kind": peak_kind, "algorithmic_bytes": algo,
+                         "note": "dependent random probes: latency-bound, not bandwidth-bound"},
+            "gpu_launches": main["launches"]}
+    line["config"]["inputs"] = "index > L2 (starts array alone 0.8 GB); L2 flushed between steps"
+    if "e2e_s" in res:
+        line["e2e"] = {"value": world * nq / res["e2e_s"], "unit": "queries/s",
+                       "h2d_bytes_per_step": res["h2d_bytes"], "d2h_bytes_per_step": res["d2h_bytes"]}
+    if not args.no_cpu:
+        nth = host_threads()
+        o, m = res["oracle_map"]
+        c = cpu_run_ub(o, m, wl, args.cpu_seconds, nth)
+        line["cpu_baseline"] = {"value": c["q_per_s"], "unit": "queries/s", "cores": nth, "kind": "port",
+                                "sample": f"{c['sample_q']} of {nq} queries, upper_bound, {nth} threads"}
+    return line
 
 
 # ----------------------------------------------------------------------------- CPU arm
@@ -360,6 +536,31 @@ def main():
     args = parse()
     rank, world, dist = init_dist(args)
     cfg = args.config
+    op = args.op or ("upper_bound" if cfg == "config4" else "search_idxs")
+    if args.impl == "reference" and op == "upper_bound":
+        if rank != 0:
+            return
+        from oracle.oracle import Oracle
+        wl = make_workload(cfg, args.scale, 0)
+        nth = host_threads()
+        o = Oracle()
+        m = o.build(wl.starts, wl.ends, wl.data, seg=wl.seg)
+        for _ in range(max(0, min(args.warmup, 1))):
+            cpu_run_ub(o, m, wl, min(2.0, args.cpu_seconds / 4), nth)
+        runs = [cpu_run_ub(o, m, wl, args.cpu_seconds / max(1, args.steps), nth) for _ in range(args.steps)]
+        qps = statistics.median(r["q_per_s"] for r in runs)
+        line = {"metric": METRIC_UB, "value": qps, "unit": "queries/s", "impl": "reference", "n_gpus": 1,
+                "steps": args.steps, "warmup": args.warmup,
+                "ms_per_step": 1000.0 * statistics.median(r["seconds"] for r in runs),
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": str(wl.dtype),
+                "data": "synthetic (seeded)",
+                "config": dict(workload_desc(cfg, wl), op="upper_bound", upper_bound="binary (reference)"),
+                "cpu_baseline": {"value": qps, "unit": "queries/s", "cores": nth, "kind": "port",
+                                 "sample": f"{runs[0]['sample_q']} of {wl.nq} queries per step, "
+                                           f"upper_bound, {nth} threads"},
+                "e2e": {"value": qps, "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+        return
     if args.impl == "reference":
         if rank != 0:
             return
@@ -388,6 +589,11 @@ def main():
         print(json.dumps(line), flush=True)
         return
 
+    if op == "upper_bound":
+        res = run_gpu_ub(args, rank, world, dist)
+        if rank == 0:
+            print(json.dumps(ub_line(args, res, world)), flush=True)
+        return
     res = run_gpu(args, rank, world, dist)
     if rank != 0:
         return

@@ -120,7 +120,10 @@ int setBatchedParamsGpu(gSuperIntervals* si, int tile_queries, int tile_candidat
 int getBatchedParamsGpu(const gSuperIntervals* si, int* tile_queries, int* tile_candidates,
                         int64_t* long_query_len, int64_t* split_len);
 /* Autotuner of the batched path: times full searches on the first `sample`
- * queries of a device-resident batch and keeps the fastest upper-bound provider,
+ * queries of a device-resident batch (sample = 0 or >= nq: the whole batch; a
+ * prefix of an unsorted batch is sparser along the genome than the batch, so it
+ * stands for the batch's tile shapes only when it keeps the batch's density)
+ * and keeps the fastest upper-bound provider,
  * tile size, candidate capacity and length split (coordinate descent from the
  * current values).  flags & SI_TUNE_KEEP_UPPER_BOUND keeps the current upper-bound
  * provider.  The choice stays set on the handle and is also written to `report`

@@ -68,6 +68,9 @@ class Oracle:
             f = getattr(self.lib, f"sio_search_batch_{sfx}")
             f.restype = None
             f.argtypes = [_P, _P, _P, _P, _P, _I64, _P, _P, _P, C.c_int, _P, _P, C.c_int]
+            f = getattr(self.lib, f"sio_upper_bound_batch_{sfx}")
+            f.restype = None
+            f.argtypes = [_P, _P, _I64, _P, _P, _P, C.c_int]
             f = getattr(self.lib, f"sio_coverage_{sfx}")
             f.restype = None
             f.argtypes = [_I64, _P, _P, _P, C.c_int64 if sfx == "i64" else C.c_int32,
@@ -125,6 +128,16 @@ class Oracle:
             _ptr(m["data"]) if values else None, qs.shape[0], _ptr(qc), _ptr(qs), _ptr(qe),
             order, _ptr(off), _ptr(out), nthreads)
         return off, out
+
+    def upper_bound_batch(self, m, qe, qc=None, nthreads=1):
+        """upper_bound (hpp:501-516) of every query end within its contig's map:
+        contig-local index of the last start <= qe, or -1."""
+        qe = np.ascontiguousarray(qe, dtype=m["starts"].dtype)
+        qc = None if qc is None else np.ascontiguousarray(qc, dtype=np.int32)
+        out = np.empty(qe.shape[0], dtype=np.int64)
+        getattr(self.lib, f"sio_upper_bound_batch_{self._sfx(qe.dtype)}")(
+            _ptr(m["seg"]), _ptr(m["starts"]), qe.shape[0], _ptr(qc), _ptr(qe), _ptr(out), nthreads)
+        return out
 
     def has_overlaps_batch(self, m, qs, qe):
         """has_overlaps (hpp:865-871): true iff the interval at upper_bound(qe)

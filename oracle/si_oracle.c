@@ -271,6 +271,15 @@ typedef struct {                                                                
     uint32_t* counts; const int64_t* offsets; int32_t* out32; int64_t* scratch;         \
 } sio_batch_ctx_##SFX;                                                                  \
                                                                                         \
+static void sio_ub_worker_##SFX(void* p, int64_t b, int64_t e) {                        \
+    sio_batch_ctx_##SFX* c = (sio_batch_ctx_##SFX*)p;                                   \
+    for (int64_t q = b; q < e; ++q) {                                                   \
+        int32_t g = c->qc ? c->qc[q] : 0;                                               \
+        int64_t lo = c->seg[g], n = c->seg[g + 1] - lo;                                 \
+        c->scratch[q] = sio_upper_bound_##SFX(n, c->starts + lo, c->qe[q]);            \
+    }                                                                                   \
+}                                                                                       \
+                                                                                        \
 static void sio_count_worker_##SFX(void* p, int64_t b, int64_t e) {                     \
     sio_batch_ctx_##SFX* c = (sio_batch_ctx_##SFX*)p;                                   \
     for (int64_t q = b; q < e; ++q) {                                                   \
@@ -306,6 +315,16 @@ void sio_count_batch_##SFX(const int64_t* seg, const S* starts, const S* ends,  
     c.seg = seg; c.starts = starts; c.ends = ends; c.branch = branch;                   \
     c.qc = qc; c.qs = qs; c.qe = qe; c.counts = counts;                                 \
     sio_parallel_for(nq, nthreads, sio_count_worker_##SFX, &c);                         \
+}                                                                                       \
+                                                                                        \
+/* upper_bound of every query end in its contig's map (hpp:501-516), -1 when none. */ \
+void sio_upper_bound_batch_##SFX(const int64_t* seg, const S* starts, int64_t nq,       \
+                                 const int32_t* qc, const S* qe, int64_t* out,          \
+                                 int nthreads) {                                        \
+    sio_batch_ctx_##SFX c;                                                              \
+    memset(&c, 0, sizeof(c));                                                           \
+    c.seg = seg; c.starts = starts; c.qc = qc; c.qe = qe; c.scratch = out;              \
+    sio_parallel_for(nq, nthreads, sio_ub_worker_##SFX, &c);                            \
 }                                                                                       \
                                                                                         \
 void sio_search_batch_##SFX(const int64_t* seg, const S* starts, const S* ends,         \

@@ -44,10 +44,11 @@ def apply(index, choice: dict):
     index.set_upper_bound(int(choice["upper_bound"]))
 
 
-def tune(index, d_qs, d_qe, d_qc, nq: int, sample: int = 2_000_000, cache_path: str = DEFAULT_CACHE,
+def tune(index, d_qs, d_qe, d_qc, nq: int, sample: int = 0, cache_path: str = DEFAULT_CACHE,
          use_cache: bool = True, keep_upper_bound: bool = False) -> dict:
     """Tune `index` (a GpuIndex) for a device-resident batch; returns the choice
-    (plus "cached": True/False).  keep_upper_bound fixes the current provider."""
+    (plus "cached": True/False).  sample = 0 times the whole batch; keep_upper_bound fixes
+    the current provider."""
     key = cache_key(index, nq) + ("|ub-fixed" if keep_upper_bound else "")
     cache = {}
     if use_cache and os.path.isfile(cache_path):

@@ -1111,7 +1111,7 @@ extern "C" int autotuneBatchedGpu(gSuperIntervals* si, const void* d_qs, const v
     SI_TRY(check_built(si));
     SI_TRY(set_dev(si));
     if (!d_qs || !d_qe || nq == 0) return fail(SI_ERR_INVALID, "autotune needs a non-empty device query batch");
-    const size_t ns = std::min(nq, std::max<size_t>(sample, 4096));
+    const size_t ns = sample == 0 ? nq : std::min(nq, std::max<size_t>(sample, 4096));
     cudaStream_t st = si->st;
     const int saved_path = si->path;
     si->path = SI_PATH_BATCHED;

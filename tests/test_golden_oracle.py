@@ -108,3 +108,19 @@ def test_planted_mistake_is_caught(oracle):
     off, out = oracle.search_batch(bad, g["q_starts"], g["q_ends"])
     assert not (np.array_equal(off, g["ref_search_idxs_off"]) and
                 np.array_equal(out, g["ref_search_idxs"]))
+
+
+@pytest.mark.parametrize("name", ["nested_dups_int32", "edges_int64", "config1_plain_small_int32"])
+def test_oracle_upper_bound_batch(oracle, name):
+    """upper_bound (hpp:501-516): the last start <= qe, -1 before the first start."""
+    if name not in fixture_names():
+        pytest.skip(f"no fixture {name}")
+    g = load(name)
+    m = oracle.build(g["starts"], g["ends"], g["data"])
+    st = m["starts"]
+    lim = np.iinfo(st.dtype)
+    extra = list(st[:3]) + [v + 1 for v in st[-3:] if v < lim.max] + ([st[0] - 1] if st[0] > lim.min else [])
+    qe = np.concatenate([g["q_ends"], np.array(extra, dtype=st.dtype)])
+    got = oracle.upper_bound_batch(m, qe, nthreads=3)
+    want = np.searchsorted(m["starts"], qe.astype(m["starts"].dtype), side="right") - 1
+    assert np.array_equal(got, want)
