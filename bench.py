@@ -385,7 +385,7 @@ def run_gpu_ub(args, rank, world, dist):
                 ms = C.c_float()
                 _capi.check(lib.eventElapsedMsGpu(ev[0], ev[1], C.byref(ms)))
                 total_ms += ms.value
-        launches = lib.getLaunchCountGpu() - k0 - args.steps   # minus the L2 flushes
+        launches = lib.getLaunchCountGpu() - k0   # the L2 flush is a memset, not counted
         total_ms = max_over_ranks(total_ms, dist)
         _capi.check(lib.memcpyGpu(C.c_void_p(host.ctypes.data), d_out, host.nbytes, st))
         _capi.check(lib.streamSynchronizeGpu(st))
