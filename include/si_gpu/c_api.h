@@ -219,6 +219,36 @@ int searchDeviceGraphGpu(gSuperIntervals* si, const void* d_qs, const void* d_qe
                          const int32_t* d_qcontig, size_t nq, int order, int64_t* d_offsets,
                          int32_t* d_values, size_t capacity, size_t* total, void* stream);
 
+/* ---- set operations: intersection / difference of a list of intervals
+ *      (the other map A, passed as queries, one per interval of A in the
+ *      order A iterates them) against this handle (map B, built).  CSR over the
+ *      queries: query i's pieces are [offsets[i], offsets[i+1]).  Coordinates
+ *      have the handle's width.  With too small a capacity the call returns
+ *      SI_ERR_CAPACITY, sets *total and (host forms) fills offsets. -------- */
+/* intersection (c_superintervals.h:286, 921-940; superintervals.hpp:1158-1177
+ * IntervalMap::intersection): for each hit h of query i in `order`
+ * (SI_ORDER_IDXS_CPP = the C++ class, SI_ORDER_DESC = the C API), the piece
+ * [max(qs, starts[h]), min(qe, ends[h])], kept when start <= end; hits[]
+ * receives h (contig-local position in the built index) so that the caller
+ * applies its combine function (the reference's default keeps A's data). */
+int intersectBatchGpu(gSuperIntervals* si, const void* qs, const void* qe, const int32_t* qcontig,
+                      size_t nq, int order, int64_t* offsets, void* starts, void* ends, int32_t* hits,
+                      size_t capacity, size_t* total);
+int intersectDeviceGpu(gSuperIntervals* si, const void* d_qs, const void* d_qe,
+                       const int32_t* d_qcontig, size_t nq, int order, int64_t* d_offsets,
+                       void* d_starts, void* d_ends, int32_t* d_hits, size_t capacity, size_t* total,
+                       void* stream);
+/* difference (c_superintervals.h:292, 950-974; superintervals.hpp:1186-1211):
+ * the pieces of each query interval not covered by this map, ascending; each
+ * inherits the query's data.  A covered piece reaching the coordinate type's
+ * maximum ends the sweep (the reference's end + 1 overflows there). */
+int differenceBatchGpu(gSuperIntervals* si, const void* qs, const void* qe, const int32_t* qcontig,
+                       size_t nq, int64_t* offsets, void* starts, void* ends, size_t capacity,
+                       size_t* total);
+int differenceDeviceGpu(gSuperIntervals* si, const void* d_qs, const void* d_qe,
+                        const int32_t* d_qcontig, size_t nq, int64_t* d_offsets, void* d_starts,
+                        void* d_ends, size_t capacity, size_t* total, void* stream);
+
 /* ---- result helpers: createIndexResult / clearIndexResult /
  *      destroyIndexResult (c_superintervals.h:339-343, 1070-1075) --------- */
 cCsrResult createCsrResult(void);

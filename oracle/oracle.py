@@ -68,6 +68,12 @@ class Oracle:
             f = getattr(self.lib, f"sio_search_batch_{sfx}")
             f.restype = None
             f.argtypes = [_P, _P, _P, _P, _P, _I64, _P, _P, _P, C.c_int, _P, _P, C.c_int]
+            f = getattr(self.lib, f"sio_intersection_{sfx}")
+            f.restype = _I64
+            f.argtypes = [_I64, _P, _P, _P, _I64, _P, _P, C.c_int, _P, _P, _P, _P, _I64]
+            f = getattr(self.lib, f"sio_difference_{sfx}")
+            f.restype = _I64
+            f.argtypes = [_I64, _P, _P, _P, _I64, _P, _P, _P, _P, _P, _I64]
             f = getattr(self.lib, f"sio_upper_bound_batch_{sfx}")
             f.restype = None
             f.argtypes = [_P, _P, _I64, _P, _P, _P, C.c_int]
@@ -129,6 +135,36 @@ class Oracle:
             order, _ptr(off), _ptr(out), nthreads)
         return off, out
 
+    def intersection(self, m, a_s, a_e, order=ORDER_IDXS_CPP):
+        """intersection (hpp:1158-1177): CSR over the A intervals of pieces
+        (start, end, b position), single-contig map m."""
+        st = m["starts"]
+        a_s = np.ascontiguousarray(a_s, dtype=st.dtype)
+        a_e = np.ascontiguousarray(a_e, dtype=st.dtype)
+        f = getattr(self.lib, f"sio_intersection_{self._sfx(st.dtype)}")
+        off = np.zeros(a_s.shape[0] + 1, np.int64)
+        args = (st.shape[0], _ptr(st), _ptr(m["ends"]), _ptr(m["branch"]), a_s.shape[0], _ptr(a_s), _ptr(a_e),
+                order, _ptr(off))
+        tot = f(*args, None, None, None, 0)
+        os_, oe_, ob = np.empty(tot, st.dtype), np.empty(tot, st.dtype), np.empty(tot, np.int64)
+        f(*args, _ptr(os_), _ptr(oe_), _ptr(ob), tot)
+        return off, os_, oe_, ob
+
+    def difference(self, m, a_s, a_e):
+        """difference (hpp:1186-1211): CSR over the A intervals of uncovered
+        pieces (start, end), single-contig map m."""
+        st = m["starts"]
+        a_s = np.ascontiguousarray(a_s, dtype=st.dtype)
+        a_e = np.ascontiguousarray(a_e, dtype=st.dtype)
+        f = getattr(self.lib, f"sio_difference_{self._sfx(st.dtype)}")
+        off = np.zeros(a_s.shape[0] + 1, np.int64)
+        args = (st.shape[0], _ptr(st), _ptr(m["ends"]), _ptr(m["branch"]), a_s.shape[0], _ptr(a_s), _ptr(a_e),
+                _ptr(off))
+        tot = f(*args, None, None, 0)
+        os_, oe_ = np.empty(tot, st.dtype), np.empty(tot, st.dtype)
+        f(*args, _ptr(os_), _ptr(oe_), tot)
+        return off, os_, oe_
+
     def upper_bound_batch(self, m, qe, qc=None, nthreads=1):
         """upper_bound (hpp:501-516) of every query end within its contig's map:
         contig-local index of the last start <= qe, or -1."""
@@ -187,6 +223,10 @@ class Reference:
             getattr(self.lib, f"ref_map_{sfx}_search").restype = _I64
             getattr(self.lib, f"ref_map_{sfx}_search").argtypes = [_P, C.c_int, _I64, _P, _P, _P, _P, _I64]
             getattr(self.lib, f"ref_map_{sfx}_coverage").argtypes = [_P, _I64, _P, _P, _P, _P]
+            getattr(self.lib, f"ref_map_{sfx}_setop").restype = _I64
+            getattr(self.lib, f"ref_map_{sfx}_setop").argtypes = [_P, _P, C.c_int, _P, _P, _P, _I64]
+        self.lib.ref_c_setop.restype = _I64
+        self.lib.ref_c_setop.argtypes = [_P, _P, C.c_int, _P, _P, _P, _I64]
         self.lib.ref_c_new.restype = _P
         self.lib.ref_c_new.argtypes = [_I64, _P, _P, _P]
         self.lib.ref_c_free.argtypes = [_P]
@@ -197,6 +237,46 @@ class Reference:
     @staticmethod
     def _sfx(dtype):
         return "i64" if np.dtype(dtype) == np.int64 else "i32"
+
+    def setops(self, a, b):
+        """a.intersection(b) (keeping a's and, separately, b's data) and
+        a.difference(b) through the reference's C++ class, and intersection /
+        difference through its C API (int32 only).  a and b are (starts, ends,
+        data) triples; A's arrays after its build() (the order the reference
+        iterates) are returned too."""
+        L = self.lib
+        dt = np.asarray(a[0]).dtype
+        sfx = self._sfx(dt)
+        arr = [tuple(np.ascontiguousarray(x, dtype=t) for x, t in zip(m, (dt, dt, np.int32))) for m in (a, b)]
+        res = {}
+        hs = [getattr(L, f"ref_map_{sfx}_new")(m[0].shape[0], _ptr(m[0]), _ptr(m[1]), _ptr(m[2])) for m in arr]
+        try:
+            na = arr[0][0].shape[0]
+            so, eo, do = np.empty(na, dt), np.empty(na, dt), np.empty(na, np.int32)
+            if na:
+                getattr(L, f"ref_map_{sfx}_arrays")(hs[0], _ptr(so), _ptr(eo), _ptr(do), None)
+            res.update(a_sorted_starts=so, a_sorted_ends=eo, a_sorted_data=do)
+            for op, key in ((0, "isect"), (1, "isect_bdata"), (2, "diff")):
+                f = getattr(L, f"ref_map_{sfx}_setop")
+                k = f(hs[0], hs[1], op, None, None, None, 0)
+                os_, oe_, od = np.empty(k, dt), np.empty(k, dt), np.empty(k, np.int32)
+                f(hs[0], hs[1], op, _ptr(os_), _ptr(oe_), _ptr(od), k)
+                res.update({key + "_starts": os_, key + "_ends": oe_, key + "_data": od})
+        finally:
+            for h in hs:
+                getattr(L, f"ref_map_{sfx}_free")(h)
+        if sfx == "i32":
+            hc = [L.ref_c_new(m[0].shape[0], _ptr(m[0]), _ptr(m[1]), _ptr(m[2])) for m in arr]
+            try:
+                for op, key in ((0, "c_isect"), (2, "c_diff")):
+                    k = L.ref_c_setop(hc[0], hc[1], op, None, None, None, 0)
+                    os_, oe_, od = np.empty(k, dt), np.empty(k, dt), np.empty(k, np.int32)
+                    L.ref_c_setop(hc[0], hc[1], op, _ptr(os_), _ptr(oe_), _ptr(od), k)
+                    res.update({key + "_starts": os_, key + "_ends": oe_, key + "_data": od})
+            finally:
+                for h in hc:
+                    L.ref_c_free(h)
+        return res
 
     def run(self, starts, ends, data, qs, qe):
         """Everything the fixtures need for one single-contig case."""

@@ -95,9 +95,33 @@ void map_coverage(void* hp, int64_t nq, const S* qs, const S* qe, int64_t* cnt, 
     }
 }
 
+// Set operations of map a against map b (hpp:1158-1211).  op 0: a.intersection(b) keeping a's
+// data, op 1: a.intersection(b) keeping b's data, op 2: a.difference(b).  The result map is not
+// built, so its arrays are in the order the reference adds pieces.  Returns the piece count;
+// writes at most cap pieces.
+template <typename S>
+int64_t map_setop(void* ap, void* bp, int op, S* os, S* oe, int32_t* od, int64_t cap) {
+    auto* a = static_cast<RefMap<S>*>(ap);
+    auto* b = static_cast<RefMap<S>*>(bp);
+    si::IntervalMap<S, int32_t> r;
+    if (op == 0) r = a->m.intersection(b->m);
+    else if (op == 1) r = a->m.intersection(b->m, [](const int32_t&, const int32_t& y) { return y; });
+    else r = a->m.difference(b->m);
+    const int64_t k = (int64_t)r.starts.size();
+    for (int64_t i = 0; i < k && i < cap; ++i) {
+        os[i] = r.starts[i];
+        oe[i] = r.ends[i];
+        od[i] = r.data[i];
+    }
+    return k;
+}
+
 }  // namespace
 
 extern "C" {
+
+int64_t ref_map_i32_setop(void* a, void* b, int op, int32_t* os, int32_t* oe, int32_t* od, int64_t cap) { return map_setop<int32_t>(a, b, op, os, oe, od, cap); }
+int64_t ref_map_i64_setop(void* a, void* b, int op, int64_t* os, int64_t* oe, int32_t* od, int64_t cap) { return map_setop<int64_t>(a, b, op, os, oe, od, cap); }
 
 void* ref_map_i32_new(int64_t n, const int32_t* s, const int32_t* e, const int32_t* d) { return map_new<int32_t>(n, s, e, d); }
 void* ref_map_i64_new(int64_t n, const int64_t* s, const int64_t* e, const int32_t* d) { return map_new<int64_t>(n, s, e, d); }

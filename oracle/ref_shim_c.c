@@ -18,6 +18,21 @@ void* ref_c_new(int64_t n, const int32_t* s, const int32_t* e, const int32_t* d)
 
 void ref_c_free(void* h) { destroySuperIntervals((cSuperIntervals*)h); }
 
+/* op 0: intersection(a, b, NULL) (keeps a's data), op 2: difference(a, b)
+ * (c_superintervals.h:921-974).  Returns the piece count; writes at most cap. */
+int64_t ref_c_setop(void* a, void* b, int op, int32_t* os, int32_t* oe, int32_t* od, int64_t cap) {
+    cSuperIntervals* r = op == 0 ? intersection((cSuperIntervals*)a, (cSuperIntervals*)b, NULL)
+                                 : difference((cSuperIntervals*)a, (cSuperIntervals*)b);
+    int64_t k = (int64_t)r->size;
+    for (int64_t i = 0; i < k && i < cap; ++i) {
+        os[i] = r->starts[i];
+        oe[i] = r->ends[i];
+        od[i] = r->data[i];
+    }
+    destroySuperIntervals(r);
+    return k;
+}
+
 void ref_c_arrays(void* h, int32_t* s, int32_t* e, int32_t* d, int64_t* br) {
     cSuperIntervals* si = (cSuperIntervals*)h;
     for (size_t i = 0; i < si->size; ++i) {

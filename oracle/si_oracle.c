@@ -239,6 +239,91 @@ int64_t sio_search_##SFX(int64_t n, const S* starts, const S* ends,             
     return w;                                                                           \
 }                                                                                       \
                                                                                         \
+/* ---- set operations of a list of intervals (map A) against this map (B) ----- */     \
+typedef struct { S s, e; } sio_key_##SFX;                                               \
+static int sio_keycmp_##SFX(const void* x, const void* y) {                             \
+    const sio_key_##SFX* a = (const sio_key_##SFX*)x;                                   \
+    const sio_key_##SFX* b = (const sio_key_##SFX*)y;                                   \
+    if (a->s != b->s) return a->s < b->s ? -1 : 1;                                      \
+    return (a->e > b->e) - (a->e < b->e);                                               \
+}                                                                                       \
+                                                                                        \
+/* intersection (hpp:1158-1177, c:921-940): for each A interval k, in order, one */     \
+/* piece [max(as, starts[h]), min(ae, ends[h])] per hit h of search (order), kept */    \
+/* when start <= end.  ob receives h.  Returns the piece count (writes <= cap).   */     \
+int64_t sio_intersection_##SFX(int64_t n, const S* starts, const S* ends,              \
+                               const int64_t* branch, int64_t na, const S* as,          \
+                               const S* ae, int order, int64_t* off, S* os, S* oe,      \
+                               int64_t* ob, int64_t cap) {                              \
+    int64_t total = 0, bcap = 0;                                                        \
+    int64_t* buf = NULL;                                                                \
+    if (off) off[0] = 0;                                                                \
+    for (int64_t k = 0; k < na; ++k) {                                                  \
+        int64_t c = sio_count_##SFX(n, starts, ends, branch, as[k], ae[k]);            \
+        if (c > bcap) { bcap = 2 * c; buf = (int64_t*)realloc(buf, 8 * (size_t)bcap); } \
+        int64_t w = c ? sio_search_##SFX(n, starts, ends, branch, NULL, as[k], ae[k],   \
+                                         order, buf) : 0;                               \
+        for (int64_t j = 0; j < w; ++j) {                                               \
+            int64_t h = buf[j];                                                         \
+            S s = as[k] > starts[h] ? as[k] : starts[h];                                \
+            S e = ae[k] < ends[h] ? ae[k] : ends[h];                                    \
+            if (s <= e) {                                                               \
+                if (total < cap) { os[total] = s; oe[total] = e; ob[total] = h; }       \
+                ++total;                                                                \
+            }                                                                           \
+        }                                                                               \
+        if (off) off[k + 1] = total;                                                    \
+    }                                                                                   \
+    free(buf);                                                                          \
+    return total;                                                                       \
+}                                                                                       \
+                                                                                        \
+/* difference (hpp:1186-1211, c:951-974): per A interval, the hits' (start, end) */     \
+/* keys sorted ascending and swept with a cursor from as; every uncovered piece   */    \
+/* is emitted.  A covered piece reaching the type's maximum ends the sweep (the  */     \
+/* reference's cursor = end + 1 overflows there).                                */     \
+int64_t sio_difference_##SFX(int64_t n, const S* starts, const S* ends,                \
+                             const int64_t* branch, int64_t na, const S* as,            \
+                             const S* ae, int64_t* off, S* os, S* oe, int64_t cap) {    \
+    const S smax = (S)((((uint64_t)1) << (sizeof(S) * 8 - 1)) - 1);                     \
+    int64_t total = 0, bcap = 0;                                                        \
+    int64_t* buf = NULL;                                                                \
+    sio_key_##SFX* keys = NULL;                                                         \
+    if (off) off[0] = 0;                                                                \
+    for (int64_t k = 0; k < na; ++k) {                                                  \
+        int64_t c = sio_count_##SFX(n, starts, ends, branch, as[k], ae[k]);            \
+        if (c > bcap) {                                                                 \
+            bcap = 2 * c;                                                               \
+            buf = (int64_t*)realloc(buf, 8 * (size_t)bcap);                             \
+            keys = (sio_key_##SFX*)realloc(keys, sizeof(sio_key_##SFX) * (size_t)bcap); \
+        }                                                                               \
+        int64_t w = c ? sio_search_##SFX(n, starts, ends, branch, NULL, as[k], ae[k],   \
+                                         SIO_ORDER_DESC, buf) : 0;                      \
+        for (int64_t j = 0; j < w; ++j) { keys[j].s = starts[buf[j]]; keys[j].e = ends[buf[j]]; } \
+        if (w > 1) qsort(keys, (size_t)w, sizeof(sio_key_##SFX), sio_keycmp_##SFX);    \
+        S cursor = as[k];                                                               \
+        int closed = 0;                                                                 \
+        for (int64_t j = 0; j < w; ++j) {                                               \
+            S cs = keys[j].s > as[k] ? keys[j].s : as[k];                               \
+            S ce = keys[j].e < ae[k] ? keys[j].e : ae[k];                               \
+            if (!closed && cs > cursor) {                                               \
+                if (total < cap) { os[total] = cursor; oe[total] = cs - 1; }            \
+                ++total;                                                                \
+            }                                                                           \
+            if (ce == smax) closed = 1;                                                 \
+            else if (ce + 1 > cursor) cursor = ce + 1;                                  \
+        }                                                                               \
+        if (!closed && cursor <= ae[k]) {                                               \
+            if (total < cap) { os[total] = cursor; oe[total] = ae[k]; }                 \
+            ++total;                                                                    \
+        }                                                                               \
+        if (off) off[k + 1] = total;                                                    \
+    }                                                                                   \
+    free(buf);                                                                          \
+    free(keys);                                                                         \
+    return total;                                                                       \
+}                                                                                       \
+                                                                                        \
 /* coverage (hpp:979-1006): count and sum of min(e)-max(s) (no +1).              */     \
 void sio_coverage_##SFX(int64_t n, const S* starts, const S* ends,                      \
                         const int64_t* branch, S qs, S qe, int64_t* cnt, S* cov) {      \

@@ -97,6 +97,10 @@ SIGNATURES = {
     "upperBoundDeviceGpu": (_I, [_H, _P, _P, _SZ, _I, _P, _P]),
     "searchDeviceGraphGpu": (_I, [_H, _P, _P, _P, _SZ, _I, _P, _P, _SZ, C.POINTER(_SZ), _P]),
     "searchIdxsNoAllocGpu": (_I, [_H, _P, _P, _P, _SZ, _I, _P, _P, _SZ, C.POINTER(_SZ), _P]),
+    "intersectBatchGpu": (_I, [_H, _P, _P, _P, _SZ, _I, _P, _P, _P, _P, _SZ, C.POINTER(_SZ)]),
+    "intersectDeviceGpu": (_I, [_H, _P, _P, _P, _SZ, _I, _P, _P, _P, _P, _SZ, C.POINTER(_SZ), _P]),
+    "differenceBatchGpu": (_I, [_H, _P, _P, _P, _SZ, _P, _P, _P, _SZ, C.POINTER(_SZ)]),
+    "differenceDeviceGpu": (_I, [_H, _P, _P, _P, _SZ, _P, _P, _P, _SZ, C.POINTER(_SZ), _P]),
     "createCsrResult": (cCsrResult, []),
     "clearCsrResult": (None, [C.POINTER(cCsrResult)]),
     "destroyCsrResult": (None, [C.POINTER(cCsrResult)]),

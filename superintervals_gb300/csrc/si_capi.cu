@@ -142,6 +142,9 @@ struct gSuperIntervals {
     // query workspace
     DevBuf wq_s, wq_e, wq_c, w_counts, w_offsets, w_out, w_tmp, w_err;
     sig::BatchedWorkspace bws;
+    // set operations: hit lists, staged pieces, and whether some interval has start > end
+    DevBuf so_hoff, so_hits, so_off, so_os, so_oe, so_ob, so_flag;
+    int inverted = -1;  // -1 unknown, else 0 / 1 (reset by every build)
     // options
     int path = SI_PATH_AUTO;
     int ub_mode = SI_UB_BINARY;
@@ -263,6 +266,7 @@ int build_impl(gSuperIntervals* si) {
     for (int g = 0; g < G; ++g)
         if (segv[g + 1] < segv[g]) return fail(SI_ERR_INVALID, "contig offsets decrease at %d", g);
     si->built = false;
+    si->inverted = -1;
     si->bws.long_ends = nullptr;  // set again once the long-interval pyramid exists
     if (si->gexec) {              // a captured graph holds the old buffers
         cudaGraphExecDestroy(si->gexec);
@@ -363,10 +367,12 @@ int check_built(const gSuperIntervals* si) {
     return SI_OK;
 }
 
-int read_dev_err(gSuperIntervals* si) {
+// Reads the device error word after the work queued on `st` (the handle's stream by default).
+int read_dev_err(gSuperIntervals* si, cudaStream_t st = nullptr) {
+    if (!st) st = si->st;
     int e = 0;
-    SI_CK(cudaMemcpyAsync(&e, si->w_err.p, sizeof(int), cudaMemcpyDeviceToHost, si->st));
-    SI_CK(cudaStreamSynchronize(si->st));
+    SI_CK(cudaMemcpyAsync(&e, si->w_err.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+    SI_CK(cudaStreamSynchronize(st));
     if (e == sig::kDevBadContig) return fail(SI_ERR_INVALID, "a query names a contig outside [0, %d)", si->G);
     if (e == sig::kDevOverflow) return fail(SI_ERR_CUDA, "internal: emit overran its offsets");
     if (e != 0) return fail(SI_ERR_CUDA, "device error word %d", e);
@@ -440,7 +446,7 @@ int search_device(gSuperIntervals* si, const sig::QueryBatch& q, int order, bool
     if (total) *total = (size_t)P;
     if ((size_t)P > cap) return fail(SI_ERR_CAPACITY, "output needs %lld values, capacity %zu", (long long)P, cap);
     SI_TRY(run_emit<S>(si, q, 0, d_offsets, 0, order, values, d_out, st));
-    return read_dev_err(si);
+    return read_dev_err(si, st);
 }
 
 template <typename S>
@@ -1310,4 +1316,182 @@ extern "C" int searchDeviceGraphGpu(gSuperIntervals* si, const void* d_qs, const
     if (e != 0) return fail(SI_ERR_CUDA, "device error word %d", e);
     sig::note_launch((int)si->g_kernels);
     return SI_OK;
+}
+
+// =====================================================================================
+// Set operations: intersection / difference of a list of intervals (map A, passed as queries)
+// against the index (map B).  The hit lists come from the search path (count -> scan -> emit);
+// the pieces from a second count -> scan -> emit over those lists (si_setops.cu).
+// =====================================================================================
+namespace {
+
+// Hit lists of a device-resident batch into so_hoff / so_hits (contig-local positions).
+template <typename S>
+int hit_lists(gSuperIntervals* si, const sig::QueryBatch& q, int order, cudaStream_t st) {
+    SI_TRY(si->so_hoff.reserve(sizeof(int64_t) * (q.nq + 1)));
+    SI_TRY(si->w_counts.reserve(sizeof(uint32_t) * std::max<int64_t>(q.nq, 1)));
+    SI_TRY(si->w_tmp.reserve(sig::scan_temp_bytes(q.nq)));
+    SI_TRY(run_count<S>(si, q, si->w_counts.as<uint32_t>(), st));
+    SI_CK(sig::exclusive_scan_u32_to_i64(si->w_counts.as<uint32_t>(), si->so_hoff.as<int64_t>(), q.nq, si->w_tmp.p,
+                                         st));
+    int64_t P = 0;
+    SI_CK(cudaMemcpyAsync(&P, si->so_hoff.as<int64_t>() + q.nq, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+    SI_CK(cudaStreamSynchronize(st));
+    SI_TRY(si->so_hits.reserve(sizeof(int32_t) * std::max<int64_t>(P, 1)));
+    SI_TRY(run_emit<S>(si, q, 0, si->so_hoff.as<int64_t>(), 0, order, false, si->so_hits.as<int32_t>(), st));
+    return read_dev_err(si, st);
+}
+
+// op 0: intersection (order = the hit order), op 1: difference.  Pieces go to caller device
+// buffers when they hold `cap` pieces; `total` always receives the piece count.
+template <typename S>
+int setop_device(gSuperIntervals* si, const sig::QueryBatch& q, int op, int order, int64_t* d_off, S* d_os,
+                 S* d_oe, int32_t* d_ob, size_t cap, size_t* total, cudaStream_t st) {
+    SI_TRY(check_built(si));
+    SI_TRY(set_dev(si));
+    if (!d_off || (q.nq && (!q.qs || !q.qe))) return fail(SI_ERR_INVALID, "null device buffer");
+    if (total) *total = 0;
+    if (q.nq == 0) {
+        SI_CK(cudaMemsetAsync(d_off, 0, sizeof(int64_t), st));
+        SI_CK(cudaStreamSynchronize(st));
+        return SI_OK;
+    }
+    SI_TRY(si->w_err.reserve(sizeof(int)));
+    if (si->n > 0) {
+        SI_TRY(hit_lists<S>(si, q, op == 0 ? order : SI_ORDER_DESC, st));
+    } else {
+        SI_TRY(si->so_hoff.reserve(sizeof(int64_t) * (q.nq + 1)));
+        SI_TRY(si->so_hits.reserve(sizeof(int32_t)));
+        SI_CK(cudaMemsetAsync(si->so_hoff.p, 0, sizeof(int64_t) * (q.nq + 1), st));
+        SI_CK(cudaMemsetAsync(si->w_err.p, 0, sizeof(int), st));
+    }
+    bool sequential = false;
+    if (op == 1 && si->n > 0) {
+        if (si->inverted < 0) {
+            SI_TRY(si->so_flag.reserve(sizeof(int)));
+            SI_CK(sig::launch_any_inverted<S>(view<S>(si), si->so_flag.as<int>(), st));
+            int f = 0;
+            SI_CK(cudaMemcpyAsync(&f, si->so_flag.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+            SI_CK(cudaStreamSynchronize(st));
+            si->inverted = f ? 1 : 0;
+        }
+        sequential = si->inverted == 1;
+    }
+    const int64_t* hoff = si->so_hoff.as<int64_t>();
+    const int32_t* hits = si->so_hits.as<int32_t>();
+    SI_TRY(si->w_counts.reserve(sizeof(uint32_t) * q.nq));
+    SI_TRY(si->w_tmp.reserve(sig::scan_temp_bytes(q.nq)));
+    uint32_t* cnt = si->w_counts.as<uint32_t>();
+    if (op == 0)
+        SI_CK(sig::launch_isect<S>(view<S>(si), q, hoff, hits, cnt, nullptr, nullptr, nullptr, nullptr, si->w_err.as<int>(), st));
+    else
+        SI_CK(sig::launch_diff<S>(view<S>(si), q, hoff, hits, sequential, cnt, nullptr, nullptr, nullptr, si->w_err.as<int>(), st));
+    SI_CK(sig::exclusive_scan_u32_to_i64(cnt, d_off, q.nq, si->w_tmp.p, st));
+    int64_t T = 0;
+    SI_CK(cudaMemcpyAsync(&T, d_off + q.nq, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+    SI_TRY(read_dev_err(si, st));  // synchronizes
+    if (total) *total = (size_t)T;
+    if ((size_t)T > cap) return fail(SI_ERR_CAPACITY, "output needs %lld pieces, capacity %zu", (long long)T, cap);
+    if (T > 0 && (!d_os || !d_oe || (op == 0 && !d_ob))) return fail(SI_ERR_INVALID, "null output buffer");
+    if (T > 0) {
+        if (op == 0)
+            SI_CK(sig::launch_isect<S>(view<S>(si), q, hoff, hits, nullptr, d_off, d_os, d_oe, d_ob, si->w_err.as<int>(), st));
+        else
+            SI_CK(sig::launch_diff<S>(view<S>(si), q, hoff, hits, sequential, nullptr, d_off, d_os, d_oe, si->w_err.as<int>(), st));
+    }
+    return read_dev_err(si, st);
+}
+
+template <typename S>
+int setop_host(gSuperIntervals* si, const S* qs, const S* qe, const int32_t* qc, size_t nq, int op, int order,
+               int64_t* h_off, S* h_os, S* h_oe, int32_t* h_ob, size_t cap, size_t* total) {
+    SI_TRY(check_width<S>(si));
+    SI_TRY(check_built(si));
+    SI_TRY(set_dev(si));
+    if (!h_off) return fail(SI_ERR_INVALID, "null offsets");
+    sig::QueryBatch q;
+    SI_TRY(upload_queries<S>(si, qs, qe, qc, nq, q));
+    SI_TRY(si->so_off.reserve(sizeof(int64_t) * (nq + 1)));
+    size_t T = 0;
+    int r = setop_device<S>(si, q, op, order, si->so_off.as<int64_t>(), nullptr, nullptr, nullptr, 0, &T, si->st);
+    if (r != SI_OK && r != SI_ERR_CAPACITY) return r;
+    if (total) *total = T;
+    SI_CK(cudaMemcpyAsync(h_off, si->so_off.p, sizeof(int64_t) * (nq + 1), cudaMemcpyDeviceToHost, si->st));
+    SI_CK(cudaStreamSynchronize(si->st));
+    if (T > cap) return fail(SI_ERR_CAPACITY, "output needs %zu pieces, capacity %zu", T, cap);
+    if (T == 0) return SI_OK;
+    SI_TRY(si->so_os.reserve(sizeof(S) * T));
+    SI_TRY(si->so_oe.reserve(sizeof(S) * T));
+    if (op == 0) SI_TRY(si->so_ob.reserve(sizeof(int32_t) * T));
+    // the hit lists are still in place: emit the pieces only
+    const int64_t* hoff = si->so_hoff.as<int64_t>();
+    const int32_t* hits = si->so_hits.as<int32_t>();
+    if (op == 0)
+        SI_CK(sig::launch_isect<S>(view<S>(si), q, hoff, hits, nullptr, si->so_off.as<int64_t>(), si->so_os.as<S>(),
+                                   si->so_oe.as<S>(), si->so_ob.as<int32_t>(), si->w_err.as<int>(), si->st));
+    else
+        SI_CK(sig::launch_diff<S>(view<S>(si), q, hoff, hits, si->inverted == 1, nullptr, si->so_off.as<int64_t>(),
+                                  si->so_os.as<S>(), si->so_oe.as<S>(), si->w_err.as<int>(), si->st));
+    if (!h_os || !h_oe || (op == 0 && !h_ob)) return fail(SI_ERR_INVALID, "null output buffer");
+    SI_CK(cudaMemcpyAsync(h_os, si->so_os.p, sizeof(S) * T, cudaMemcpyDeviceToHost, si->st));
+    SI_CK(cudaMemcpyAsync(h_oe, si->so_oe.p, sizeof(S) * T, cudaMemcpyDeviceToHost, si->st));
+    if (op == 0) SI_CK(cudaMemcpyAsync(h_ob, si->so_ob.p, sizeof(int32_t) * T, cudaMemcpyDeviceToHost, si->st));
+    SI_CK(cudaStreamSynchronize(si->st));
+    return SI_OK;
+}
+
+int check_order(int order) {
+    if (order != SI_ORDER_IDXS_CPP && order != SI_ORDER_DESC) return fail(SI_ERR_INVALID, "unknown order %d", order);
+    return SI_OK;
+}
+
+}  // namespace
+
+extern "C" int intersectDeviceGpu(gSuperIntervals* si, const void* d_qs, const void* d_qe, const int32_t* d_qc,
+                                  size_t nq, int order, int64_t* d_offsets, void* d_starts, void* d_ends,
+                                  int32_t* d_hits, size_t capacity, size_t* total, void* stream) {
+    SI_TRY(check_built(si));
+    SI_TRY(check_order(order));
+    cudaStream_t st = stream ? (cudaStream_t)stream : si->st;
+    sig::QueryBatch q{d_qs, d_qe, d_qc, (int64_t)nq};
+    if (si->bits == 64)
+        return setop_device<int64_t>(si, q, 0, order, d_offsets, (int64_t*)d_starts, (int64_t*)d_ends, d_hits,
+                                     capacity, total, st);
+    return setop_device<int32_t>(si, q, 0, order, d_offsets, (int32_t*)d_starts, (int32_t*)d_ends, d_hits,
+                                 capacity, total, st);
+}
+
+extern "C" int differenceDeviceGpu(gSuperIntervals* si, const void* d_qs, const void* d_qe, const int32_t* d_qc,
+                                   size_t nq, int64_t* d_offsets, void* d_starts, void* d_ends, size_t capacity,
+                                   size_t* total, void* stream) {
+    SI_TRY(check_built(si));
+    cudaStream_t st = stream ? (cudaStream_t)stream : si->st;
+    sig::QueryBatch q{d_qs, d_qe, d_qc, (int64_t)nq};
+    if (si->bits == 64)
+        return setop_device<int64_t>(si, q, 1, 0, d_offsets, (int64_t*)d_starts, (int64_t*)d_ends, nullptr, capacity,
+                                     total, st);
+    return setop_device<int32_t>(si, q, 1, 0, d_offsets, (int32_t*)d_starts, (int32_t*)d_ends, nullptr, capacity,
+                                 total, st);
+}
+
+extern "C" int intersectBatchGpu(gSuperIntervals* si, const void* qs, const void* qe, const int32_t* qc, size_t nq,
+                                 int order, int64_t* offsets, void* starts, void* ends, int32_t* hits,
+                                 size_t capacity, size_t* total) {
+    SI_TRY(check_built(si));
+    SI_TRY(check_order(order));
+    if (si->bits == 64)
+        return setop_host<int64_t>(si, (const int64_t*)qs, (const int64_t*)qe, qc, nq, 0, order, offsets,
+                                   (int64_t*)starts, (int64_t*)ends, hits, capacity, total);
+    return setop_host<int32_t>(si, (const int32_t*)qs, (const int32_t*)qe, qc, nq, 0, order, offsets,
+                               (int32_t*)starts, (int32_t*)ends, hits, capacity, total);
+}
+
+extern "C" int differenceBatchGpu(gSuperIntervals* si, const void* qs, const void* qe, const int32_t* qc, size_t nq,
+                                  int64_t* offsets, void* starts, void* ends, size_t capacity, size_t* total) {
+    SI_TRY(check_built(si));
+    if (si->bits == 64)
+        return setop_host<int64_t>(si, (const int64_t*)qs, (const int64_t*)qe, qc, nq, 1, 0, offsets,
+                                   (int64_t*)starts, (int64_t*)ends, nullptr, capacity, total);
+    return setop_host<int32_t>(si, (const int32_t*)qs, (const int32_t*)qe, qc, nq, 1, 0, offsets,
+                               (int32_t*)starts, (int32_t*)ends, nullptr, capacity, total);
 }

@@ -154,6 +154,19 @@ struct MapView {
     int64_t n;
 };
 
+// set operations over hit lists (CSR of contig-local positions): intersection pieces (kept when
+// start <= end) and difference pieces; counts when ooff is null, else writes at ooff
+template <typename S>
+cudaError_t launch_isect(MapView<S> m, QueryBatch q, const int64_t* hoff, const int32_t* hits,
+                         uint32_t* counts, const int64_t* ooff, S* os, S* oe, int32_t* ob, int* d_err,
+                         cudaStream_t st);
+template <typename S>
+cudaError_t launch_diff(MapView<S> m, QueryBatch q, const int64_t* hoff, const int32_t* hits, bool sequential,
+                        uint32_t* counts, const int64_t* ooff, S* os, S* oe, int* d_err, cudaStream_t st);
+// flag = 1 when some interval has start > end
+template <typename S>
+cudaError_t launch_any_inverted(MapView<S> m, int* flag, cudaStream_t st);
+
 // plain one-query-per-thread path: upper_bound + branch walk per query
 template <typename S>
 cudaError_t launch_count_plain(MapView<S> m, QueryBatch q, uint32_t* counts, int* d_err,

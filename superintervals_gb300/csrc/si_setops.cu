@@ -1,0 +1,285 @@
+// si_setops.cu -- batch set operations of a list of intervals (map A, given as queries) against
+// the index (map B), built on the hit lists of the search path.
+//
+//   intersection (src/superintervals.hpp:1158-1177, src/c_superintervals.h:921-940): for query
+//     interval [qs, qe] and each hit h in the search order, the piece
+//     [max(qs, starts[h]), min(qe, ends[h])], kept when start <= end.
+//   difference (hpp:1186-1211, c:951-974): the hits' (start, end) keys sorted ascending and
+//     swept with a cursor from qs; every uncovered piece [cursor, cs - 1] and the trailing
+//     [cursor, qe] are emitted.
+//
+// Both run count -> scan -> emit over the hit lists (CSR of contig-local positions), one warp
+// per query.  Intersection compacts kept pieces with a ballot.  Difference walks the hits in
+// ascending position order (the reverse of the fully descending list): with start <= end for
+// every hit and qs <= qe, the order inside a run of equal starts does not change the pieces, so
+// the cursor before each hit is a warp max-scan of (ce + 1) and the gaps are a ballot.  When B
+// holds intervals with start > end the order inside equal-start runs matters (the reference
+// sorts by (start, end) ascending), and lane 0 sweeps the query sequentially in exactly that
+// order.  A covered piece reaching the type's maximum ends the sweep (the reference's
+// cursor = end + 1 overflows there).
+#include <algorithm>
+#include "si_internal.cuh"
+
+namespace sig {
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kWarpsPerBlock = kThreads / kWarp;
+
+template <typename S>
+__device__ __forceinline__ S smax(S a, S b) { return a > b ? a : b; }
+template <typename S>
+__device__ __forceinline__ S smin(S a, S b) { return a < b ? a : b; }
+
+template <typename S>
+__device__ __forceinline__ S warp_incl_max(S v) {
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const S o = __shfl_up_sync(kFull, v, d);
+        if (lane >= d) v = smax(v, o);
+    }
+    return v;
+}
+
+// One warp per query, grid-stride over queries.
+template <typename S, bool EMIT>
+__global__ void __launch_bounds__(kThreads) k_isect(MapView<S> m, const S* __restrict__ qs,
+                                                    const S* __restrict__ qe, const int32_t* __restrict__ qc,
+                                                    int64_t nq, const int64_t* __restrict__ hoff,
+                                                    const int32_t* __restrict__ hits, uint32_t* __restrict__ cnt,
+                                                    const int64_t* __restrict__ ooff, S* __restrict__ os,
+                                                    S* __restrict__ oe, int32_t* __restrict__ ob, int* d_err) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warps = (int64_t)gridDim.x * kWarpsPerBlock;
+    for (int64_t q = (int64_t)blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5); q < nq; q += warps) {
+        const int g = qc ? qc[q] : 0;
+        if (g < 0 || g >= m.G) {  // reported; such a query has no piece
+            if (lane == 0) {
+                atomicCAS(d_err, kDevOk, kDevBadContig);
+                if (!EMIT) cnt[q] = 0;
+            }
+            continue;
+        }
+        const int64_t a = hoff[q], b = hoff[q + 1];
+        const S s0 = qs[q], e0 = qe[q];
+        const int64_t lo = m.seg[g];
+        int64_t w = EMIT ? ooff[q] : 0;
+        uint32_t c = 0;
+        for (int64_t p0 = a; p0 < b; p0 += 32) {
+            const int64_t p = p0 + lane;
+            bool keep = false;
+            S s = 0, e = 0;
+            int32_t h = 0;
+            if (p < b) {
+                h = hits[p];
+                s = smax(s0, m.starts[lo + h]);
+                e = smin(e0, m.ends[lo + h]);
+                keep = s <= e;
+            }
+            const uint32_t bal = __ballot_sync(kFull, keep);
+            if (EMIT && keep) {
+                const int64_t at = w + __popc(bal & lanemask_lt());
+                os[at] = s;
+                oe[at] = e;
+                ob[at] = h;
+            }
+            w += __popc(bal);
+            c += __popc(bal);
+        }
+        if (!EMIT && lane == 0) cnt[q] = c;
+    }
+}
+
+// Exact sequential sweep of one query (lane 0): runs of equal start in ascending start order,
+// each run in ascending end order.  The hit list is fully descending in position, i.e. start
+// descending and, inside an equal-start run, end ascending.
+template <typename S, bool EMIT>
+__device__ uint32_t diff_sequential(const S* __restrict__ st, const S* __restrict__ en,
+                                    const int32_t* __restrict__ list, int64_t m, S s0, S e0, S* os, S* oe,
+                                    int64_t w) {
+    uint32_t c = 0;
+    S cursor = s0;
+    bool closed = false;
+    int64_t j = m - 1;
+    while (j >= 0) {
+        const S rs = st[list[j]];
+        int64_t r = j;
+        while (r > 0 && st[list[r - 1]] == rs) --r;
+        for (int64_t k = r; k <= j; ++k) {
+            const int32_t h = list[k];
+            const S cs = smax(st[h], s0), ce = smin(en[h], e0);
+            if (!closed && cs > cursor) {
+                if (EMIT) {
+                    os[w + c] = cursor;
+                    oe[w + c] = cs - 1;
+                }
+                ++c;
+            }
+            if (ce == Lim<S>::hi) closed = true;
+            else if (ce + 1 > cursor) cursor = ce + 1;
+        }
+        j = r - 1;
+    }
+    if (!closed && cursor <= e0) {
+        if (EMIT) {
+            os[w + c] = cursor;
+            oe[w + c] = e0;
+        }
+        ++c;
+    }
+    return c;
+}
+
+template <typename S, bool EMIT>
+__global__ void __launch_bounds__(kThreads) k_diff(MapView<S> m, const S* __restrict__ qs,
+                                                   const S* __restrict__ qe, const int32_t* __restrict__ qc,
+                                                   int64_t nq, const int64_t* __restrict__ hoff,
+                                                   const int32_t* __restrict__ hits, int sequential,
+                                                   uint32_t* __restrict__ cnt, const int64_t* __restrict__ ooff,
+                                                   S* __restrict__ os, S* __restrict__ oe, int* d_err) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warps = (int64_t)gridDim.x * kWarpsPerBlock;
+    for (int64_t q = (int64_t)blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5); q < nq; q += warps) {
+        const int g = qc ? qc[q] : 0;
+        if (g < 0 || g >= m.G) {  // reported; such a query has no piece
+            if (lane == 0) {
+                atomicCAS(d_err, kDevOk, kDevBadContig);
+                if (!EMIT) cnt[q] = 0;
+            }
+            continue;
+        }
+        const int64_t a = hoff[q], b = hoff[q + 1], mq = b - a;
+        const S s0 = qs[q], e0 = qe[q];
+        const int64_t lo = m.seg[g];
+        const S* st = m.starts + lo;
+        const S* en = m.ends + lo;
+        const int64_t w0 = EMIT ? ooff[q] : 0;
+        if (sequential) {
+            if (lane == 0) {
+                const uint32_t c = diff_sequential<S, EMIT>(st, en, hits + a, mq, s0, e0, os, oe, w0);
+                if (!EMIT) cnt[q] = c;
+            }
+            continue;
+        }
+        // qs > qe: every hit starts at or before qe < qs, so no gap opens before the cursor qs,
+        // and the trailing piece needs cursor <= qe: no piece at all
+        if (s0 > e0) {
+            if (!EMIT && lane == 0) cnt[q] = 0;
+            continue;
+        }
+        S cursor = s0;
+        bool closed = false;
+        int64_t w = w0;
+        uint32_t c = 0;
+        for (int64_t t0 = 0; t0 < mq; t0 += 32) {
+            const int64_t t = t0 + lane;
+            const bool valid = t < mq;
+            S cs = 0, nxt = Lim<S>::lo;
+            bool cl = false;
+            if (valid) {
+                const int32_t h = hits[b - 1 - t];  // ascending position order
+                cs = smax(st[h], s0);
+                const S ce = smin(en[h], e0);
+                cl = ce == Lim<S>::hi;
+                nxt = cl ? Lim<S>::lo : ce + 1;
+            }
+            const S incl = warp_incl_max(nxt);
+            S excl = __shfl_up_sync(kFull, incl, 1);
+            if (lane == 0) excl = Lim<S>::lo;
+            const uint32_t clb = __ballot_sync(kFull, cl);
+            const S cur = smax(cursor, excl);
+            const bool closed_here = closed || (clb & lanemask_lt()) != 0;
+            const bool gap = valid && !closed_here && cs > cur;
+            const uint32_t gb = __ballot_sync(kFull, gap);
+            if (EMIT && gap) {
+                const int64_t at = w + __popc(gb & lanemask_lt());
+                os[at] = cur;
+                oe[at] = cs - 1;
+            }
+            w += __popc(gb);
+            c += __popc(gb);
+            cursor = smax(cursor, __shfl_sync(kFull, incl, 31));
+            closed = closed || clb != 0;
+        }
+        if (!closed && cursor <= e0) {
+            if (EMIT && lane == 0) {
+                os[w] = cursor;
+                oe[w] = e0;
+            }
+            ++c;
+        }
+        if (!EMIT && lane == 0) cnt[q] = c;
+    }
+}
+
+template <typename S>
+__global__ void k_any_inverted(const S* __restrict__ starts, const S* __restrict__ ends, int64_t n,
+                               int* __restrict__ flag) {
+    bool inv = false;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        inv = inv || starts[i] > ends[i];
+    if (__any_sync(kFull, inv) && (threadIdx.x & 31) == 0) atomicOr(flag, 1);
+}
+
+inline unsigned warp_blocks(int64_t nq) {
+    // one warp per query, at most 16 resident blocks of 8 warps per SM on 152 SMs
+    return (unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(nq, kWarpsPerBlock), 152 * 16 * 8));
+}
+
+}  // namespace
+
+template <typename S>
+cudaError_t launch_isect(MapView<S> m, QueryBatch q, const int64_t* hoff, const int32_t* hits,
+                         uint32_t* counts, const int64_t* ooff, S* os, S* oe, int32_t* ob, int* d_err,
+                         cudaStream_t st) {
+    if (q.nq <= 0) return cudaSuccess;
+    const S* qs = static_cast<const S*>(q.qs);
+    const S* qe = static_cast<const S*>(q.qe);
+    if (ooff)
+        k_isect<S, true><<<warp_blocks(q.nq), kThreads, 0, st>>>(m, qs, qe, q.qc, q.nq, hoff, hits, nullptr, ooff,
+                                                                 os, oe, ob, d_err);
+    else
+        k_isect<S, false><<<warp_blocks(q.nq), kThreads, 0, st>>>(m, qs, qe, q.qc, q.nq, hoff, hits, counts,
+                                                                  nullptr, nullptr, nullptr, nullptr, d_err);
+    note_launch();
+    return cudaGetLastError();
+}
+
+template <typename S>
+cudaError_t launch_diff(MapView<S> m, QueryBatch q, const int64_t* hoff, const int32_t* hits, bool sequential,
+                        uint32_t* counts, const int64_t* ooff, S* os, S* oe, int* d_err, cudaStream_t st) {
+    if (q.nq <= 0) return cudaSuccess;
+    const S* qs = static_cast<const S*>(q.qs);
+    const S* qe = static_cast<const S*>(q.qe);
+    if (ooff)
+        k_diff<S, true><<<warp_blocks(q.nq), kThreads, 0, st>>>(m, qs, qe, q.qc, q.nq, hoff, hits, sequential ? 1 : 0,
+                                                                nullptr, ooff, os, oe, d_err);
+    else
+        k_diff<S, false><<<warp_blocks(q.nq), kThreads, 0, st>>>(m, qs, qe, q.qc, q.nq, hoff, hits,
+                                                                 sequential ? 1 : 0, counts, nullptr, nullptr,
+                                                                 nullptr, d_err);
+    note_launch();
+    return cudaGetLastError();
+}
+
+template <typename S>
+cudaError_t launch_any_inverted(MapView<S> m, int* flag, cudaStream_t st) {
+    cudaError_t e = cudaMemsetAsync(flag, 0, sizeof(int), st);
+    if (e != cudaSuccess || m.n <= 0) return e;
+    const unsigned blocks = (unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(m.n, kThreads), 152 * 8));
+    k_any_inverted<S><<<blocks, kThreads, 0, st>>>(m.starts, m.ends, m.n, flag);
+    note_launch();
+    return cudaGetLastError();
+}
+
+#define SIG_SINST(S)                                                                                          \
+    template cudaError_t launch_isect<S>(MapView<S>, QueryBatch, const int64_t*, const int32_t*, uint32_t*,   \
+                                         const int64_t*, S*, S*, int32_t*, int*, cudaStream_t);               \
+    template cudaError_t launch_diff<S>(MapView<S>, QueryBatch, const int64_t*, const int32_t*, bool,         \
+                                        uint32_t*, const int64_t*, S*, S*, int*, cudaStream_t);               \
+    template cudaError_t launch_any_inverted<S>(MapView<S>, int*, cudaStream_t);
+SIG_SINST(int32_t)
+SIG_SINST(int64_t)
+
+}  // namespace sig

@@ -162,6 +162,39 @@ class GpuIndex:
             break
         return off, out[: int(off[-1])] if nq else out[:0]
 
+    def _setop(self, fn, qs, qe, qc, extra, want_hits):
+        qs, qe, qc = self._queries(qs, qe, qc)
+        nq = qs.shape[0]
+        off = np.empty(nq + 1, np.int64)
+        total = C.c_size_t(0)
+        cap = 0
+        bufs = (np.empty(1, self.dtype), np.empty(1, self.dtype), np.empty(1, np.int32))
+        for _ in range(2):
+            args = [self.h, _p(qs), _p(qe), _p(qc), nq, *extra, _p(off), _p(bufs[0]), _p(bufs[1])]
+            if want_hits:
+                args.append(_p(bufs[2]))
+            st = fn(*args, cap, C.byref(total))
+            if st == _capi.SI_ERR_CAPACITY:
+                cap = int(total.value)
+                bufs = (np.empty(cap, self.dtype), np.empty(cap, self.dtype), np.empty(cap, np.int32))
+                continue
+            check(st)
+            break
+        k = int(total.value)
+        return off, bufs[0][:k], bufs[1][:k], bufs[2][:k]
+
+    def intersect(self, qs, qe, qc=None, order=ORDER_IDXS_CPP):
+        """intersection (superintervals.hpp:1158-1177) of the query intervals (another
+        map's) with this index: CSR offsets, piece starts, piece ends and the hit's
+        contig-local position, in the search order ``order``."""
+        return self._setop(self.lib.intersectBatchGpu, qs, qe, qc, [int(order)], True)
+
+    def difference(self, qs, qe, qc=None):
+        """difference (superintervals.hpp:1186-1211): the pieces of each query interval
+        not covered by this index (CSR offsets, piece starts, piece ends)."""
+        off, s, e, _ = self._setop(self.lib.differenceBatchGpu, qs, qe, qc, [], False)
+        return off, s, e
+
 
 class IntervalMap:
     """Drop-in mirror of the reference's Python ``IntervalMap``
@@ -297,6 +330,38 @@ class IntervalMap:
         off, out = self._idx.search(s, e, order=ORDER_IDXS_CPP)
         vals = out.tolist()
         return [vals[off[i]:off[i + 1]] for i in range(s.shape[0])]
+
+    # set operations (pyx:577-643); results are new, built maps
+    def intersection(self, other: "IntervalMap", combine=None) -> "IntervalMap":
+        """Regions covered by both maps: for each interval of this map (in its
+        current order) and each hit in ``other`` (C++ search_idxs order), the
+        overlapping piece; data = combine(a, b), by default the tuple (a, b)."""
+        other._need()
+        out = IntervalMap()
+        if self.size() and other.size():
+            off, s, e, h = other._idx.intersect(np.asarray(self._starts, np.int32),
+                                                 np.asarray(self._ends, np.int32), order=ORDER_IDXS_CPP)
+            owner = np.repeat(np.arange(self.size()), np.diff(off)).tolist()
+            av, bv = self._values, other._values
+            for k, (ps, pe, hh) in enumerate(zip(s.tolist(), e.tolist(), h.tolist())):
+                a, b = av[owner[k]], bv[hh]
+                out.add(ps, pe, combine(a, b) if combine is not None else (a, b))
+        out.build()
+        return out
+
+    def difference(self, other: "IntervalMap") -> "IntervalMap":
+        """Regions of this map not covered by ``other`` (A minus B); each piece
+        keeps its source interval's value."""
+        other._need()
+        out = IntervalMap()
+        if self.size():
+            off, s, e = other._idx.difference(np.asarray(self._starts, np.int32),
+                                              np.asarray(self._ends, np.int32))
+            owner = np.repeat(np.arange(self.size()), np.diff(off)).tolist()
+            for k, (ps, pe) in enumerate(zip(s.tolist(), e.tolist())):
+                out.add(ps, pe, self._values[owner[k]])
+        out.build()
+        return out
 
     def search_values_batch(self, starts, ends) -> list:
         s, e = self._q(starts, ends)

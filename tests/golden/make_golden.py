@@ -114,6 +114,48 @@ def save_case(ref, name, starts, ends, data, qs, qe, extra=None):
           f"{os.path.getsize(path) / 1024:.0f} KiB")
 
 
+def setop_cases():
+    """(name, A triples, B triples) for intersection / difference."""
+    cases = [
+        ("setops_small", [(1, 10, 0), (5, 20, 1), (30, 40, 2), (50, 55, 3)],
+         [(3, 4, 0), (8, 12, 1), (15, 35, 2), (52, 53, 3)]),
+        # touching, not overlapping; a cover that reaches past A on both sides; duplicates
+        ("setops_touching", [(5, 35, 0), (10, 19, 1), (40, 60, 2), (40, 60, 3)],
+         [(10, 19, 0), (20, 29, 1), (0, 100, 2), (45, 45, 3), (45, 45, 4), (61, 70, 5)]),
+        ("setops_emptyb", [(1, 5, 0), (7, 9, 1)], []),
+        ("setops_emptya", [], [(1, 5, 0)]),
+    ]
+    return cases
+
+
+def random_setop(seed, na, nb, dt, span=60_000, max_len=1_500, inverted=0.0):
+    r = np.random.Generator(np.random.PCG64(seed))
+
+    def draw(n):
+        s = r.integers(0, span, n)
+        ln = np.minimum(np.rint(np.exp(r.normal(np.log(200), 1.2, n))), max_len).astype(np.int64)
+        k = np.nonzero(r.random(n - 1) < 0.05)[0] + 1  # exact duplicates of the previous interval
+        s[k], ln[k] = s[k - 1], ln[k - 1]
+        k = np.nonzero(r.random(n - 1) < 0.05)[0] + 1  # shared start, own length
+        s[k] = s[k - 1]
+        e = s + ln - 1
+        inv = r.random(n) < inverted                  # start > end
+        s[inv], e[inv] = e[inv] + 3, s[inv]
+        return s.astype(dt), e.astype(dt), np.arange(n, dtype=np.int32)
+    return draw(na), draw(nb)
+
+
+def save_setop(ref, name, a, b):
+    res = ref.setops(a, b)
+    payload = dict(a_starts=np.asarray(a[0]), a_ends=np.asarray(a[1]), a_data=np.asarray(a[2], np.int32),
+                   b_starts=np.asarray(b[0]), b_ends=np.asarray(b[1]), b_data=np.asarray(b[2], np.int32))
+    payload.update({"ref_" + k: v for k, v in res.items()})
+    path = os.path.join(HERE, name + ".npz")
+    np.savez_compressed(path, **payload)
+    print(f"{name}: |A|={len(a[0])} |B|={len(b[0])} isect={len(res['isect_starts'])} "
+          f"diff={len(res['diff_starts'])} {os.path.getsize(path) / 1024:.0f} KiB")
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref-src", default=O.REF_SRC_DEFAULT)
@@ -163,6 +205,21 @@ def main():
         save_case(ref, f"contigs3_g{g}_int32", wl.starts[lo:hi], wl.ends[lo:hi],
                   wl.data[lo:hi], wl.q_starts[sel], wl.q_ends[sel],
                   extra=dict(q_index=np.nonzero(sel)[0].astype(np.int64)))
+    # set operations: intersection / difference of map A against map B
+    for name, a, b in setop_cases():
+        for dt in (np.int32, np.int64):
+            tr = [tuple(np.array([t[i] for t in m], dtype=(dt if i < 2 else np.int32)) for i in range(3))
+                  for m in (a, b)]
+            save_setop(ref, f"{name}_{np.dtype(dt).name}", tr[0], tr[1])
+    for seed, dt in ((21, np.int32), (22, np.int64)):
+        a, b = random_setop(seed, 1500, 3000, dt)                       # dense: B covers ~20x
+        save_setop(ref, f"setops_random_{np.dtype(dt).name}", a, b)
+        a, b = random_setop(seed + 10, 1500, 3000, dt, span=1_500_000)  # sparse: many gaps
+        save_setop(ref, f"setops_sparse_{np.dtype(dt).name}", a, b)
+    # B (and A) holding some start > end intervals: the sweep order inside equal-start runs matters
+    a, b = random_setop(23, 800, 2000, np.int32, span=300_000, inverted=0.03)
+    save_setop(ref, "setops_inverted_int32", a, b)
+
     np.savez_compressed(os.path.join(HERE, "contigs3_stream_int32.npz"), starts=wl.starts,
                         ends=wl.ends, data=wl.data, seg=wl.seg, q_starts=wl.q_starts,
                         q_ends=wl.q_ends, q_contig=wl.q_contig)

@@ -8,8 +8,10 @@ GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
 
 def fixture_names(prefix=""):
-    return sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, prefix + "*.npz"))
-                  if not os.path.basename(p).startswith("contigs3_stream"))
+    """Single-map query fixtures (prefix "setops_" selects the set-operation ones)."""
+    names = sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, prefix + "*.npz"))
+                   if not os.path.basename(p).startswith("contigs3_stream"))
+    return names if prefix.startswith("setops") else [n for n in names if not n.startswith("setops_")]
 
 
 def load(name):

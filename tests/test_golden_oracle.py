@@ -124,3 +124,30 @@ def test_oracle_upper_bound_batch(oracle, name):
     got = oracle.upper_bound_batch(m, qe, nthreads=3)
     want = np.searchsorted(m["starts"], qe.astype(m["starts"].dtype), side="right") - 1
     assert np.array_equal(got, want)
+
+
+SETOP_FIXTURES = fixture_names("setops_")
+
+
+@pytest.mark.parametrize("name", SETOP_FIXTURES)
+def test_oracle_setops_match_reference(oracle, name):
+    """intersection / difference (hpp:1158-1211, c:921-974) of the reference's
+    built A against B: pieces, their order and their data."""
+    g = load(name)
+    m = oracle.build(g["b_starts"], g["b_ends"], g["b_data"])
+    a_s, a_e, a_d = g["ref_a_sorted_starts"], g["ref_a_sorted_ends"], g["ref_a_sorted_data"]
+    off, os_, oe_, ob = oracle.intersection(m, a_s, a_e, ORDER_IDXS_CPP)
+    assert np.array_equal(os_, g["ref_isect_starts"]) and np.array_equal(oe_, g["ref_isect_ends"])
+    owner = np.repeat(np.arange(len(a_s)), np.diff(off))
+    assert np.array_equal(a_d[owner], g["ref_isect_data"])
+    # b's data names the B interval by insertion index: same coordinates as the hit
+    bd = g["ref_isect_bdata_data"]
+    assert np.array_equal(g["b_starts"][bd], m["starts"][ob]) and np.array_equal(g["b_ends"][bd], m["ends"][ob])
+    off, os_, oe_ = oracle.difference(m, a_s, a_e)
+    assert np.array_equal(os_, g["ref_diff_starts"]) and np.array_equal(oe_, g["ref_diff_ends"])
+    owner = np.repeat(np.arange(len(a_s)), np.diff(off))
+    assert np.array_equal(a_d[owner], g["ref_diff_data"])
+    if "ref_c_isect_starts" in g:   # the C API: searchIdxs order (fully descending)
+        _, os_, oe_, _ = oracle.intersection(m, a_s, a_e, ORDER_DESC)
+        assert np.array_equal(os_, g["ref_c_isect_starts"]) and np.array_equal(oe_, g["ref_c_isect_ends"])
+        assert np.array_equal(g["ref_c_diff_starts"], g["ref_diff_starts"])
