@@ -842,6 +842,17 @@ __global__ void __launch_bounds__(kThreads, 4) k_tiles(TileArgs<S> a) {
                     q_lb[i] = flags ? -1 - lb : lb;  // negative: some long candidate misses
                 }
                 __syncthreads();
+                // the lists now only feed the writes: turn positions into the values written
+                // (contig-local positions, or payloads), once per run instead of once per hit
+                for (int k = tid; k < nc; k += kThreads) {
+                    const int32_t p = cpos[k];
+                    cpos[k] = a.values ? a.data[p] : p - (int32_t)lo;
+                }
+                for (int k = tid; k < nl; k += kThreads) {
+                    const int32_t p = lpos[k];
+                    lpos[k] = a.values ? a.data[p] : p - (int32_t)lo;
+                }
+                __syncthreads();
             }
             for (int i = r0 + warp; EMIT && !per_query && !long_run && i < r1; i += kWarpsPerCta) {
                 // emit, step 2: one query per WARP writes its hits, coalesced
@@ -858,24 +869,29 @@ __global__ void __launch_bounds__(kThreads, 4) k_tiles(TileArgs<S> a) {
                     const int64_t pos = (a.order == kOrderIdxsCpp) ? (u - h + 1 + r) : (u - r);
                     dst[r] = a.values ? a.data[pos] : (int32_t)(pos - lo);
                 }
-                int64_t w = h;
+                const unsigned lt = lanemask_lt();
+                int32_t* d = dst + h;            // next write
+                int64_t room = capq - h;         // writes left for this query
                 bool bad = false;
-                const int ta = q_ta[i], tsplit = q_tsplit[i];
-                // part A: candidates near qs after the head
-                for (int kk = ta; kk < tsplit; kk += 32) {
-                    const int tt = kk + lane;
-                    const bool hit = tt < tsplit && cend[tt] >= qs;
-                    const unsigned m = __ballot_sync(kFull, hit);
-                    const int k = __popc(m);
-                    if (w + k > capq) {
-                        bad = true;
-                        break;
+                // part A: candidates near qs after the head, two 32-wide slices per round
+                {
+                    const int ta = q_ta[i], tsplit = q_tsplit[i];
+                    for (int kk = ta; kk < tsplit; kk += 64) {
+                        const int t0 = kk + lane, t1 = t0 + 32;
+                        const bool h0 = t0 < tsplit && cend[t0] >= qs;
+                        const bool h1 = t1 < tsplit && cend[t1] >= qs;
+                        const int32_t v0 = h0 ? cpos[t0] : 0, v1 = h1 ? cpos[t1] : 0;
+                        const unsigned m0 = __ballot_sync(kFull, h0), m1 = __ballot_sync(kFull, h1);
+                        const int c0 = __popc(m0), c = c0 + __popc(m1);
+                        if (c > room) {
+                            bad = true;
+                            break;
+                        }
+                        if (h0) d[__popc(m0 & lt)] = v0;
+                        if (h1) d[c0 + __popc(m1 & lt)] = v1;
+                        d += c;
+                        room -= c;
                     }
-                    if (hit) {
-                        const int32_t pos = cpos[tt];
-                        dst[w + __popc(m & lanemask_lt())] = a.values ? a.data[pos] : pos - (int32_t)lo;
-                    }
-                    w += k;
                 }
                 // part B: the long candidates from lb on
                 const int lbf = q_lb[i];
@@ -884,19 +900,21 @@ __global__ void __launch_bounds__(kThreads, 4) k_tiles(TileArgs<S> a) {
                 if (!bad && lb < nl) {
                     if (!miss) {
                         const int len = nl - lb;
-                        if (w + len > capq) {
+                        if (len > room) {
                             bad = true;
                         } else {
-                            for (int k = lane; k < len; k += 32) {
-                                const int32_t pos = lpos[lb + k];
-                                dst[w + k] = a.values ? a.data[pos] : pos - (int32_t)lo;
+                            const int32_t* src = lpos + lb;
+                            int k = lane;
+                            for (; k + 32 < len; k += 64) {
+                                const int32_t v0 = src[k], v1 = src[k + 32];
+                                d[k] = v0;
+                                d[k + 32] = v1;
                             }
-                            w += len;
+                            if (k < len) d[k] = src[k];
                         }
                     } else {
                         // 128 candidates per round as four independent 32-wide slices, so their
                         // shared-memory reads and ballots overlap instead of chaining
-                        const unsigned lt = lanemask_lt();
                         for (int kk = lb; kk < nl; kk += 128) {
                             bool hit[4];
                             int32_t pv[4];
@@ -904,23 +922,24 @@ __global__ void __launch_bounds__(kThreads, 4) k_tiles(TileArgs<S> a) {
 #pragma unroll
                             for (int s = 0; s < 4; ++s) {
                                 const int tt = kk + 32 * s + lane;
-                                hit[s] = tt < nl && lend[tt] >= qs;
-                                pv[s] = hit[s] ? lpos[tt] : 0;
+                                const bool in = tt < nl;
+                                hit[s] = in && lend[tt] >= qs;
+                                pv[s] = in ? lpos[tt] : 0;
                             }
 #pragma unroll
                             for (int s = 0; s < 4; ++s) m[s] = __ballot_sync(kFull, hit[s]);
-                            const int c0 = __popc(m[0]), c1 = __popc(m[1]), c2 = __popc(m[2]), c3 = __popc(m[3]);
-                            if (w + c0 + c1 + c2 + c3 > capq) {
+                            const int c0 = __popc(m[0]), c1 = c0 + __popc(m[1]), c2 = c1 + __popc(m[2]);
+                            const int c = c2 + __popc(m[3]);
+                            if (c > room) {
                                 bad = true;
                                 break;
                             }
-                            const int64_t base[4] = {w, w + c0, w + c0 + c1, w + c0 + c1 + c2};
-#pragma unroll
-                            for (int s = 0; s < 4; ++s) {
-                                if (hit[s])
-                                    dst[base[s] + __popc(m[s] & lt)] = a.values ? a.data[pv[s]] : pv[s] - (int32_t)lo;
-                            }
-                            w += c0 + c1 + c2 + c3;
+                            if (hit[0]) d[__popc(m[0] & lt)] = pv[0];
+                            if (hit[1]) d[c0 + __popc(m[1] & lt)] = pv[1];
+                            if (hit[2]) d[c1 + __popc(m[2] & lt)] = pv[2];
+                            if (hit[3]) d[c2 + __popc(m[3] & lt)] = pv[3];
+                            d += c;
+                            room -= c;
                         }
                     }
                 }
