@@ -130,7 +130,9 @@ __device__ __forceinline__ unsigned above_mask(int lane) {
 template <typename S>
 struct TileArgs {
     Pyr<S> P;
-    Pyr<S> PL;               // pyramid over the ends of intervals >= long_split long
+    Pyr<S> PL;               // pyramid over the long-interval list (intervals >= long_split long)
+    const int32_t* long_pos; // its global positions, in position order
+    const int64_t* long_seg; // first list index of each contig
     int64_t long_split;
     const S* starts;
     int64_t split_len;
@@ -264,7 +266,8 @@ __device__ void block_excl_scan(int32_t* v, int n, int* s_wsum, int* s_sum) {
 // or C would exceed `cap`.  Block-uniform.
 template <typename S>
 __device__ int gather_bfs(const Pyr<S>& P, int64_t lo, int64_t umax, S L, int cap, int32_t* cpos, S* cend,
-                          int32_t* lst, int32_t* cnt, uint32_t* msk, int* s_wsum, int* s_n, int* s_sum) {
+                          int32_t* lst, int32_t* cnt, uint32_t* msk, int* s_wsum, int* s_n, int* s_sum,
+                          const int32_t* remap = nullptr) {
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     if (umax < lo) return 0;
     const int H = P.H;
@@ -275,15 +278,17 @@ __device__ int gather_bfs(const Pyr<S>& P, int64_t lo, int64_t umax, S L, int ca
         if (ok) v = (H == 0) ? P.ends[lane] : P.m[H - 1][lane];
         ok = ok && v >= L;
         const unsigned m = __ballot_sync(kFull, ok);
-        if (ok) {
+        const bool fits = __popc(m) <= cap;  // nothing is written past `cap`
+        if (ok && fits) {
             const int idx = __popc(m & above_mask(lane));
-            ((H & 1) ? lst : cpos)[idx] = lane;
+            ((H & 1) ? lst : cpos)[idx] = (H == 0 && remap) ? remap[lane] : lane;
             if (H == 0) cend[idx] = v;
         }
-        if (lane == 0) *s_n = __popc(m);
+        if (lane == 0) *s_n = fits ? __popc(m) : -1;
     }
     __syncthreads();
     int nf = *s_n;
+    if (nf < 0) return -1;
     for (int h = H; h >= 1; --h) {
         const S* A = (h == 1) ? P.ends : P.m[h - 2];
         const int sh = 5 * (h - 1);
@@ -323,7 +328,7 @@ __device__ int gather_bfs(const Pyr<S>& P, int64_t lo, int64_t umax, S L, int ca
             if ((m >> lane) & 1u) {
                 const int64_t c = ((int64_t)in[f] << 5) + lane;
                 const int idx = cnt[f] + __popc(m & above_mask(lane));
-                out[idx] = (int32_t)c;
+                out[idx] = (h == 1 && remap) ? remap[c] : (int32_t)c;
                 if (h == 1) cend[idx] = A[c];
             }
         }
@@ -370,6 +375,30 @@ __device__ __forceinline__ int64_t warp_first_near(const S* __restrict__ starts,
     }
     const int64_t idx = a + lane;
     const unsigned m = __ballot_sync(kFull, idx < b && near_start<S>(starts[idx], qs, X));
+    return m ? a + __ffs(m) - 1 : b;
+}
+
+// First index in [a, b) of an ascending position list whose position is >= key (b when none).
+// Warp-cooperative 32-ary search over global memory.  Warp-uniform.
+__device__ __forceinline__ int64_t warp_first_pos_geq(const int32_t* __restrict__ pos, int64_t a, int64_t b,
+                                                      int64_t key, int lane) {
+    while (b - a > 32) {
+        const int64_t step = (b - a + 31) >> 5;
+        const int64_t idx = a + lane * step;
+        const unsigned m = __ballot_sync(kFull, idx < b && (int64_t)pos[idx] >= key);
+        if (!m) {
+            const int64_t last = min((int64_t)31, (b - 1 - a) / step);
+            a = a + last * step + 1;
+        } else {
+            const int k = __ffs(m) - 1;
+            if (k == 0) return a;
+            const int64_t na = a + (int64_t)(k - 1) * step + 1, nb = a + (int64_t)k * step;
+            a = na;
+            b = nb;
+        }
+    }
+    const int64_t idx = a + lane;
+    const unsigned m = __ballot_sync(kFull, idx < b && (int64_t)pos[idx] >= key);
     return m ? a + __ffs(m) - 1 : b;
 }
 
@@ -498,6 +527,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_tiles(TileArgs<S> a) {
     S* lend = reinterpret_cast<S*>(cnt);
     S* cstart = (sizeof(S) == 4) ? reinterpret_cast<S*>(msk) : reinterpret_cast<S*>(msk + cap);
     __shared__ int s_tile, s_n, s_sum, s_nlnu, s_next;
+    __shared__ int64_t s_cut[2];
     __shared__ int s_wsum[kWarpsPerCta];
     __shared__ S s_red[kWarpsPerCta], s_red2[kWarpsPerCta];
     __shared__ int32_t s_red3[kWarpsPerCta];
@@ -627,7 +657,26 @@ __global__ void __launch_bounds__(kThreads, 4) k_tiles(TileArgs<S> a) {
                         umx = max(umx, s_red3[w]);
                     }
                     const int64_t umax = umx;
-                    nc = gather_bfs<S>(a.P, lo, umax, L, cap, cpos, cend, lst, cnt, msk, s_wsum, &s_n, &s_sum);
+                    // positions below p_cut hold intervals starting more than long_split before L;
+                    // those that reach L are at least long_split long, so they are gathered from
+                    // the long-interval list instead of the whole position range
+                    if (warp == 0) {
+                        const int64_t pc =
+                            umax < lo ? lo : warp_first_near<S>(a.starts, lo, umax + 1, L, a.long_split, lane);
+                        const int64_t ch = warp_first_pos_geq(a.long_pos, a.long_seg[g], a.long_seg[g + 1], pc, lane);
+                        if (lane == 0) {
+                            s_cut[0] = pc;
+                            s_cut[1] = ch;
+                        }
+                    }
+                    __syncthreads();
+                    const int64_t pcut = s_cut[0], c_lo = a.long_seg[g], c_hi = s_cut[1];
+                    nc = gather_bfs<S>(a.P, pcut, umax, L, cap, cpos, cend, lst, cnt, msk, s_wsum, &s_n, &s_sum);
+                    if (nc >= 0 && c_hi > c_lo) {  // then the long ones below p_cut, still descending
+                        const int nlong = gather_bfs<S>(a.PL, c_lo, c_hi - 1, L, cap - nc, cpos + nc, cend + nc,
+                                                        lst + nc, cnt, msk, s_wsum, &s_n, &s_sum, a.long_pos);
+                        nc = nlong < 0 ? -1 : nc + nlong;
+                    }
                     per_query = nc < 0;
                     if (!per_query && nc > 0) {
                         // long candidates (end - start >= X) into (lpos, lend), in order; the ones
@@ -721,8 +770,16 @@ __global__ void __launch_bounds__(kThreads, 4) k_tiles(TileArgs<S> a) {
                     L = s_red[w] < L ? s_red[w] : L;
                     umx = max(umx, s_red3[w]);
                 }
-                nc = gather_bfs<S>(a.PL, lo, (int64_t)umx, L, cap, cpos, cend, lst, cnt, msk, s_wsum, &s_n,
-                                   &s_sum);
+                if (warp == 0) {
+                    const int64_t ch =
+                        warp_first_pos_geq(a.long_pos, a.long_seg[g], a.long_seg[g + 1], (int64_t)umx + 1, lane);
+                    if (lane == 0) s_cut[1] = ch;
+                }
+                __syncthreads();
+                const int64_t c_lo = a.long_seg[g], c_hi = s_cut[1];
+                nc = c_hi > c_lo ? gather_bfs<S>(a.PL, c_lo, c_hi - 1, L, cap, cpos, cend, lst, cnt, msk, s_wsum,
+                                                 &s_n, &s_sum, a.long_pos)
+                                 : 0;
                 if (nc < 0) {
                     per_query = true;
                     nc = 0;
@@ -1484,7 +1541,9 @@ static int run_tiles(BatchedWorkspace& ws, MapView<S> m, Levels<S> L, int H, int
     a.P = make_pyr<S>(m, L, H);
     a.PL.ends = static_cast<const S*>(ws.long_ends);
     for (int h = 0; h < kMaxLevels; ++h) a.PL.m[h] = static_cast<const S*>(ws.long_lvl[h]);
-    a.PL.H = H;
+    a.PL.H = ws.long_H;
+    a.long_pos = ws.long_pos;
+    a.long_seg = ws.long_seg;
     a.long_split = ws.long_split;
     a.starts = m.starts;
     a.split_len = ws.prm.split_len;

@@ -69,13 +69,17 @@ struct BatchedWorkspace {
     bool cache_ok = false;
     int64_t cache_stride = 0;
     int cache_prm_tile = 0, cache_prm_cap = 0;
-    // pyramid over the ends of intervals at least long_split long (long-query tiles)
+    // long-interval list: global positions and ends of the intervals at least long_split long,
+    // in position order, its max pyramid (long_H levels) and each contig's first list index
     const void* long_ends = nullptr;
+    const int32_t* long_pos = nullptr;
+    const int64_t* long_seg = nullptr;
     const void* long_lvl[kMaxLevels] = {nullptr};
+    int long_H = 0;
     int64_t long_split = 0;
 };
 
-// Interval length from which an interval enters the long-interval pyramid.
+// Interval length from which an interval enters the long-interval list.
 constexpr int64_t kLongIntervalSplit = 65536;
 
 template <typename S>

@@ -131,17 +131,41 @@ __global__ void k_level_max(const S* __restrict__ in, int64_t n_out, int64_t n_o
     out[c] = m;
 }
 
+// Long-interval list: the intervals with end - start >= X, in position order (their global
+// positions and ends), padded with (-1, S_MIN) to a multiple of 32.
 template <typename S>
-__global__ void k_long_ends(const S* __restrict__ starts, const S* __restrict__ ends, int64_t n, int64_t n_pad,
-                            int64_t X, S* __restrict__ out) {
+__device__ __forceinline__ bool long_iv(S s, S e, int64_t X) {
+    return e >= s && (uint64_t)e - (uint64_t)s >= (uint64_t)X;
+}
+
+template <typename S>
+__global__ void k_long_flags(const S* __restrict__ starts, const S* __restrict__ ends, int64_t n, int64_t X,
+                             uint32_t* __restrict__ flags) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n_pad) return;
-    S v = Lim<S>::lo;
-    if (i < n) {
-        const S s = starts[i], e = ends[i];
-        if (e >= s && (uint64_t)e - (uint64_t)s >= (uint64_t)X) v = e;
+    if (i < n) flags[i] = long_iv(starts[i], ends[i], X) ? 1u : 0u;
+}
+
+template <typename S>
+__global__ void k_long_scatter(const S* __restrict__ starts, const S* __restrict__ ends, int64_t n, int64_t X,
+                               const int64_t* __restrict__ offs, int64_t n_long, int64_t n_long_pad,
+                               int32_t* __restrict__ pos, S* __restrict__ lend) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n && long_iv(starts[i], ends[i], X)) {
+        const int64_t k = offs[i];
+        pos[k] = (int32_t)i;
+        lend[k] = ends[i];
     }
-    out[i] = v;
+    if (i >= n_long && i < n_long_pad) {
+        pos[i] = -1;
+        lend[i] = Lim<S>::lo;
+    }
+}
+
+// out[g] = offs[seg[g]]: first long-list index of each contig (g = 0..G)
+__global__ void k_long_seg(const int64_t* __restrict__ offs, const int64_t* __restrict__ seg, int G,
+                           int64_t* __restrict__ out) {
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g <= G) out[g] = offs[seg[g]];
 }
 
 template <typename S>
@@ -294,10 +318,24 @@ cudaError_t launch_pyramid(const S* ends, const int64_t* sizes, int H, S* const*
 }
 
 template <typename S>
-cudaError_t launch_long_ends(const S* starts, const S* ends, int64_t n, int64_t n_pad, int64_t X, S* out,
-                             cudaStream_t st) {
-    if (n_pad <= 0) return cudaSuccess;
-    k_long_ends<S><<<blocks_for(n_pad), kThreads, 0, st>>>(starts, ends, n, n_pad, X, out);
+cudaError_t launch_long_flags(const S* starts, const S* ends, int64_t n, int64_t X, uint32_t* flags,
+                              cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    k_long_flags<S><<<blocks_for(n), kThreads, 0, st>>>(starts, ends, n, X, flags);
+    note_launch();
+    return cudaGetLastError();
+}
+
+template <typename S>
+cudaError_t launch_long_scatter(const S* starts, const S* ends, int64_t n, int64_t X, const int64_t* offs,
+                                int64_t n_long, int64_t n_long_pad, const int64_t* seg, int G, int32_t* pos,
+                                S* lend, int64_t* long_seg, cudaStream_t st) {
+    const int64_t m = std::max(n, n_long_pad);
+    if (m > 0) {
+        k_long_scatter<S><<<blocks_for(m), kThreads, 0, st>>>(starts, ends, n, X, offs, n_long, n_long_pad, pos, lend);
+        note_launch();
+    }
+    k_long_seg<<<blocks_for(G + 1), kThreads, 0, st>>>(offs, seg, G, long_seg);
     note_launch();
     return cudaGetLastError();
 }
@@ -322,7 +360,10 @@ cudaError_t launch_branch(const S* ends, int64_t n, int64_t n_pad, Levels<S> L, 
     template cudaError_t launch_copy_pad<S>(const S*, const S*, const int32_t*, int64_t, int64_t, \
                                             S*, S*, int32_t*, uint32_t*, cudaStream_t);          \
     template cudaError_t launch_pyramid<S>(const S*, const int64_t*, int, S* const*, cudaStream_t); \
-    template cudaError_t launch_long_ends<S>(const S*, const S*, int64_t, int64_t, int64_t, S*, cudaStream_t); \
+    template cudaError_t launch_long_flags<S>(const S*, const S*, int64_t, int64_t, uint32_t*, cudaStream_t); \
+    template cudaError_t launch_long_scatter<S>(const S*, const S*, int64_t, int64_t, const int64_t*, int64_t, \
+                                                int64_t, const int64_t*, int, int32_t*, S*, int64_t*,        \
+                                                cudaStream_t);                                               \
     template cudaError_t launch_branch<S>(const S*, int64_t, int64_t, Levels<S>, int,           \
                                           const int64_t*, int, int32_t*, cudaStream_t);
 SIG_INST(int32_t)

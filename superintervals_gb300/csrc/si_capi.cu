@@ -135,8 +135,11 @@ struct gSuperIntervals {
     int64_t lvl_sizes[sig::kMaxLevels + 1] = {0};
     DevBuf starts, ends, data, branch, seg, perm;
     DevBuf lvl[sig::kMaxLevels];
-    DevBuf ends_long;                  // ends of intervals >= kLongIntervalSplit long, else S_MIN
-    DevBuf lvl_long[sig::kMaxLevels];  // their max pyramid
+    // long-interval list: intervals >= kLongIntervalSplit long, position order, own pyramid
+    DevBuf long_pos, long_end, long_seg;
+    DevBuf long_lvl[sig::kMaxLevels];
+    int64_t long_sizes[sig::kMaxLevels + 1] = {0};
+    int long_H = 0;
     int sort_passes = 0;
     bool input_was_sorted = false;
     // query workspace
@@ -342,16 +345,39 @@ int build_impl(gSuperIntervals* si) {
     SI_CK(sig::launch_pyramid<S>(ends, si->lvl_sizes, si->H, lp, st));
     SI_CK(sig::launch_branch<S>(ends, n, n_pad, levels<S>(si), si->H, si->seg.as<int64_t>(), G,
                                 si->branch.as<int32_t>(), st));
-    // long-interval pyramid (long-query tiles of the batched path)
-    SI_TRY(si->ends_long.reserve(sizeof(S) * n_pad));
-    for (int h = 1; h <= si->H; ++h) SI_TRY(si->lvl_long[h - 1].reserve(sizeof(S) * si->lvl_sizes[h]));
-    SI_CK(sig::launch_long_ends<S>(si->starts.as<S>(), ends, n, n_pad, sig::kLongIntervalSplit,
-                                   si->ends_long.as<S>(), st));
-    S* lpl[sig::kMaxLevels];
-    for (int h = 0; h < sig::kMaxLevels; ++h) lpl[h] = si->lvl_long[h].as<S>();
-    SI_CK(sig::launch_pyramid<S>(si->ends_long.as<S>(), si->lvl_sizes, si->H, lpl, st));
-    si->bws.long_ends = si->ends_long.p;
-    for (int h = 0; h < sig::kMaxLevels; ++h) si->bws.long_lvl[h] = si->lvl_long[h].p;
+    // long-interval list of the batched path: intervals at least kLongIntervalSplit long, in
+    // position order, with their own max pyramid (a tile reaches them without visiting the
+    // positions in between)
+    {
+        DevBuf flags, offs, tmp;
+        SI_TRY(flags.reserve(sizeof(uint32_t) * n));
+        SI_TRY(offs.reserve(sizeof(int64_t) * (n + 1)));
+        SI_TRY(tmp.reserve(sig::scan_temp_bytes(n)));
+        SI_CK(sig::launch_long_flags<S>(si->starts.as<S>(), ends, n, sig::kLongIntervalSplit, flags.as<uint32_t>(),
+                                        st));
+        SI_CK(sig::exclusive_scan_u32_to_i64(flags.as<uint32_t>(), offs.as<int64_t>(), n, tmp.p, st));
+        int64_t n_long = 0;
+        SI_CK(cudaMemcpyAsync(&n_long, offs.as<int64_t>() + n, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+        SI_CK(cudaStreamSynchronize(st));
+        const int64_t n_long_pad = sig::round_up(std::max<int64_t>(n_long, 1), 32);
+        SI_TRY(si->long_pos.reserve(sizeof(int32_t) * n_long_pad));
+        SI_TRY(si->long_end.reserve(sizeof(S) * n_long_pad));
+        SI_TRY(si->long_seg.reserve(sizeof(int64_t) * (G + 1)));
+        si->long_H = sig::pyramid_levels(n_long_pad, si->long_sizes);
+        for (int h = 1; h <= si->long_H; ++h) SI_TRY(si->long_lvl[h - 1].reserve(sizeof(S) * si->long_sizes[h]));
+        SI_CK(sig::launch_long_scatter<S>(si->starts.as<S>(), ends, n, sig::kLongIntervalSplit, offs.as<int64_t>(),
+                                          n_long, n_long_pad, si->seg.as<int64_t>(), G, si->long_pos.as<int32_t>(),
+                                          si->long_end.as<S>(), si->long_seg.as<int64_t>(), st));
+        S* llv[sig::kMaxLevels];
+        for (int h = 0; h < sig::kMaxLevels; ++h) llv[h] = si->long_lvl[h].as<S>();
+        SI_CK(sig::launch_pyramid<S>(si->long_end.as<S>(), si->long_sizes, si->long_H, llv, st));
+        SI_CK(cudaStreamSynchronize(st));  // the temporaries are released on scope exit
+    }
+    si->bws.long_ends = si->long_end.p;
+    si->bws.long_pos = si->long_pos.as<int32_t>();
+    si->bws.long_seg = si->long_seg.as<int64_t>();
+    for (int h = 0; h < sig::kMaxLevels; ++h) si->bws.long_lvl[h] = si->long_lvl[h].p;
+    si->bws.long_H = si->long_H;
     si->bws.long_split = sig::kLongIntervalSplit;
     SI_TRY(sig::batched_prepare<S>(si->bws, view<S>(si), levels<S>(si), si->H, si->lvl_sizes,
                                    si->ub_mode, st));

@@ -126,9 +126,16 @@ cudaError_t launch_pyramid(const S* ends, const int64_t* sizes, int H, S* const*
                            cudaStream_t st);
 // ends of intervals at least X long (end - start >= X), S_MIN for the others: the base of
 // the long-interval pyramid used by the batched path's long-query tiles.
+// long-interval list (end - start >= X) in position order: flags per interval; then, with
+// offs = exclusive scan of the flags (n + 1 entries), the positions and ends of the n_long
+// long intervals padded to n_long_pad, and each contig's first list index (G + 1 entries)
 template <typename S>
-cudaError_t launch_long_ends(const S* starts, const S* ends, int64_t n, int64_t n_pad, int64_t X, S* out,
-                             cudaStream_t st);
+cudaError_t launch_long_flags(const S* starts, const S* ends, int64_t n, int64_t X, uint32_t* flags,
+                              cudaStream_t st);
+template <typename S>
+cudaError_t launch_long_scatter(const S* starts, const S* ends, int64_t n, int64_t X, const int64_t* offs,
+                                int64_t n_long, int64_t n_long_pad, const int64_t* seg, int G, int32_t* pos,
+                                S* lend, int64_t* long_seg, cudaStream_t st);
 template <typename S>
 cudaError_t launch_branch(const S* ends, int64_t n, int64_t n_pad, Levels<S> L, int H,
                           const int64_t* seg, int G, int32_t* branch, cudaStream_t st);
