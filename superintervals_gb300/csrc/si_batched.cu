@@ -270,18 +270,22 @@ __device__ int gather_bfs(const Pyr<S>& P, int64_t lo, int64_t umax, S L, int ca
                           const int32_t* remap = nullptr) {
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     if (umax < lo) return 0;
-    const int H = P.H;
+    // start at the lowest level whose nodes covering [lo, umax] are at most 32 (the top level
+    // always is): the levels above it hold no extra information for this range
+    int H = 0;
+    while (H < P.H && (umax >> (5 * H)) - (lo >> (5 * H)) >= 32) ++H;
     if (warp == 0) {
         const int64_t nlo = lo >> (5 * H), nhi = umax >> (5 * H);
-        bool ok = lane >= nlo && lane <= nhi;
+        const int64_t node = nlo + lane;
+        bool ok = node <= nhi;
         S v = Lim<S>::lo;
-        if (ok) v = (H == 0) ? P.ends[lane] : P.m[H - 1][lane];
+        if (ok) v = (H == 0) ? P.ends[node] : P.m[H - 1][node];
         ok = ok && v >= L;
         const unsigned m = __ballot_sync(kFull, ok);
         const bool fits = __popc(m) <= cap;  // nothing is written past `cap`
         if (ok && fits) {
             const int idx = __popc(m & above_mask(lane));
-            ((H & 1) ? lst : cpos)[idx] = (H == 0 && remap) ? remap[lane] : lane;
+            ((H & 1) ? lst : cpos)[idx] = (H == 0 && remap) ? remap[node] : (int32_t)node;
             if (H == 0) cend[idx] = v;
         }
         if (lane == 0) *s_n = fits ? __popc(m) : -1;
@@ -342,6 +346,14 @@ __device__ int gather_bfs(const Pyr<S>& P, int64_t lo, int64_t umax, S L, int ca
 template <typename S>
 __device__ __forceinline__ bool near_start(S start, S qs, int64_t X) {
     return start >= qs || (uint64_t)qs - (uint64_t)start <= (uint64_t)X;
+}
+
+// The smallest start that near_start accepts: qs - X clamped to the coordinate range, so that
+// near_start(start, qs, X) == (start >= near_threshold(qs, X)).
+template <typename S>
+__device__ __forceinline__ S near_threshold(S qs, int64_t X) {
+    const uint64_t room = (uint64_t)qs - (uint64_t)Lim<S>::lo;  // qs - S_MIN >= 0
+    return (uint64_t)X >= room ? Lim<S>::lo : (S)((uint64_t)qs - (uint64_t)X);
 }
 
 // end - start >= X, without overflow
@@ -817,18 +829,16 @@ __global__ void __launch_bounds__(kThreads, 4) k_tiles(TileArgs<S> a) {
                             else b1 = mid;
                         }
                         const int t0 = b0;
-                        // part A and the head run: candidates whose start is within X of qs
+                        // part A and the head run: candidates whose start is within X of qs, i.e.
+                        // start >= thr (thr = qs - X, clamped to the coordinate range)
+                        const S thr = near_threshold<S>(qs, X);
                         int t = t0;
-                        bool open = true;
-                        while (t < nc && near_start<S>(cstart[t], qs, X)) {
-                            const bool hit = cend[t] >= qs;
-                            c += hit ? 1u : 0u;
-                            if (open) {
-                                if (hit && cpos[t] == u - (t - t0)) ++head;
-                                else open = false;
-                            }
-                            ++t;
-                        }
+                        // the head run: consecutive positions u, u-1, ... that are hits
+                        while (t < nc && cstart[t] >= thr && cend[t] >= qs && cpos[t] == u - (t - t0)) ++t;
+                        head = t - t0;
+                        c = (uint32_t)head;
+                        bool open = t == nc || cstart[t] < thr;  // the head may go on below the split
+                        for (; t < nc && cstart[t] >= thr; ++t) c += cend[t] >= qs ? 1u : 0u;
                         const int tsplit = t;
                         for (; open && t < nc; ++t) {  // a head run reaching into the long candidates
                             if (cpos[t] == u - (t - t0) && cend[t] >= qs) ++head;
@@ -874,7 +884,8 @@ __global__ void __launch_bounds__(kThreads, 4) k_tiles(TileArgs<S> a) {
                         const int h = q_h[i];
                         ta = t0 + (h < nc - t0 ? h : nc - t0);
                         int t = ta;
-                        while (t < nc && near_start<S>(cstart[t], qs, X)) ++t;
+                        const S thr = near_threshold<S>(qs, X);
+                        while (t < nc && cstart[t] >= thr) ++t;
                         tsplit = t;
                         const int tb = max(tsplit, ta);
                         if (tb < nc && nl > 0) {
@@ -971,17 +982,27 @@ __global__ void __launch_bounds__(kThreads, 4) k_tiles(TileArgs<S> a) {
                         }
                     } else {
                         // 128 candidates per round as four independent 32-wide slices, so their
-                        // shared-memory reads and ballots overlap instead of chaining
+                        // shared-memory reads and ballots overlap instead of chaining; only the
+                        // last round checks the list end
                         for (int kk = lb; kk < nl; kk += 128) {
                             bool hit[4];
                             int32_t pv[4];
                             unsigned m[4];
+                            if (kk + 128 <= nl) {
 #pragma unroll
-                            for (int s = 0; s < 4; ++s) {
-                                const int tt = kk + 32 * s + lane;
-                                const bool in = tt < nl;
-                                hit[s] = in && lend[tt] >= qs;
-                                pv[s] = in ? lpos[tt] : 0;
+                                for (int s = 0; s < 4; ++s) {
+                                    const int tt = kk + 32 * s + lane;
+                                    hit[s] = lend[tt] >= qs;
+                                    pv[s] = lpos[tt];
+                                }
+                            } else {
+#pragma unroll
+                                for (int s = 0; s < 4; ++s) {
+                                    const int tt = kk + 32 * s + lane;
+                                    const bool in = tt < nl;
+                                    hit[s] = in && lend[tt] >= qs;
+                                    pv[s] = in ? lpos[tt] : 0;
+                                }
                             }
 #pragma unroll
                             for (int s = 0; s < 4; ++s) m[s] = __ballot_sync(kFull, hit[s]);
