@@ -10,6 +10,7 @@ reference's published timings use BED files that are not available here).
                   [--path batched|plain] [--ub learned|eytzinger|binary]
   python bench.py --impl reference ...   # the reference algorithm on the host cores
   python bench.py --config config4       # --op upper_bound: learned vs Eytzinger vs binary
+  python bench.py --config config5       # serving loop: Poisson requests, p50/p99 latency
 
 Prints one JSON line.  `value` = queries/s with inputs resident in HBM;
 `e2e` = the same through the C-ABI with pinned host buffers (H2D of the
@@ -36,6 +37,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = ("overlap queries/s + result pairs/s on 1 GB300; % HBM peak; batched+learned vs plain")
+METRIC_SERVE = "serving loop on 1 GB300: queries/s (saturated) and p50/p99 request latency at the offered rate"
 METRIC_UB = "upper-bound queries/s on 1 GB300: learned two-stage index vs binary search, bit-identical"
 PEAK_FALLBACK_GBS = 6800.0
 
@@ -47,7 +49,9 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", default="config3",
-                    choices=["config1", "config2", "config3", "config4"])
+                    choices=["config1", "config2", "config3", "config4", "config5"])
+    ap.add_argument("--requests", type=int, default=600, help="config5: requests in the stream")
+    ap.add_argument("--rate", type=float, default=200.0, help="config5: offered requests/s (Poisson)")
     ap.add_argument("--scale", type=float, default=1.0, help="shrink N and Q (tests only)")
     ap.add_argument("--path", default="batched", choices=["batched", "plain", "auto"])
     ap.add_argument("--ub", default="learned", choices=["learned", "eytzinger", "binary"])
@@ -491,6 +495,166 @@ def ub_line(args, res, world):
     return line
 
 
+# ----------------------------------------------------------------------------- serving loop
+def serving_workload(args):
+    from superintervals_gb300 import workloads as W
+    n = max(100_000, int(200_000_000 * args.scale))
+    wl = W.config5_index(n=n)
+    max_size = max(1000, int(1_000_000 * args.scale))
+    nreq = max(20, int(args.requests * min(1.0, 10 * args.scale)))
+    arrival, sizes, qc, qs, qe = W.config5_requests(nreq, rate_per_s=args.rate, max_size=max_size)
+    return wl, arrival - arrival[0], sizes, qc, qs, qe
+
+
+def run_serving(args, rank, world, dist):
+    """A device-resident index answers a stream of requests.  Requests arrive by a seeded
+    Poisson process; the loop takes every request that has arrived (up to a batch cap and
+    the free device memory) as one batch through the host-buffer C-ABI call
+    (searchBatchIntoGpu: H2D of the queries, count -> scan -> emit, D2H of the CSR result)
+    and a request's latency runs from its arrival to its results in host memory."""
+    from superintervals_gb300 import _capi
+    from superintervals_gb300.interval_map import GpuIndex
+    lib = _capi.load()
+    wl, arrival, sizes, qc, qs, qe = serving_workload(args)
+    idx = GpuIndex(32, 0)
+    idx.add_arrays(wl.starts, wl.ends, wl.data, seg=wl.seg)
+    t0 = time.perf_counter()
+    idx.build()
+    build_s = time.perf_counter() - t0
+    nreq = len(sizes)
+    roff = np.zeros(nreq + 1, np.int64)
+    np.cumsum(sizes, out=roff[1:])
+    nq_all = int(roff[-1])
+
+    def pinned(nbytes):
+        p = C.c_void_p()
+        _capi.check(lib.hostMallocPinnedGpu(C.byref(p), max(int(nbytes), 1)))
+        return p
+    hq = [pinned(a.nbytes) for a in (qs, qe, qc)]
+    for p, a in zip(hq, (qs, qe, qc)):
+        C.memmove(p, a.ctypes.data, a.nbytes)
+    max_batch = max(1_000_000, int(8_000_000 * min(1.0, 10 * args.scale)))
+    h_off = pinned(8 * (max_batch + 1 + int(sizes.max())))
+    cap = [max(1 << 20, 120 * max_batch)]
+    h_out = [pinned(4 * cap[0])]
+    idx.set_output_budget(16 << 30)
+    free_b, tot_b = C.c_size_t(0), C.c_size_t(0)
+    total = C.c_size_t(0)
+
+    def serve(path, ub, saturate):
+        idx.set_path(path)
+        idx.set_upper_bound(ub)
+        lat = np.zeros(nreq)
+        pairs = 0
+        hits_per_q = 100.0
+        batches = 0
+        k0 = lib.getLaunchCountGpu()
+        start = time.perf_counter()
+        r = 0
+        while r < nreq:
+            now = time.perf_counter() - start
+            if not saturate and arrival[r] > now:
+                time.sleep(min(arrival[r] - now, 0.0005))
+                continue
+            # admission: arrived requests, at most max_batch queries, and no more than half of
+            # the free device memory at the current hits-per-query estimate
+            _capi.check(lib.deviceMemInfoGpu(0, C.byref(free_b), C.byref(tot_b)))
+            per_q = 48 + 4 * hits_per_q
+            room = min(max_batch, int(0.5 * free_b.value / per_q))
+            r1 = r + 1
+            while r1 < nreq and (saturate or arrival[r1] <= now) and roff[r1 + 1] - roff[r] <= room:
+                r1 += 1
+            q0, nq = int(roff[r]), int(roff[r1] - roff[r])
+            args_ = [idx.h] + [C.c_void_p(p.value + a.itemsize * q0) for p, a in zip(hq, (qs, qe, qc))] + \
+                    [nq, 0, 0, h_off]
+            st = lib.searchBatchIntoGpu(*args_, h_out[0], cap[0], C.byref(total))
+            if st == _capi.SI_ERR_CAPACITY:
+                lib.hostFreePinnedGpu(h_out[0])
+                cap[0] = int(total.value * 1.25) + 1
+                h_out[0] = pinned(4 * cap[0])
+                st = lib.searchBatchIntoGpu(*args_, h_out[0], cap[0], C.byref(total))
+            _capi.check(st)
+            done = time.perf_counter() - start
+            lat[r:r1] = done - (0.0 if saturate else arrival[r:r1])
+            pairs += int(total.value)
+            hits_per_q = max(1.0, 0.8 * hits_per_q + 0.2 * total.value / max(nq, 1))
+            batches += 1
+            r = r1
+        wall = time.perf_counter() - start
+        return {"queries_per_s": nq_all / wall, "pairs_per_s": pairs / wall, "wall_s": wall, "batches": batches,
+                "p50_ms": 1e3 * float(np.percentile(lat, 50)), "p99_ms": 1e3 * float(np.percentile(lat, 99)),
+                "launches": lib.getLaunchCountGpu() - k0, "pairs": pairs}
+
+    res = {"wl": wl, "build_s": build_s, "nreq": nreq, "nq": nq_all, "sizes": sizes, "qs": qs, "qe": qe, "qc": qc}
+    with ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) as clk:
+        serve(_capi.PATH_BATCHED, _capi.UB_LEARNED, True)               # warm-up
+        res["batched_sat"] = serve(_capi.PATH_BATCHED, _capi.UB_LEARNED, True)
+        res["batched_rate"] = serve(_capi.PATH_BATCHED, _capi.UB_LEARNED, False)
+    res["clocks"] = clk.summary()
+    if not args.no_plain:
+        res["plain_sat"] = serve(_capi.PATH_PLAIN, _capi.UB_BINARY, True)
+        res["plain_rate"] = serve(_capi.PATH_PLAIN, _capi.UB_BINARY, False)
+    for p in hq + [h_off, h_out[0]]:
+        lib.hostFreePinnedGpu(p)
+    idx.close()
+    return res
+
+
+def serving_line(args, res, world):
+    b, br = res["batched_sat"], res["batched_rate"]
+    wl = res["wl"]
+    line = {"metric": METRIC_SERVE, "value": world * b["queries_per_s"], "unit": "queries/s", "n_gpus": world,
+            "steps": res["nreq"], "warmup": 1, "ms_per_step": 1e3 * b["wall_s"] / res["nreq"],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
+            "data": "synthetic (seeded)",
+            "config": {"workload": f"serving n={wl.n} int32 24 contigs, {res['nreq']} Poisson requests "
+                                   f"({res['nq']} queries, sizes log-uniform), offered {args.rate}/s",
+                       "n_intervals": wl.n, "requests": res["nreq"], "queries": res["nq"],
+                       "op": "search_idxs (C++ order) per request batch", "path": "batched + learned",
+                       "inputs": "queries from pinned host memory; results to pinned host memory"},
+            "latency_ms": {"offered_rate_per_s": args.rate, "p50": br["p50_ms"], "p99": br["p99_ms"],
+                           "queries_per_s": br["queries_per_s"], "batches": br["batches"]},
+            "saturated": {"p50_ms": b["p50_ms"], "p99_ms": b["p99_ms"], "batches": b["batches"],
+                          "pairs_per_s": b["pairs_per_s"]},
+            "build_s": res["build_s"], "clocks": res["clocks"], "gpu_launches": b["launches"],
+            "e2e": {"value": world * b["queries_per_s"], "unit": "queries/s",
+                    "h2d_bytes_per_step": int(12 * res["nq"] / max(b["batches"], 1)),
+                    "d2h_bytes_per_step": int((8 * res["nq"] + 4 * b["pairs"]) / max(b["batches"], 1))}}
+    if "plain_sat" in res:
+        p, pr = res["plain_sat"], res["plain_rate"]
+        line["plain_gpu"] = {"queries_per_s": p["queries_per_s"], "p50_ms": pr["p50_ms"], "p99_ms": pr["p99_ms"],
+                             "saturated_speedup": b["queries_per_s"] / p["queries_per_s"]}
+    if not args.no_cpu:
+        nth = host_threads()
+        c = serving_cpu(wl, res["qs"], res["qe"], res["qc"], args.cpu_seconds, nth)
+        line["cpu_baseline"] = {"value": c["q_per_s"], "unit": "queries/s", "cores": nth, "kind": "port",
+                                "sample": c["sample"]}
+    return line
+
+
+def serving_cpu(wl, qs, qe, qc, seconds, nth):
+    """The oracle port over the three smallest contigs of the resident index and the stream's
+    queries on them (building the whole 200 M-interval index on the host takes minutes)."""
+    from superintervals_gb300.workloads import Workload
+    G = len(wl.seg) - 1
+    lens = np.array([c[1] for c in wl.contigs])
+    pick = np.sort(np.argsort(lens)[:3])
+    parts = [np.arange(wl.seg[g], wl.seg[g + 1]) for g in pick]
+    sel = np.concatenate(parts)
+    seg = np.zeros(len(pick) + 1, np.int64)
+    seg[1:] = np.cumsum([len(x) for x in parts])
+    remap = np.full(G, -1, np.int32)
+    remap[pick] = np.arange(len(pick), dtype=np.int32)
+    qmask = remap[qc] >= 0
+    sub = Workload(name="serving sample", starts=wl.starts[sel], ends=wl.ends[sel], data=wl.data[sel], seg=seg,
+                   q_starts=qs[qmask][:2_000_000], q_ends=qe[qmask][:2_000_000],
+                   q_contig=remap[qc[qmask]][:2_000_000], contigs=[wl.contigs[g] for g in pick])
+    c = cpu_run(sub, seconds, nth)
+    c["sample"] = (f"{c['sample_q']} queries of the request stream on {len(pick)} contigs "
+                   f"({len(sel)} intervals), search_idxs C++ order ({c['pairs']} pairs), {nth} threads")
+    return c
+
+
 # ----------------------------------------------------------------------------- CPU arm
 def cpu_run(wl, seconds, nthreads):
     """The reference algorithm (oracle port, oracle/si_oracle.c) on the host
@@ -537,6 +701,24 @@ def main():
     rank, world, dist = init_dist(args)
     cfg = args.config
     op = args.op or ("upper_bound" if cfg == "config4" else "search_idxs")
+    if args.impl == "reference" and cfg == "config5":
+        if rank != 0:
+            return
+        wl, arrival, sizes, qc, qs, qe = serving_workload(args)
+        nth = host_threads()
+        runs = [serving_cpu(wl, qs, qe, qc, args.cpu_seconds / max(1, args.steps), nth) for _ in range(args.steps)]
+        qps = statistics.median(r["q_per_s"] for r in runs)
+        line = {"metric": METRIC_SERVE, "value": qps, "unit": "queries/s", "impl": "reference", "n_gpus": 1,
+                "steps": args.steps, "warmup": 0,
+                "ms_per_step": 1000.0 * statistics.median(r["seconds"] for r in runs),
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
+                "data": "synthetic (seeded)",
+                "config": {"workload": f"serving n={wl.n} int32 24 contigs", "op": "search_idxs (C++ order)"},
+                "cpu_baseline": {"value": qps, "unit": "queries/s", "cores": nth, "kind": "port",
+                                 "sample": runs[0]["sample"]},
+                "e2e": {"value": qps, "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+        return
     if args.impl == "reference" and op == "upper_bound":
         if rank != 0:
             return
@@ -589,6 +771,11 @@ def main():
         print(json.dumps(line), flush=True)
         return
 
+    if cfg == "config5":
+        res = run_serving(args, rank, world, dist)
+        if rank == 0:
+            print(json.dumps(serving_line(args, res, world)), flush=True)
+        return
     if op == "upper_bound":
         res = run_gpu_ub(args, rank, world, dist)
         if rank == 0:

@@ -144,6 +144,8 @@ int getPhaseTimesGpu(const gSuperIntervals* si, double* ms, int64_t* calls);
 /* Process-wide cap on device bytes the library allocates (0 = no cap). */
 int setDeviceBudgetGpu(size_t bytes);
 size_t deviceBytesInUseGpu(void);
+/* Free and total device memory of `device` (admission control of a serving loop). */
+int deviceMemInfoGpu(int device, size_t* free_bytes, size_t* total_bytes);
 
 /* ---- batch queries with HOST buffers.  coordinates: int32 (handle made with
  *      32) or the _i64 forms; qcontig may be NULL (all contig 0). ---------- */

@@ -83,6 +83,7 @@ SIGNATURES = {
     "getPhaseTimesGpu": (_I, [_H, _P, _P]),
     "setDeviceBudgetGpu": (_I, [_SZ]),
     "deviceBytesInUseGpu": (_SZ, []),
+    "deviceMemInfoGpu": (_I, [_I, C.POINTER(_SZ), C.POINTER(_SZ)]),
     "countOverlapsBatchGpu": (_I, [_H, _P, _P, _P, _SZ, _P]),
     "countOverlapsBatchGpu_i64": (_I, [_H, _P, _P, _P, _SZ, _P]),
     "anyOverlapsBatchGpu": (_I, [_H, _P, _P, _P, _SZ, _P]),

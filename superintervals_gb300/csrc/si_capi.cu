@@ -801,6 +801,15 @@ int setDeviceBudgetGpu(size_t bytes) {
 }
 size_t deviceBytesInUseGpu(void) { return g_used.load(); }
 
+int deviceMemInfoGpu(int device, size_t* free_bytes, size_t* total_bytes) {
+    SI_CK(cudaSetDevice(device));
+    size_t f = 0, t = 0;
+    SI_CK(cudaMemGetInfo(&f, &t));
+    if (free_bytes) *free_bytes = f;
+    if (total_bytes) *total_bytes = t;
+    return SI_OK;
+}
+
 int countOverlapsBatchGpu(gSuperIntervals* si, const int32_t* qs, const int32_t* qe, const int32_t* qc,
                           size_t nq, uint32_t* counts) {
     return count_host<int32_t>(si, qs, qe, qc, nq, counts);

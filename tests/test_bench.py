@@ -21,7 +21,7 @@ def _run(args, env=None, timeout=600):
     return [json.loads(l) for l in lines]
 
 
-@pytest.mark.parametrize("cfg", ["config1", "config4"])
+@pytest.mark.parametrize("cfg", ["config1", "config4", "config5"])
 def test_reference_arm_line(cfg):
     (line,) = _run(["--impl", "reference", "--config", cfg, "--scale", "0.001", "--steps", "2",
                     "--warmup", "1", "--cpu-seconds", "0.5"])
@@ -32,6 +32,7 @@ def test_reference_arm_line(cfg):
     assert line["value"] > 0 and line["e2e"]["h2d_bytes_per_step"] == 0
     assert line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["cores"] >= 1
     assert line["config"]["op"] == ("upper_bound" if cfg == "config4" else "search_idxs (C++ order)")
+    assert "cores" in line["cpu_baseline"] and "sample" in line["cpu_baseline"]
 
 
 def test_reference_arm_two_ranks_prints_once():
@@ -97,3 +98,12 @@ def test_bench_upper_bound_line_gpu():
     assert line["oracle_sample_identical"]
     assert all(v["identical_to_binary"] for v in line["providers"].values())
     assert line["gpu_launches"] == 3 and "e2e" in line and "cpu_baseline" in line
+
+
+@pytest.mark.gpu
+def test_bench_serving_line_gpu():
+    (line,) = _run(["--config", "config5", "--scale", "0.005", "--requests", "60", "--rate", "2000",
+                    "--cpu-seconds", "0.5"])
+    assert line["value"] > 0 and line["gpu_launches"] > 0
+    assert 0 < line["latency_ms"]["p50"] <= line["latency_ms"]["p99"]
+    assert "plain_gpu" in line and "cpu_baseline" in line and "e2e" in line
