@@ -587,9 +587,10 @@ def run_serving(args, rank, world, dist):
 
     res = {"wl": wl, "build_s": build_s, "nreq": nreq, "nq": nq_all, "sizes": sizes, "qs": qs, "qe": qe, "qc": qc}
     with ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) as clk:
-        serve(_capi.PATH_BATCHED, _capi.UB_LEARNED, True)               # warm-up
-        res["batched_sat"] = serve(_capi.PATH_BATCHED, _capi.UB_LEARNED, True)
-        res["batched_rate"] = serve(_capi.PATH_BATCHED, _capi.UB_LEARNED, False)
+        # the library picks the batched path for batches of 4096+ queries and the plain one below
+        serve(_capi.PATH_AUTO, _capi.UB_LEARNED, True)               # warm-up
+        res["batched_sat"] = serve(_capi.PATH_AUTO, _capi.UB_LEARNED, True)
+        res["batched_rate"] = serve(_capi.PATH_AUTO, _capi.UB_LEARNED, False)
     res["clocks"] = clk.summary()
     if not args.no_plain:
         res["plain_sat"] = serve(_capi.PATH_PLAIN, _capi.UB_BINARY, True)
@@ -610,7 +611,8 @@ def serving_line(args, res, world):
             "config": {"workload": f"serving n={wl.n} int32 24 contigs, {res['nreq']} Poisson requests "
                                    f"({res['nq']} queries, sizes log-uniform), offered {args.rate}/s",
                        "n_intervals": wl.n, "requests": res["nreq"], "queries": res["nq"],
-                       "op": "search_idxs (C++ order) per request batch", "path": "batched + learned",
+                       "op": "search_idxs (C++ order) per request batch",
+                       "path": "auto (batched for 4096+ queries, else plain) + learned upper bound",
                        "inputs": "queries from pinned host memory; results to pinned host memory"},
             "latency_ms": {"offered_rate_per_s": args.rate, "p50": br["p50_ms"], "p99": br["p99_ms"],
                            "queries_per_s": br["queries_per_s"], "batches": br["batches"]},

@@ -251,6 +251,28 @@ int differenceDeviceGpu(gSuperIntervals* si, const void* d_qs, const void* d_qe,
                         const int32_t* d_qcontig, size_t nq, int64_t* d_offsets, void* d_starts,
                         void* d_ends, size_t capacity, size_t* total, void* stream);
 
+/* ---- keys and coverage ------------------------------------------------- */
+/* search_keys (superintervals.hpp:913-938; order SI_ORDER_DESC) / searchKeys
+ * (c_superintervals.h:217) and the Python search_keys / search_items
+ * (intervalmap.pyx:302-345; order SI_ORDER_IDXS_CPP): each hit's start and end
+ * (and payload when data is not NULL), CSR over the queries.  With too small a
+ * capacity: SI_ERR_CAPACITY, *total set, offsets filled. */
+int searchKeysBatchGpu(gSuperIntervals* si, const void* qs, const void* qe, const int32_t* qcontig,
+                       size_t nq, int order, int64_t* offsets, void* starts, void* ends, int32_t* data,
+                       size_t capacity, size_t* total);
+int searchKeysDeviceGpu(gSuperIntervals* si, const void* d_qs, const void* d_qe,
+                        const int32_t* d_qcontig, size_t nq, int order, int64_t* d_offsets,
+                        void* d_starts, void* d_ends, int32_t* d_data, size_t capacity,
+                        size_t* total, void* stream);
+/* coverage (superintervals.hpp:979-1006, intervalmap.pyx:347-361): per query the
+ * number of overlapping intervals and the sum of min(end, qe) - max(start, qs)
+ * over them (no +1), in the coordinate type (wrapping on overflow). */
+int coverageBatchGpu(gSuperIntervals* si, const void* qs, const void* qe, const int32_t* qcontig,
+                     size_t nq, uint64_t* count, void* covered);
+int coverageDeviceGpu(gSuperIntervals* si, const void* d_qs, const void* d_qe,
+                      const int32_t* d_qcontig, size_t nq, uint64_t* d_count, void* d_covered,
+                      void* stream);
+
 /* ---- result helpers: createIndexResult / clearIndexResult /
  *      destroyIndexResult (c_superintervals.h:339-343, 1070-1075) --------- */
 cCsrResult createCsrResult(void);

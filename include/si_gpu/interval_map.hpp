@@ -8,9 +8,10 @@
 //   * add (hpp:95-105), reserve, clear, size, build (hpp:112-130), at;
 //   * count (hpp:651-825), has_overlaps (hpp:865-871), search_idxs (hpp:879-905, appends in the
 //     C++ order), search_values (hpp:551-579, appends, descending), search_keys (hpp:913-938),
-//     upper_bound (hpp:501-516);
+//     coverage (hpp:979-1006), upper_bound (hpp:501-516);
 //   * batch forms modelled on the Cython ones (intervalmap.pyx:363-494): count_batch,
-//     search_idxs_batch, search_values_batch, returning CSR (offsets + flat values).
+//     search_idxs_batch, search_values_batch, search_keys_batch (CSR: offsets + flat values) and
+//     coverage_batch.
 // S is int32_t or int64_t; T is any copyable payload, kept on the host and permuted with the
 // intervals exactly as the reference permutes its data vector (stable order inside exact
 // (start, end) duplicates, where the reference's std::sort order is unspecified).
@@ -148,18 +149,19 @@ public:
     void search_keys(S start, S end, std::vector<std::pair<S, S>>& found) const {
         if (starts.empty()) return;
         std::vector<int64_t> off;
-        std::vector<int32_t> val;
-        search_into(&start, &end, 1, SI_ORDER_DESC, off, val);
-        for (int32_t v : val) found.emplace_back(starts[(size_t)v], ends[(size_t)v]);
+        std::vector<S> ks, ke;
+        keys_into(&start, &end, 1, SI_ORDER_DESC, off, ks, ke);
+        for (size_t k = 0; k < ks.size(); ++k) found.emplace_back(ks[k], ke[k]);
     }
     // hpp:979-1006: adds the number of overlaps and the sum of min(end) - max(start) (no +1)
     void coverage(S start, S end, std::pair<size_t, S>& cov_result) const {
-        std::vector<std::pair<S, S>> keys;
-        search_keys(start, end, keys);
-        for (const auto& k : keys) {
-            ++cov_result.first;
-            cov_result.second += (k.second < end ? k.second : end) - (k.first > start ? k.first : start);
-        }
+        if (starts.empty()) return;
+        uint64_t c = 0;
+        S v = 0;
+        need();
+        check(coverageBatchGpu(h_, &start, &end, nullptr, 1, &c, &v));
+        cov_result.first += (size_t)c;
+        cov_result.second += v;
     }
     // hpp:501-516: last index with starts[idx] <= value, SIZE_MAX when none
     size_t upper_bound(S value) const {
@@ -183,6 +185,20 @@ public:
     void search_idxs_batch(const S* qs, const S* qe, size_t nq, std::vector<int64_t>& offsets,
                            std::vector<int32_t>& values) const {
         search_into(qs, qe, nq, SI_ORDER_IDXS_CPP, offsets, values);
+    }
+    // CSR of each hit's (start, end), in the order of search_keys (fully descending)
+    void search_keys_batch(const S* qs, const S* qe, size_t nq, std::vector<int64_t>& offsets,
+                           std::vector<S>& key_starts, std::vector<S>& key_ends) const {
+        keys_into(qs, qe, nq, SI_ORDER_DESC, offsets, key_starts, key_ends);
+    }
+    // per query: number of overlaps and the sum of overlapping lengths (coverage, no +1)
+    void coverage_batch(const S* qs, const S* qe, size_t nq, std::vector<uint64_t>& counts,
+                        std::vector<S>& covered) const {
+        counts.assign(nq, 0);
+        covered.assign(nq, 0);
+        if (starts.empty() || nq == 0) return;
+        need();
+        check(coverageBatchGpu(h_, qs, qe, nullptr, nq, counts.data(), covered.data()));
     }
     void search_values_batch(const S* qs, const S* qe, size_t nq, std::vector<int64_t>& offsets,
                              std::vector<T>& values) const {
@@ -219,6 +235,24 @@ private:
         else
             check(countOverlapsBatchGpu_i64(h_, reinterpret_cast<const int64_t*>(qs),
                                             reinterpret_cast<const int64_t*>(qe), nullptr, nq, out));
+    }
+    void keys_into(const S* qs, const S* qe, size_t nq, int order, std::vector<int64_t>& offsets,
+                   std::vector<S>& ks, std::vector<S>& ke) const {
+        offsets.assign(nq + 1, 0);
+        ks.clear();
+        ke.clear();
+        if (starts.empty() || nq == 0) return;
+        need();
+        size_t total = 0;
+        int st = searchKeysBatchGpu(h_, qs, qe, nullptr, nq, order, offsets.data(), nullptr, nullptr, nullptr, 0,
+                                    &total);
+        if (st == SI_ERR_CAPACITY) {
+            ks.resize(total);
+            ke.resize(total);
+            st = searchKeysBatchGpu(h_, qs, qe, nullptr, nq, order, offsets.data(), ks.data(), ke.data(), nullptr,
+                                    total, &total);
+        }
+        check(st);
     }
     void search_into(const S* qs, const S* qe, size_t nq, int order, std::vector<int64_t>& offsets,
                      std::vector<int32_t>& values) const {

@@ -102,6 +102,10 @@ SIGNATURES = {
     "intersectDeviceGpu": (_I, [_H, _P, _P, _P, _SZ, _I, _P, _P, _P, _P, _SZ, C.POINTER(_SZ), _P]),
     "differenceBatchGpu": (_I, [_H, _P, _P, _P, _SZ, _P, _P, _P, _SZ, C.POINTER(_SZ)]),
     "differenceDeviceGpu": (_I, [_H, _P, _P, _P, _SZ, _P, _P, _P, _SZ, C.POINTER(_SZ), _P]),
+    "searchKeysBatchGpu": (_I, [_H, _P, _P, _P, _SZ, _I, _P, _P, _P, _P, _SZ, C.POINTER(_SZ)]),
+    "searchKeysDeviceGpu": (_I, [_H, _P, _P, _P, _SZ, _I, _P, _P, _P, _P, _SZ, C.POINTER(_SZ), _P]),
+    "coverageBatchGpu": (_I, [_H, _P, _P, _P, _SZ, _P, _P]),
+    "coverageDeviceGpu": (_I, [_H, _P, _P, _P, _SZ, _P, _P, _P]),
     "createCsrResult": (cCsrResult, []),
     "clearCsrResult": (None, [C.POINTER(cCsrResult)]),
     "destroyCsrResult": (None, [C.POINTER(cCsrResult)]),

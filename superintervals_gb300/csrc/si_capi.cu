@@ -1530,3 +1530,160 @@ extern "C" int differenceBatchGpu(gSuperIntervals* si, const void* qs, const voi
     return setop_host<int32_t>(si, (const int32_t*)qs, (const int32_t*)qe, qc, nq, 1, 0, offsets,
                                (int32_t*)starts, (int32_t*)ends, nullptr, capacity, total);
 }
+
+// =====================================================================================
+// Key gathers and coverage over the hit lists.
+// =====================================================================================
+namespace {
+
+// Hit lists of a device batch (so_hoff / so_hits); an empty index gives empty lists.
+template <typename S>
+int lists_or_empty(gSuperIntervals* si, const sig::QueryBatch& q, int order, cudaStream_t st, int64_t* P) {
+    SI_TRY(si->w_err.reserve(sizeof(int)));
+    if (si->n > 0) {
+        SI_TRY(hit_lists<S>(si, q, order, st));
+        SI_CK(cudaMemcpyAsync(P, si->so_hoff.as<int64_t>() + q.nq, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+        SI_CK(cudaStreamSynchronize(st));
+    } else {
+        SI_TRY(si->so_hoff.reserve(sizeof(int64_t) * (q.nq + 1)));
+        SI_TRY(si->so_hits.reserve(sizeof(int32_t)));
+        SI_CK(cudaMemsetAsync(si->so_hoff.p, 0, sizeof(int64_t) * (q.nq + 1), st));
+        *P = 0;
+    }
+    return SI_OK;
+}
+
+template <typename S>
+int keys_device(gSuperIntervals* si, const sig::QueryBatch& q, int order, int64_t* d_off, S* d_s, S* d_e,
+                int32_t* d_d, size_t cap, size_t* total, cudaStream_t st) {
+    SI_TRY(check_built(si));
+    SI_TRY(set_dev(si));
+    SI_TRY(check_order(order));
+    if (!d_off || (q.nq && (!q.qs || !q.qe))) return fail(SI_ERR_INVALID, "null device buffer");
+    if (total) *total = 0;
+    if (q.nq == 0) {
+        SI_CK(cudaMemsetAsync(d_off, 0, sizeof(int64_t), st));
+        SI_CK(cudaStreamSynchronize(st));
+        return SI_OK;
+    }
+    int64_t P = 0;
+    SI_TRY(lists_or_empty<S>(si, q, order, st, &P));
+    SI_CK(cudaMemcpyAsync(d_off, si->so_hoff.p, sizeof(int64_t) * (q.nq + 1), cudaMemcpyDeviceToDevice, st));
+    if (total) *total = (size_t)P;
+    if ((size_t)P > cap) {
+        SI_CK(cudaStreamSynchronize(st));
+        return fail(SI_ERR_CAPACITY, "output needs %lld keys, capacity %zu", (long long)P, cap);
+    }
+    if (P > 0) {
+        if (!d_s || !d_e) return fail(SI_ERR_INVALID, "null output buffer");
+        SI_CK(sig::launch_keys<S>(view<S>(si), q, si->so_hoff.as<int64_t>(), si->so_hits.as<int32_t>(), d_s, d_e,
+                                  d_d, st));
+    }
+    SI_CK(cudaStreamSynchronize(st));
+    SI_CK(cudaGetLastError());
+    return SI_OK;
+}
+
+template <typename S>
+int coverage_device(gSuperIntervals* si, const sig::QueryBatch& q, uint64_t* d_count, S* d_cov, cudaStream_t st) {
+    SI_TRY(check_built(si));
+    SI_TRY(set_dev(si));
+    if (q.nq && (!q.qs || !q.qe || !d_count || !d_cov)) return fail(SI_ERR_INVALID, "null device buffer");
+    if (q.nq == 0) return SI_OK;
+    int64_t P = 0;
+    SI_TRY(lists_or_empty<S>(si, q, SI_ORDER_DESC, st, &P));
+    SI_CK(sig::launch_coverage<S>(view<S>(si), q, si->so_hoff.as<int64_t>(), si->so_hits.as<int32_t>(), d_count,
+                                  d_cov, st));
+    SI_CK(cudaStreamSynchronize(st));
+    SI_CK(cudaGetLastError());
+    return SI_OK;
+}
+
+}  // namespace
+
+extern "C" int searchKeysDeviceGpu(gSuperIntervals* si, const void* d_qs, const void* d_qe, const int32_t* d_qc,
+                                   size_t nq, int order, int64_t* d_offsets, void* d_starts, void* d_ends,
+                                   int32_t* d_data, size_t capacity, size_t* total, void* stream) {
+    SI_TRY(check_built(si));
+    cudaStream_t st = stream ? (cudaStream_t)stream : si->st;
+    sig::QueryBatch q{d_qs, d_qe, d_qc, (int64_t)nq};
+    if (si->bits == 64)
+        return keys_device<int64_t>(si, q, order, d_offsets, (int64_t*)d_starts, (int64_t*)d_ends, d_data, capacity,
+                                    total, st);
+    return keys_device<int32_t>(si, q, order, d_offsets, (int32_t*)d_starts, (int32_t*)d_ends, d_data, capacity,
+                                total, st);
+}
+
+extern "C" int searchKeysBatchGpu(gSuperIntervals* si, const void* qs, const void* qe, const int32_t* qc, size_t nq,
+                                  int order, int64_t* offsets, void* starts, void* ends, int32_t* data,
+                                  size_t capacity, size_t* total) {
+    SI_TRY(check_built(si));
+    SI_TRY(set_dev(si));
+    if (!offsets) return fail(SI_ERR_INVALID, "null offsets");
+    const size_t sb = si->bits / 8;
+    sig::QueryBatch q;
+    int r = si->bits == 64 ? upload_queries<int64_t>(si, (const int64_t*)qs, (const int64_t*)qe, qc, nq, q)
+                           : upload_queries<int32_t>(si, (const int32_t*)qs, (const int32_t*)qe, qc, nq, q);
+    SI_TRY(r);
+    SI_TRY(si->so_off.reserve(sizeof(int64_t) * (nq + 1)));
+    size_t T = 0;
+    r = si->bits == 64 ? keys_device<int64_t>(si, q, order, si->so_off.as<int64_t>(), nullptr, nullptr, nullptr, 0,
+                                              &T, si->st)
+                       : keys_device<int32_t>(si, q, order, si->so_off.as<int64_t>(), nullptr, nullptr, nullptr, 0,
+                                              &T, si->st);
+    if (r != SI_OK && r != SI_ERR_CAPACITY) return r;
+    if (total) *total = T;
+    SI_CK(cudaMemcpyAsync(offsets, si->so_off.p, sizeof(int64_t) * (nq + 1), cudaMemcpyDeviceToHost, si->st));
+    SI_CK(cudaStreamSynchronize(si->st));
+    if (T > capacity) return fail(SI_ERR_CAPACITY, "output needs %zu keys, capacity %zu", T, capacity);
+    if (T == 0) return SI_OK;
+    if (!starts || !ends) return fail(SI_ERR_INVALID, "null output buffer");
+    SI_TRY(si->so_os.reserve(sb * T));
+    SI_TRY(si->so_oe.reserve(sb * T));
+    if (data) SI_TRY(si->so_ob.reserve(sizeof(int32_t) * T));
+    // the hit lists are still in place: gather only
+    if (si->bits == 64)
+        SI_CK(sig::launch_keys<int64_t>(view<int64_t>(si), q, si->so_hoff.as<int64_t>(), si->so_hits.as<int32_t>(),
+                                        si->so_os.as<int64_t>(), si->so_oe.as<int64_t>(),
+                                        data ? si->so_ob.as<int32_t>() : nullptr, si->st));
+    else
+        SI_CK(sig::launch_keys<int32_t>(view<int32_t>(si), q, si->so_hoff.as<int64_t>(), si->so_hits.as<int32_t>(),
+                                        si->so_os.as<int32_t>(), si->so_oe.as<int32_t>(),
+                                        data ? si->so_ob.as<int32_t>() : nullptr, si->st));
+    SI_CK(cudaMemcpyAsync(starts, si->so_os.p, sb * T, cudaMemcpyDeviceToHost, si->st));
+    SI_CK(cudaMemcpyAsync(ends, si->so_oe.p, sb * T, cudaMemcpyDeviceToHost, si->st));
+    if (data) SI_CK(cudaMemcpyAsync(data, si->so_ob.p, sizeof(int32_t) * T, cudaMemcpyDeviceToHost, si->st));
+    SI_CK(cudaStreamSynchronize(si->st));
+    return SI_OK;
+}
+
+extern "C" int coverageDeviceGpu(gSuperIntervals* si, const void* d_qs, const void* d_qe, const int32_t* d_qc,
+                                 size_t nq, uint64_t* d_count, void* d_cov, void* stream) {
+    SI_TRY(check_built(si));
+    cudaStream_t st = stream ? (cudaStream_t)stream : si->st;
+    sig::QueryBatch q{d_qs, d_qe, d_qc, (int64_t)nq};
+    if (si->bits == 64) return coverage_device<int64_t>(si, q, d_count, (int64_t*)d_cov, st);
+    return coverage_device<int32_t>(si, q, d_count, (int32_t*)d_cov, st);
+}
+
+extern "C" int coverageBatchGpu(gSuperIntervals* si, const void* qs, const void* qe, const int32_t* qc, size_t nq,
+                                uint64_t* count, void* cov) {
+    SI_TRY(check_built(si));
+    SI_TRY(set_dev(si));
+    if (nq && (!count || !cov)) return fail(SI_ERR_INVALID, "null output");
+    const size_t sb = si->bits / 8;
+    sig::QueryBatch q;
+    int r = si->bits == 64 ? upload_queries<int64_t>(si, (const int64_t*)qs, (const int64_t*)qe, qc, nq, q)
+                           : upload_queries<int32_t>(si, (const int32_t*)qs, (const int32_t*)qe, qc, nq, q);
+    SI_TRY(r);
+    if (nq == 0) return SI_OK;
+    SI_TRY(si->so_off.reserve(sizeof(uint64_t) * nq));
+    SI_TRY(si->so_os.reserve(sb * nq));
+    r = si->bits == 64 ? coverage_device<int64_t>(si, q, si->so_off.as<uint64_t>(), si->so_os.as<int64_t>(), si->st)
+                       : coverage_device<int32_t>(si, q, si->so_off.as<uint64_t>(), si->so_os.as<int32_t>(), si->st);
+    SI_TRY(r);
+    SI_CK(cudaMemcpyAsync(count, si->so_off.p, sizeof(uint64_t) * nq, cudaMemcpyDeviceToHost, si->st));
+    SI_CK(cudaMemcpyAsync(cov, si->so_os.p, sb * nq, cudaMemcpyDeviceToHost, si->st));
+    SI_CK(cudaStreamSynchronize(si->st));
+    return SI_OK;
+}

@@ -170,6 +170,14 @@ cudaError_t launch_isect(MapView<S> m, QueryBatch q, const int64_t* hoff, const 
 template <typename S>
 cudaError_t launch_diff(MapView<S> m, QueryBatch q, const int64_t* hoff, const int32_t* hits, bool sequential,
                         uint32_t* counts, const int64_t* ooff, S* os, S* oe, int* d_err, cudaStream_t st);
+// the hits' (start, end, data) in hit-list order (od may be null)
+template <typename S>
+cudaError_t launch_keys(MapView<S> m, QueryBatch q, const int64_t* hoff, const int32_t* hits, S* os, S* oe,
+                        int32_t* od, cudaStream_t st);
+// per query: number of hits and the wrapped sum of min(end, qe) - max(start, qs)
+template <typename S>
+cudaError_t launch_coverage(MapView<S> m, QueryBatch q, const int64_t* hoff, const int32_t* hits,
+                            uint64_t* count, S* cov, cudaStream_t st);
 // flag = 1 when some interval has start > end
 template <typename S>
 cudaError_t launch_any_inverted(MapView<S> m, int* flag, cudaStream_t st);

@@ -1,5 +1,6 @@
-// si_setops.cu -- batch set operations of a list of intervals (map A, given as queries) against
-// the index (map B), built on the hit lists of the search path.
+// si_setops.cu -- operations over the hit lists of the search path (CSR of contig-local
+// positions): batch set operations of a list of intervals (map A, given as queries) against the
+// index (map B), key gathers and coverage.
 //
 //   intersection (src/superintervals.hpp:1158-1177, src/c_superintervals.h:921-940): for query
 //     interval [qs, qe] and each hit h in the search order, the piece
@@ -18,6 +19,7 @@
 // order.  A covered piece reaching the type's maximum ends the sweep (the reference's
 // cursor = end + 1 overflows there).
 #include <algorithm>
+#include <type_traits>
 #include "si_internal.cuh"
 
 namespace sig {
@@ -213,6 +215,65 @@ __global__ void __launch_bounds__(kThreads) k_diff(MapView<S> m, const S* __rest
     }
 }
 
+// search_keys / search_items (hpp:913-938, pyx:302-345): the hits' (start, end[, data]) in
+// hit-list order.  One warp per query.
+template <typename S>
+__global__ void __launch_bounds__(kThreads) k_keys(MapView<S> m, const int32_t* __restrict__ qc, int64_t nq,
+                                                   const int64_t* __restrict__ hoff,
+                                                   const int32_t* __restrict__ hits, S* __restrict__ os,
+                                                   S* __restrict__ oe, int32_t* __restrict__ od) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warps = (int64_t)gridDim.x * kWarpsPerBlock;
+    for (int64_t q = (int64_t)blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5); q < nq; q += warps) {
+        const int g = qc ? qc[q] : 0;  // reported by the search that made the lists
+        if (g < 0 || g >= m.G) continue;
+        const int64_t lo = m.seg[g];
+        for (int64_t p = hoff[q] + lane; p < hoff[q + 1]; p += 32) {
+            const int64_t k = lo + hits[p];
+            os[p] = m.starts[k];
+            oe[p] = m.ends[k];
+            if (od) od[p] = m.data[k];
+        }
+    }
+}
+
+// coverage (hpp:979-1006, pyx:347-361): per query the number of hits and the sum of
+// min(end, qe) - max(start, qs) over them (no +1), accumulated in the coordinate type with
+// two's-complement wrap.  One warp per query.
+template <typename S>
+__global__ void __launch_bounds__(kThreads) k_coverage(MapView<S> m, const S* __restrict__ qs,
+                                                       const S* __restrict__ qe, const int32_t* __restrict__ qc,
+                                                       int64_t nq, const int64_t* __restrict__ hoff,
+                                                       const int32_t* __restrict__ hits,
+                                                       uint64_t* __restrict__ count, S* __restrict__ cov) {
+    using U = typename std::make_unsigned<S>::type;
+    const int lane = threadIdx.x & 31;
+    const int64_t warps = (int64_t)gridDim.x * kWarpsPerBlock;
+    for (int64_t q = (int64_t)blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5); q < nq; q += warps) {
+        const int g = qc ? qc[q] : 0;
+        if (g < 0 || g >= m.G) {  // reported by the search that made the lists (no hits)
+            if (lane == 0) {
+                count[q] = 0;
+                cov[q] = 0;
+            }
+            continue;
+        }
+        const int64_t lo = m.seg[g];
+        const S s0 = qs[q], e0 = qe[q];
+        U acc = 0;
+        for (int64_t p = hoff[q] + lane; p < hoff[q + 1]; p += 32) {
+            const int64_t k = lo + hits[p];
+            acc += (U)smin(m.ends[k], e0) - (U)smax(m.starts[k], s0);
+        }
+#pragma unroll
+        for (int d = 16; d > 0; d >>= 1) acc += __shfl_xor_sync(kFull, acc, d);
+        if (lane == 0) {
+            count[q] = (uint64_t)(hoff[q + 1] - hoff[q]);
+            cov[q] = (S)acc;
+        }
+    }
+}
+
 template <typename S>
 __global__ void k_any_inverted(const S* __restrict__ starts, const S* __restrict__ ends, int64_t n,
                                int* __restrict__ flag) {
@@ -264,6 +325,26 @@ cudaError_t launch_diff(MapView<S> m, QueryBatch q, const int64_t* hoff, const i
 }
 
 template <typename S>
+cudaError_t launch_keys(MapView<S> m, QueryBatch q, const int64_t* hoff, const int32_t* hits, S* os, S* oe,
+                        int32_t* od, cudaStream_t st) {
+    if (q.nq <= 0) return cudaSuccess;
+    k_keys<S><<<warp_blocks(q.nq), kThreads, 0, st>>>(m, q.qc, q.nq, hoff, hits, os, oe, od);
+    note_launch();
+    return cudaGetLastError();
+}
+
+template <typename S>
+cudaError_t launch_coverage(MapView<S> m, QueryBatch q, const int64_t* hoff, const int32_t* hits,
+                            uint64_t* count, S* cov, cudaStream_t st) {
+    if (q.nq <= 0) return cudaSuccess;
+    k_coverage<S><<<warp_blocks(q.nq), kThreads, 0, st>>>(m, static_cast<const S*>(q.qs),
+                                                           static_cast<const S*>(q.qe), q.qc, q.nq, hoff, hits,
+                                                           count, cov);
+    note_launch();
+    return cudaGetLastError();
+}
+
+template <typename S>
 cudaError_t launch_any_inverted(MapView<S> m, int* flag, cudaStream_t st) {
     cudaError_t e = cudaMemsetAsync(flag, 0, sizeof(int), st);
     if (e != cudaSuccess || m.n <= 0) return e;
@@ -278,7 +359,11 @@ cudaError_t launch_any_inverted(MapView<S> m, int* flag, cudaStream_t st) {
                                          const int64_t*, S*, S*, int32_t*, int*, cudaStream_t);               \
     template cudaError_t launch_diff<S>(MapView<S>, QueryBatch, const int64_t*, const int32_t*, bool,         \
                                         uint32_t*, const int64_t*, S*, S*, int*, cudaStream_t);               \
-    template cudaError_t launch_any_inverted<S>(MapView<S>, int*, cudaStream_t);
+    template cudaError_t launch_any_inverted<S>(MapView<S>, int*, cudaStream_t);                          \
+    template cudaError_t launch_keys<S>(MapView<S>, QueryBatch, const int64_t*, const int32_t*, S*, S*,        \
+                                        int32_t*, cudaStream_t);                                              \
+    template cudaError_t launch_coverage<S>(MapView<S>, QueryBatch, const int64_t*, const int32_t*,            \
+                                            uint64_t*, S*, cudaStream_t);
 SIG_SINST(int32_t)
 SIG_SINST(int64_t)
 

@@ -183,6 +183,37 @@ class GpuIndex:
         k = int(total.value)
         return off, bufs[0][:k], bufs[1][:k], bufs[2][:k]
 
+    def search_keys(self, qs, qe, qc=None, order=ORDER_DESC, with_data=False):
+        """search_keys (superintervals.hpp:913-938) / search_items: CSR offsets, each
+        hit's start and end (and payload with ``with_data``), in ``order``."""
+        qs, qe, qc = self._queries(qs, qe, qc)
+        nq = qs.shape[0]
+        off = np.empty(nq + 1, np.int64)
+        total = C.c_size_t(0)
+        cap = 0
+        bufs = (np.empty(1, self.dtype), np.empty(1, self.dtype), np.empty(1, np.int32))
+        for _ in range(2):
+            st = self.lib.searchKeysBatchGpu(self.h, _p(qs), _p(qe), _p(qc), nq, int(order), _p(off), _p(bufs[0]),
+                                             _p(bufs[1]), _p(bufs[2]) if with_data else None, cap,
+                                             C.byref(total))
+            if st == _capi.SI_ERR_CAPACITY:
+                cap = int(total.value)
+                bufs = (np.empty(cap, self.dtype), np.empty(cap, self.dtype), np.empty(cap, np.int32))
+                continue
+            check(st)
+            break
+        k = int(total.value)
+        return (off, bufs[0][:k], bufs[1][:k]) + ((bufs[2][:k],) if with_data else ())
+
+    def coverage(self, qs, qe, qc=None):
+        """coverage (superintervals.hpp:979-1006) per query: (count uint64, covered)."""
+        qs, qe, qc = self._queries(qs, qe, qc)
+        nq = qs.shape[0]
+        cnt = np.empty(nq, np.uint64)
+        cov = np.empty(nq, self.dtype)
+        check(self.lib.coverageBatchGpu(self.h, _p(qs), _p(qe), _p(qc), nq, _p(cnt), _p(cov)))
+        return cnt, cov
+
     def intersect(self, qs, qe, qc=None, order=ORDER_IDXS_CPP):
         """intersection (superintervals.hpp:1158-1177) of the query intervals (another
         map's) with this index: CSR offsets, piece starts, piece ends and the hit's
@@ -241,6 +272,7 @@ class IntervalMap:
         s, e, perm, _ = idx.arrays()
         self._idx = idx
         self._sorted = (s, e, perm)
+        self._by_input = self._values  # the device payload of an interval is its index here
         self._values = [self._values[p] for p in perm.tolist()] if n else []
         self._starts, self._ends = s.tolist(), e.tolist()
 
@@ -294,10 +326,28 @@ class IntervalMap:
         return self.search_values_batch([start], [end])[0] if self.size() else []
 
     def search_keys(self, start: int, end: int) -> list:
-        return [(self._starts[i], self._ends[i]) for i in self.search_idxs(start, end)]
+        self._need()
+        if not self.size():
+            return []
+        _, s, e = self._idx.search_keys([start], [end], order=ORDER_IDXS_CPP)
+        return list(zip(s.tolist(), e.tolist()))
 
     def search_items(self, start: int, end: int) -> list:
-        return [(self._starts[i], self._ends[i], self._values[i]) for i in self.search_idxs(start, end)]
+        self._need()
+        if not self.size():
+            return []
+        _, s, e, d = self._idx.search_keys([start], [end], order=ORDER_IDXS_CPP, with_data=True)
+        v = self._by_input
+        return [(a, b, v[p]) for a, b, p in zip(s.tolist(), e.tolist(), d.tolist())]
+
+    def coverage(self, start: int, end: int):
+        """(count, covered) as pyx:347-361: the number of overlapping intervals and the sum
+        of their overlapping lengths min(end) - max(start) (no +1)."""
+        self._need()
+        if not self.size():
+            return 0, 0
+        cnt, cov = self._idx.coverage([start], [end])
+        return int(cnt[0]), int(cov[0])
 
     # batch queries (pyx:363-494)
     @staticmethod

@@ -137,6 +137,17 @@ int batch_readme() {  // src/superintervals/README.md:16-27
     std::vector<const char*> vals;
     imap.search_values_batch(qs, qe, 3, off, vals);
     CHECK(vals[1][0] == 'B' && vals[2][0] == 'A');
+    // keys in search_keys order (descending) and coverage (no +1), batch and single
+    std::vector<int32_t> ks, ke;
+    imap.search_keys_batch(qs, qe, 3, off, ks, ke);
+    CHECK(off[3] == 4 && ks[1] == 15 && ke[1] == 25 && ks[2] == 10 && ke[3] == 40);
+    std::vector<uint64_t> cc;
+    std::vector<int32_t> cv;
+    imap.coverage_batch(qs, qe, 3, cc, cv);
+    CHECK(cc[0] == 1 && cv[0] == 2 && cc[1] == 2 && cv[1] == 2 + 4 && cc[2] == 1 && cv[2] == 5);
+    std::pair<size_t, int32_t> one{0, 0};
+    imap.coverage(18, 22, one);
+    CHECK(one.first == 2 && one.second == 6);
     return 0;
 }
 

@@ -1,6 +1,8 @@
-"""GPU parity of the set operations (intersection / difference of map A against the
-index B) through the C-ABI: against the golden fixtures made by the reference's
-own C++ class and C API, and against the oracle on seeded multi-contig inputs."""
+"""GPU parity of the operations over hit lists through the C-ABI: set operations
+(intersection / difference of map A against the index B), key gathers
+(search_keys / search_items) and coverage.  Against the golden fixtures made by the
+reference's own C++ class and C API, and against the oracle on seeded multi-contig
+inputs."""
 import ctypes as C
 
 import numpy as np
@@ -181,3 +183,55 @@ def test_python_intervalmap_setops(api):
     got = A.difference(B)
     want = sorted(zip(g["ref_diff_starts"].tolist(), g["ref_diff_ends"].tolist(), g["ref_diff_data"].tolist()))
     assert sorted(got.at(i) for i in range(got.size())) == want
+
+
+@pytest.mark.parametrize("name", fixture_names())
+def test_keys_and_coverage_fixture_parity(api, name):
+    """search_keys (both orders) and coverage against the reference's own outputs."""
+    g = load(name)
+    idx = _index(api, g["starts"], g["ends"], g["data"], path="batched")
+    rs, re_ = g["ref_sorted_starts"], g["ref_sorted_ends"]
+    qs, qe = g["q_starts"], g["q_ends"]
+    off, s, e = idx.search_keys(qs, qe, order=api.ORDER_IDXS_CPP)
+    assert np.array_equal(off, g["ref_search_idxs_off"])
+    pos = g["ref_search_idxs"].astype(np.int64)
+    assert np.array_equal(s, rs[pos]) and np.array_equal(e, re_[pos])
+    cnt, cov = idx.coverage(qs, qe)
+    assert np.array_equal(cnt.astype(np.int64), g["ref_coverage_count"].astype(np.int64))
+    assert np.array_equal(cov, g["ref_coverage"].astype(cov.dtype))
+    if "ref_c_search_idxs" in g:      # the fully descending order
+        off, s, e = idx.search_keys(qs, qe, order=api.ORDER_DESC)
+        pos = g["ref_c_search_idxs"].astype(np.int64)
+        assert np.array_equal(s, rs[pos]) and np.array_equal(e, re_[pos])
+    idx.close()
+
+
+def test_keys_and_coverage_multicontig(api, oracle):
+    from superintervals_gb300 import workloads as W
+    wl = W.config3(n=100_000, nq=20_000, contigs=W.HUMAN_CONTIGS[20:24])
+    idx = _index(api, wl.starts, wl.ends, wl.data, seg=wl.seg, path="batched")
+    bs, be, bd, _ = idx.arrays()
+    off, out = idx.search(wl.q_starts, wl.q_ends, wl.q_contig, order=api.ORDER_DESC)
+    koff, ks, ke, kd = idx.search_keys(wl.q_starts, wl.q_ends, wl.q_contig, order=api.ORDER_DESC, with_data=True)
+    glo = wl.seg[wl.q_contig].repeat(np.diff(off)) + out    # global positions of the hits
+    assert np.array_equal(koff, off)
+    assert np.array_equal(ks, bs[glo]) and np.array_equal(ke, be[glo]) and np.array_equal(kd, bd[glo])
+    cnt, cov = idx.coverage(wl.q_starts, wl.q_ends, wl.q_contig)
+    for gi in range(len(wl.seg) - 1):
+        lo, hi = int(wl.seg[gi]), int(wl.seg[gi + 1])
+        m = oracle.build(wl.starts[lo:hi], wl.ends[lo:hi], wl.data[lo:hi])
+        sel = np.nonzero(wl.q_contig == gi)[0][:500]
+        rc, rv = oracle.coverage(m, wl.q_starts[sel], wl.q_ends[sel])
+        assert np.array_equal(cnt[sel].astype(np.int64), rc) and np.array_equal(cov[sel], rv)
+    idx.close()
+
+
+def test_python_keys_items_coverage(api):
+    """The Python mirror's single-query search_keys / search_items / coverage (pyx:302-361)."""
+    g = load("kat_coverage_int32")
+    imap = api.IntervalMap.from_arrays(g["starts"], g["ends"], ["v%d" % i for i in g["data"].tolist()])
+    q0, q1 = int(g["q_starts"][0]), int(g["q_ends"][0])
+    assert imap.coverage(q0, q1) == (int(g["ref_coverage_count"][0]), int(g["ref_coverage"][0]))
+    idxs = imap.search_idxs(q0, q1)
+    assert imap.search_keys(q0, q1) == [(imap.starts_at(i), imap.ends_at(i)) for i in idxs]
+    assert imap.search_items(q0, q1) == [imap.at(i) for i in idxs]
