@@ -106,6 +106,20 @@ int indexSuperIntervalsGpu(gSuperIntervals* si);
 int getIndexArraysGpu(const gSuperIntervals* si, void* starts, void* ends, int32_t* data,
                       int64_t* branch);
 
+/* ---- index image: the counterpart of the Rust crate's serde derive on
+ *      IntervalMap (superintervals.rs:35-44) ---------------------------------
+ * One flat little-endian byte image of a built index: header, contig offsets,
+ * sorted starts / ends / payloads, branch array.  serializeIndexGpu writes it
+ * into buf (SI_ERR_CAPACITY with the size in *size when cap is too small);
+ * deserializeIndexGpu replaces the handle's intervals with the image's and
+ * indexes them without sorting (the coordinate width must match the handle's;
+ * a corrupt image is rejected with SI_ERR_INVALID).  save/load do the same
+ * through a file. */
+int serializeIndexGpu(const gSuperIntervals* si, void* buf, size_t cap, size_t* size);
+int deserializeIndexGpu(gSuperIntervals* si, const void* buf, size_t len);
+int saveIndexGpu(const gSuperIntervals* si, const char* path);
+int loadIndexGpu(gSuperIntervals* si, const char* path);
+
 /* ---- options (no reference counterpart) ------------------------------- */
 int setQueryPathGpu(gSuperIntervals* si, int path);
 int setUpperBoundModeGpu(gSuperIntervals* si, int mode);

@@ -73,6 +73,10 @@ SIGNATURES = {
     "numContigsGpu": (_SZ, [_H]),
     "indexSuperIntervalsGpu": (_I, [_H]),
     "getIndexArraysGpu": (_I, [_H, _P, _P, _P, _P]),
+    "serializeIndexGpu": (_I, [_H, _P, _SZ, C.POINTER(_SZ)]),
+    "deserializeIndexGpu": (_I, [_H, _P, _SZ]),
+    "saveIndexGpu": (_I, [_H, C.c_char_p]),
+    "loadIndexGpu": (_I, [_H, C.c_char_p]),
     "setQueryPathGpu": (_I, [_H, _I]),
     "setUpperBoundModeGpu": (_I, [_H, _I]),
     "setOutputBudgetGpu": (_I, [_H, _SZ]),

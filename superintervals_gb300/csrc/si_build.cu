@@ -161,6 +161,15 @@ __global__ void k_long_scatter(const S* __restrict__ starts, const S* __restrict
     }
 }
 
+// flag = 1 when a[i] != b[i] for some i < n
+__global__ void k_differs_i32(const int32_t* __restrict__ a, const int32_t* __restrict__ b, int64_t n,
+                              int* __restrict__ flag) {
+    bool d = false;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        d = d || a[i] != b[i];
+    if (__any_sync(kFull, d) && (threadIdx.x & 31) == 0) atomicOr(flag, 1);
+}
+
 // out[g] = offs[seg[g]]: first long-list index of each contig (g = 0..G)
 __global__ void k_long_seg(const int64_t* __restrict__ offs, const int64_t* __restrict__ seg, int G,
                            int64_t* __restrict__ out) {
@@ -336,6 +345,14 @@ cudaError_t launch_long_scatter(const S* starts, const S* ends, int64_t n, int64
         note_launch();
     }
     k_long_seg<<<blocks_for(G + 1), kThreads, 0, st>>>(offs, seg, G, long_seg);
+    note_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t launch_differs_i32(const int32_t* a, const int32_t* b, int64_t n, int* flag, cudaStream_t st) {
+    cudaError_t e = cudaMemsetAsync(flag, 0, sizeof(int), st);
+    if (e != cudaSuccess || n <= 0) return e;
+    k_differs_i32<<<(unsigned)std::min<int64_t>(blocks_for(n), 152 * 8), kThreads, 0, st>>>(a, b, n, flag);
     note_launch();
     return cudaGetLastError();
 }

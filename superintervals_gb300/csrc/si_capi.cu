@@ -1687,3 +1687,153 @@ extern "C" int coverageBatchGpu(gSuperIntervals* si, const void* qs, const void*
     SI_CK(cudaStreamSynchronize(si->st));
     return SI_OK;
 }
+
+// =====================================================================================
+// Index image: the built index as one flat little-endian byte image -- header, contig
+// offsets, the sorted starts / ends / payloads and the branch array -- the counterpart of the
+// Rust crate's serde derive on IntervalMap (src/superintervals.rs:35-44).  Loading puts the
+// image's (already sorted) intervals into staging and indexes them: the sortedness check
+// skips the radix sort, the cheap passes (pyramid, branch, long-interval list, upper-bound
+// model) run again, and the recomputed branch array must equal the stored one.
+// =====================================================================================
+namespace {
+
+constexpr char kImageMagic[8] = {'S', 'I', 'G', 'P', 'U', 'I', 'X', '1'};
+constexpr uint32_t kImageVersion = 1;
+
+struct ImageHeader {
+    char magic[8];
+    uint32_t version;
+    uint32_t coord_bits;
+    uint64_t n;
+    uint64_t n_contigs;
+};
+
+inline size_t pad8(size_t x) { return (x + 7) & ~(size_t)7; }
+
+size_t image_bytes(int bits, uint64_t n, uint64_t G) {
+    const size_t sb = (size_t)bits / 8;
+    return sizeof(ImageHeader) + 8 * (G + 1) + 2 * pad8(sb * n) + 2 * pad8(4 * n);
+}
+
+template <typename S>
+int deserialize_impl(gSuperIntervals* si, const ImageHeader& h, const unsigned char* p) {
+    const uint64_t n = h.n, G = h.n_contigs;
+    const int64_t* seg = reinterpret_cast<const int64_t*>(p);
+    p += 8 * (G + 1);
+    if (seg[0] != 0 || seg[G] != (int64_t)n) return fail(SI_ERR_INVALID, "index image: bad contig offsets");
+    for (uint64_t g = 0; g < G; ++g)
+        if (seg[g + 1] < seg[g]) return fail(SI_ERR_INVALID, "index image: contig offsets decrease");
+    const S* st = reinterpret_cast<const S*>(p);
+    p += pad8(sizeof(S) * n);
+    const S* en = reinterpret_cast<const S*>(p);
+    p += pad8(sizeof(S) * n);
+    const int32_t* da = reinterpret_cast<const int32_t*>(p);
+    p += pad8(4 * n);
+    const int32_t* br = reinterpret_cast<const int32_t*>(p);
+    hs<S>(si).assign(st, st + n);
+    he<S>(si).assign(en, en + n);
+    si->hdata.assign(da, da + n);
+    si->hseg.clear();
+    if (G > 1) si->hseg.assign(seg, seg + G + 1);
+    si->built = false;
+    SI_TRY(build_impl<S>(si));
+    if (n == 0) return SI_OK;
+    DevBuf tmp, flag;
+    SI_TRY(tmp.reserve(4 * n));
+    SI_TRY(flag.reserve(sizeof(int)));
+    SI_CK(cudaMemcpyAsync(tmp.p, br, 4 * n, cudaMemcpyHostToDevice, si->st));
+    SI_CK(sig::launch_differs_i32(tmp.as<int32_t>(), si->branch.as<int32_t>(), (int64_t)n, flag.as<int>(), si->st));
+    int differs = 0;
+    SI_CK(cudaMemcpyAsync(&differs, flag.p, sizeof(int), cudaMemcpyDeviceToHost, si->st));
+    SI_CK(cudaStreamSynchronize(si->st));
+    if (!si->input_was_sorted || differs) {
+        si->built = false;
+        return fail(SI_ERR_INVALID, "index image: intervals are not in index order or the branch array differs");
+    }
+    return SI_OK;
+}
+
+}  // namespace
+
+extern "C" int serializeIndexGpu(const gSuperIntervals* si, void* buf, size_t cap, size_t* size) {
+    SI_TRY(check_built(si));
+    SI_TRY(set_dev(si));
+    const uint64_t n = (uint64_t)si->n, G = (uint64_t)si->G;
+    const size_t need = image_bytes(si->bits, n, G);
+    if (size) *size = need;
+    if (!buf || cap < need) return fail(SI_ERR_CAPACITY, "index image needs %zu bytes, capacity %zu", need, cap);
+    unsigned char* p = static_cast<unsigned char*>(buf);
+    memset(p, 0, need);
+    ImageHeader h;
+    memcpy(h.magic, kImageMagic, 8);
+    h.version = kImageVersion;
+    h.coord_bits = (uint32_t)si->bits;
+    h.n = n;
+    h.n_contigs = G;
+    memcpy(p, &h, sizeof(h));
+    p += sizeof(h);
+    std::vector<int64_t> segv = si->hseg;
+    if (segv.empty()) segv = {0, (int64_t)n};
+    memcpy(p, segv.data(), 8 * (G + 1));
+    p += 8 * (G + 1);
+    const size_t sb = (size_t)si->bits / 8;
+    if (n) {
+        SI_CK(cudaMemcpyAsync(p, si->starts.p, sb * n, cudaMemcpyDeviceToHost, si->st));
+        p += pad8(sb * n);
+        SI_CK(cudaMemcpyAsync(p, si->ends.p, sb * n, cudaMemcpyDeviceToHost, si->st));
+        p += pad8(sb * n);
+        SI_CK(cudaMemcpyAsync(p, si->data.p, 4 * n, cudaMemcpyDeviceToHost, si->st));
+        p += pad8(4 * n);
+        SI_CK(cudaMemcpyAsync(p, si->branch.p, 4 * n, cudaMemcpyDeviceToHost, si->st));
+        SI_CK(cudaStreamSynchronize(si->st));
+    }
+    return SI_OK;
+}
+
+extern "C" int deserializeIndexGpu(gSuperIntervals* si, const void* buf, size_t len) {
+    if (!si) return fail(SI_ERR_INVALID, "null handle");
+    if (!buf || len < sizeof(ImageHeader)) return fail(SI_ERR_INVALID, "index image too short");
+    ImageHeader h;
+    memcpy(&h, buf, sizeof(h));
+    if (memcmp(h.magic, kImageMagic, 8) != 0) return fail(SI_ERR_INVALID, "not an index image");
+    if (h.version != kImageVersion) return fail(SI_ERR_INVALID, "index image version %u unsupported", h.version);
+    if ((int)h.coord_bits != si->bits)
+        return fail(SI_ERR_INVALID, "index image has %u-bit coordinates, the handle %d-bit", h.coord_bits, si->bits);
+    if (h.n >= ((uint64_t)1 << 31) || h.n_contigs < 1 || h.n_contigs > ((uint64_t)1 << 24))
+        return fail(SI_ERR_INVALID, "index image sizes out of range");
+    if (len < image_bytes(si->bits, h.n, h.n_contigs)) return fail(SI_ERR_INVALID, "index image truncated");
+    SI_TRY(set_dev(si));
+    const unsigned char* p = static_cast<const unsigned char*>(buf) + sizeof(h);
+    if (si->bits == 64) return deserialize_impl<int64_t>(si, h, p);
+    return deserialize_impl<int32_t>(si, h, p);
+}
+
+extern "C" int saveIndexGpu(const gSuperIntervals* si, const char* path) {
+    SI_TRY(check_built(si));
+    if (!path) return fail(SI_ERR_INVALID, "null path");
+    size_t need = 0;
+    serializeIndexGpu(si, nullptr, 0, &need);
+    std::vector<unsigned char> img(need);
+    SI_TRY(serializeIndexGpu(si, img.data(), img.size(), &need));
+    FILE* f = fopen(path, "wb");
+    if (!f) return fail(SI_ERR_INVALID, "cannot open %s for writing", path);
+    const size_t w = fwrite(img.data(), 1, img.size(), f);
+    const int c = fclose(f);
+    if (w != img.size() || c != 0) return fail(SI_ERR_INVALID, "writing %s failed", path);
+    return SI_OK;
+}
+
+extern "C" int loadIndexGpu(gSuperIntervals* si, const char* path) {
+    if (!si || !path) return fail(SI_ERR_INVALID, "null argument");
+    FILE* f = fopen(path, "rb");
+    if (!f) return fail(SI_ERR_INVALID, "cannot open %s", path);
+    std::vector<unsigned char> img;
+    unsigned char chunk[1 << 16];
+    size_t r;
+    while ((r = fread(chunk, 1, sizeof(chunk), f)) > 0) img.insert(img.end(), chunk, chunk + r);
+    const bool bad = ferror(f) != 0;
+    fclose(f);
+    if (bad) return fail(SI_ERR_INVALID, "reading %s failed", path);
+    return deserializeIndexGpu(si, img.data(), img.size());
+}

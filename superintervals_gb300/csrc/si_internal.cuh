@@ -136,6 +136,8 @@ template <typename S>
 cudaError_t launch_long_scatter(const S* starts, const S* ends, int64_t n, int64_t X, const int64_t* offs,
                                 int64_t n_long, int64_t n_long_pad, const int64_t* seg, int G, int32_t* pos,
                                 S* lend, int64_t* long_seg, cudaStream_t st);
+// flag = 1 when a[i] != b[i] for some i < n
+cudaError_t launch_differs_i32(const int32_t* a, const int32_t* b, int64_t n, int* flag, cudaStream_t st);
 template <typename S>
 cudaError_t launch_branch(const S* ends, int64_t n, int64_t n_pad, Levels<S> L, int H,
                           const int64_t* seg, int G, int32_t* branch, cudaStream_t st);

@@ -9,6 +9,7 @@
 from __future__ import annotations
 
 import ctypes as C
+import os
 from typing import Optional
 
 import numpy as np
@@ -101,6 +102,25 @@ class GpuIndex:
         d, b = np.empty(n, np.int32), np.empty(n, np.int64)
         check(self.lib.getIndexArraysGpu(self.h, _p(s), _p(e), _p(d), _p(b)))
         return s, e, d, b
+
+    # -- index image (the Rust crate's serde counterpart, superintervals.rs:35-44) --
+    def to_bytes(self) -> bytes:
+        """The built index as one flat byte image."""
+        size = C.c_size_t(0)
+        self.lib.serializeIndexGpu(self.h, None, 0, C.byref(size))
+        buf = C.create_string_buffer(max(size.value, 1))
+        check(self.lib.serializeIndexGpu(self.h, buf, size.value, C.byref(size)))
+        return buf.raw[: size.value]
+
+    def from_bytes(self, image: bytes):
+        """Replace this handle's intervals with an image's and index them (no sort)."""
+        check(self.lib.deserializeIndexGpu(self.h, C.c_char_p(image), len(image)))
+
+    def save(self, path: str):
+        check(self.lib.saveIndexGpu(self.h, os.fsencode(path)))
+
+    def load(self, path: str):
+        check(self.lib.loadIndexGpu(self.h, os.fsencode(path)))
 
     # -- options ---------------------------------------------------------------
     def set_path(self, path: int):

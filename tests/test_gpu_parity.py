@@ -441,3 +441,36 @@ def test_graph_replay_matches_and_respects_capacity(api):
     assert (tail == -9).all()
     d.close()
     idx.close()
+
+
+def test_index_image_roundtrip(api, tmp_path):
+    """An index saved as an image and loaded into a new handle answers identically; the
+    load skips the sort; corrupt, truncated or wrong-width images are rejected."""
+    from superintervals_gb300 import workloads as W
+    wl = W.config3(n=150_000, nq=20_000, contigs=W.HUMAN_CONTIGS[19:24])
+    a = _index(api, wl.starts, wl.ends, wl.data, seg=wl.seg, path="batched")
+    want = a.search(wl.q_starts, wl.q_ends, wl.q_contig)
+    img = a.to_bytes()
+    b = api.GpuIndex(32)
+    b.from_bytes(img)
+    b.set_path(api.PATH_BATCHED)
+    got = b.search(wl.q_starts, wl.q_ends, wl.q_contig)
+    assert np.array_equal(got[0], want[0]) and np.array_equal(got[1], want[1])
+    for x, y in zip(a.arrays(), b.arrays()):
+        assert np.array_equal(x, y)
+    p = str(tmp_path / "index.sig")
+    a.save(p)
+    c = api.GpuIndex(32)
+    c.load(p)
+    assert np.array_equal(c.count(wl.q_starts, wl.q_ends, wl.q_contig),
+                          a.count(wl.q_starts, wl.q_ends, wl.q_contig))
+    bad = bytearray(img)
+    bad[-5] ^= 0x40                                     # inside the branch array
+    with pytest.raises(api.SIError):
+        api.GpuIndex(32).from_bytes(bytes(bad))
+    with pytest.raises(api.SIError):
+        api.GpuIndex(32).from_bytes(img[: len(img) // 2])
+    with pytest.raises(api.SIError):
+        api.GpuIndex(64).from_bytes(img)
+    for h in (a, b, c):
+        h.close()
