@@ -106,10 +106,37 @@ int indexSuperIntervalsGpu(gSuperIntervals* si);
 int getIndexArraysGpu(const gSuperIntervals* si, void* starts, void* ends, int32_t* data,
                       int64_t* branch);
 
+/* ---- BED ingest: the format step in front of the index
+ *      (examples/bed-intersect-si.rs:63-120 read_bed_file / parse_bed_line,
+ *      test/bench.cpp:67-102 load_intervals), parsed on the GPU ------------
+ * Columns: chrom, start, end (tab-separated; further columns ignored).  Lines
+ * that are empty or start with '#', "track" or "browser" are skipped; lines with
+ * fewer than three columns or a non-integer start / end are counted as
+ * malformed and skipped; with SI_BED_HALF_OPEN the stored end is column 3 - 1
+ * (BED ends are exclusive, the index is end-inclusive, as bed-intersect-si.rs
+ * does); lines with end < 0 or end < start are skipped (as there); coordinates
+ * outside the handle's width are counted and skipped. */
+#define SI_BED_HALF_OPEN 1
+typedef struct {
+    size_t lines, intervals, skipped_headers, malformed, filtered, out_of_range, unknown_contig;
+} cBedStats;
+/* Replaces the staged intervals with the file's: one contig per distinct chrom
+ * name, ids in order of first appearance, intervals of a contig in file order,
+ * payload = 0-based line number.  Call indexSuperIntervalsGpu afterwards. */
+int ingestBedGpu(gSuperIntervals* si, const char* text, size_t len, int options, cBedStats* stats);
+/* Queries from BED text against the handle's contig names: lines on chroms the
+ * index does not hold are skipped (counted in unknown_contig); output in file
+ * order with each query's contig id and 0-based line number (line may be NULL).
+ * SI_ERR_CAPACITY with *n set when capacity is too small. */
+int bedQueriesGpu(gSuperIntervals* si, const char* text, size_t len, int options, void* qs, void* qe,
+                  int32_t* qcontig, int64_t* line, size_t capacity, size_t* n, cBedStats* stats);
+/* Name of contig `contig` after ingestBedGpu (NUL-terminated; *len = length). */
+int contigNameGpu(const gSuperIntervals* si, size_t contig, char* buf, size_t cap, size_t* len);
+
 /* ---- index image: the counterpart of the Rust crate's serde derive on
  *      IntervalMap (superintervals.rs:35-44) ---------------------------------
  * One flat little-endian byte image of a built index: header, contig offsets,
- * sorted starts / ends / payloads, branch array.  serializeIndexGpu writes it
+ * sorted starts / ends / payloads, branch array, contig names (when known).  serializeIndexGpu writes it
  * into buf (SI_ERR_CAPACITY with the size in *size when cap is too small);
  * deserializeIndexGpu replaces the handle's intervals with the image's and
  * indexes them without sorting (the coordinate width must match the handle's;

@@ -53,6 +53,13 @@ class cCsrResult(C.Structure):
                 ("offsets_capacity", C.c_size_t)]
 
 
+class cBedStats(C.Structure):
+    _fields_ = [(k, C.c_size_t) for k in ("lines", "intervals", "skipped_headers", "malformed", "filtered",
+                                         "out_of_range", "unknown_contig")]
+
+
+BED_HALF_OPEN = 1
+
 _P = C.c_void_p
 _H = C.c_void_p
 _SZ = C.c_size_t
@@ -74,6 +81,9 @@ SIGNATURES = {
     "indexSuperIntervalsGpu": (_I, [_H]),
     "getIndexArraysGpu": (_I, [_H, _P, _P, _P, _P]),
     "serializeIndexGpu": (_I, [_H, _P, _SZ, C.POINTER(_SZ)]),
+    "ingestBedGpu": (_I, [_H, C.c_char_p, _SZ, _I, C.POINTER(cBedStats)]),
+    "bedQueriesGpu": (_I, [_H, C.c_char_p, _SZ, _I, _P, _P, _P, _P, _SZ, C.POINTER(_SZ), C.POINTER(cBedStats)]),
+    "contigNameGpu": (_I, [_H, _SZ, C.c_char_p, _SZ, C.POINTER(_SZ)]),
     "deserializeIndexGpu": (_I, [_H, _P, _SZ]),
     "saveIndexGpu": (_I, [_H, C.c_char_p]),
     "loadIndexGpu": (_I, [_H, C.c_char_p]),

@@ -148,6 +148,8 @@ struct gSuperIntervals {
     // set operations: hit lists, staged pieces, and whether some interval has start > end
     DevBuf so_hoff, so_hits, so_off, so_os, so_oe, so_ob, so_flag;
     int inverted = -1;  // -1 unknown, else 0 / 1 (reset by every build)
+    // contig names, in contig-id order, when the intervals came from BED text
+    std::vector<std::string> contig_names;
     // options
     int path = SI_PATH_AUTO;
     int ub_mode = SI_UB_BINARY;
@@ -686,6 +688,7 @@ int clearSuperIntervalsGpu(gSuperIntervals* si) {
     if (!si) return fail(SI_ERR_INVALID, "null handle");
     si->hs32.clear(); si->he32.clear(); si->hs64.clear(); si->he64.clear(); si->hdata.clear();
     si->hseg.clear();
+    si->contig_names.clear();
     si->built = false;
     si->n = 0;
     return SI_OK;
@@ -721,6 +724,7 @@ int setContigsGpu(gSuperIntervals* si, size_t n_contigs, const int64_t* offsets)
         if (offsets[g + 1] < offsets[g]) return fail(SI_ERR_INVALID, "contig offsets decrease at %zu", g);
     if (n_contigs >= (size_t)INT32_MAX) return fail(SI_ERR_INVALID, "too many contigs");
     si->hseg.assign(offsets, offsets + n_contigs + 1);
+    if (si->contig_names.size() != n_contigs) si->contig_names.clear();
     si->built = false;
     return SI_OK;
 }
@@ -1711,13 +1715,22 @@ struct ImageHeader {
 
 inline size_t pad8(size_t x) { return (x + 7) & ~(size_t)7; }
 
+// header, seg[G+1], starts, ends, data, branch (each padded to 8 bytes), then the contig names:
+// u64 count (0 or G), int64 offsets[count + 1], name bytes (padded to 8)
 size_t image_bytes(int bits, uint64_t n, uint64_t G) {
     const size_t sb = (size_t)bits / 8;
-    return sizeof(ImageHeader) + 8 * (G + 1) + 2 * pad8(sb * n) + 2 * pad8(4 * n);
+    return sizeof(ImageHeader) + 8 * (G + 1) + 2 * pad8(sb * n) + 2 * pad8(4 * n) + 8;
+}
+
+size_t names_bytes(const std::vector<std::string>& names) {
+    if (names.empty()) return 0;
+    size_t b = 0;
+    for (const auto& s : names) b += s.size();
+    return 8 * (names.size() + 1) + pad8(b);
 }
 
 template <typename S>
-int deserialize_impl(gSuperIntervals* si, const ImageHeader& h, const unsigned char* p) {
+int deserialize_impl(gSuperIntervals* si, const ImageHeader& h, const unsigned char* p, const unsigned char* end) {
     const uint64_t n = h.n, G = h.n_contigs;
     const int64_t* seg = reinterpret_cast<const int64_t*>(p);
     p += 8 * (G + 1);
@@ -1731,11 +1744,29 @@ int deserialize_impl(gSuperIntervals* si, const ImageHeader& h, const unsigned c
     const int32_t* da = reinterpret_cast<const int32_t*>(p);
     p += pad8(4 * n);
     const int32_t* br = reinterpret_cast<const int32_t*>(p);
+    p += pad8(4 * n);
+    uint64_t nn = 0;
+    memcpy(&nn, p, 8);
+    p += 8;
+    std::vector<std::string> names;
+    if (nn) {
+        if (nn != G || (size_t)(end - p) < 8 * (nn + 1)) return fail(SI_ERR_INVALID, "index image: bad name table");
+        std::vector<int64_t> at(nn + 1);
+        memcpy(at.data(), p, 8 * (nn + 1));
+        p += 8 * (nn + 1);
+        if (at[0] != 0 || at[nn] < 0 || (size_t)(end - p) < (size_t)at[nn])
+            return fail(SI_ERR_INVALID, "index image: bad name table");
+        for (uint64_t c = 0; c < nn; ++c) {
+            if (at[c + 1] < at[c]) return fail(SI_ERR_INVALID, "index image: bad name table");
+            names.emplace_back(reinterpret_cast<const char*>(p) + at[c], (size_t)(at[c + 1] - at[c]));
+        }
+    }
     hs<S>(si).assign(st, st + n);
     he<S>(si).assign(en, en + n);
     si->hdata.assign(da, da + n);
     si->hseg.clear();
     if (G > 1) si->hseg.assign(seg, seg + G + 1);
+    si->contig_names = names;
     si->built = false;
     SI_TRY(build_impl<S>(si));
     if (n == 0) return SI_OK;
@@ -1760,7 +1791,9 @@ extern "C" int serializeIndexGpu(const gSuperIntervals* si, void* buf, size_t ca
     SI_TRY(check_built(si));
     SI_TRY(set_dev(si));
     const uint64_t n = (uint64_t)si->n, G = (uint64_t)si->G;
-    const size_t need = image_bytes(si->bits, n, G);
+    const std::vector<std::string>& names = si->contig_names.size() == G ? si->contig_names
+                                                                          : std::vector<std::string>();
+    const size_t need = image_bytes(si->bits, n, G) + names_bytes(names);
     if (size) *size = need;
     if (!buf || cap < need) return fail(SI_ERR_CAPACITY, "index image needs %zu bytes, capacity %zu", need, cap);
     unsigned char* p = static_cast<unsigned char*>(buf);
@@ -1786,8 +1819,24 @@ extern "C" int serializeIndexGpu(const gSuperIntervals* si, void* buf, size_t ca
         SI_CK(cudaMemcpyAsync(p, si->data.p, 4 * n, cudaMemcpyDeviceToHost, si->st));
         p += pad8(4 * n);
         SI_CK(cudaMemcpyAsync(p, si->branch.p, 4 * n, cudaMemcpyDeviceToHost, si->st));
-        SI_CK(cudaStreamSynchronize(si->st));
+        p += pad8(4 * n);
     }
+    const uint64_t nn = names.size();
+    memcpy(p, &nn, 8);
+    p += 8;
+    if (nn) {
+        int64_t at = 0;
+        for (uint64_t c = 0; c <= nn; ++c) {
+            memcpy(p + 8 * c, &at, 8);
+            if (c < nn) at += (int64_t)names[c].size();
+        }
+        p += 8 * (nn + 1);
+        for (const auto& s : names) {
+            memcpy(p, s.data(), s.size());
+            p += s.size();
+        }
+    }
+    SI_CK(cudaStreamSynchronize(si->st));
     return SI_OK;
 }
 
@@ -1805,8 +1854,9 @@ extern "C" int deserializeIndexGpu(gSuperIntervals* si, const void* buf, size_t 
     if (len < image_bytes(si->bits, h.n, h.n_contigs)) return fail(SI_ERR_INVALID, "index image truncated");
     SI_TRY(set_dev(si));
     const unsigned char* p = static_cast<const unsigned char*>(buf) + sizeof(h);
-    if (si->bits == 64) return deserialize_impl<int64_t>(si, h, p);
-    return deserialize_impl<int32_t>(si, h, p);
+    const unsigned char* end = static_cast<const unsigned char*>(buf) + len;
+    if (si->bits == 64) return deserialize_impl<int64_t>(si, h, p, end);
+    return deserialize_impl<int32_t>(si, h, p, end);
 }
 
 extern "C" int saveIndexGpu(const gSuperIntervals* si, const char* path) {
@@ -1836,4 +1886,318 @@ extern "C" int loadIndexGpu(gSuperIntervals* si, const char* path) {
     fclose(f);
     if (bad) return fail(SI_ERR_INVALID, "reading %s failed", path);
     return deserializeIndexGpu(si, img.data(), img.size());
+}
+
+// =====================================================================================
+// BED ingest (examples/bed-intersect-si.rs:63-120, test/bench.cpp:67-102): the text is parsed
+// on the GPU (si_bed.cu); the contig dictionary and the per-contig bucketing are radix sorts.
+// =====================================================================================
+namespace {
+
+struct BedRecords {
+    DevBuf text, nl, status, valid, hash, start, end, noff, nlen, voffs, tmp;
+    DevBuf h_lo, h_hi, rec, r_start, r_end, r_noff, r_nlen, r_line;
+    int64_t n_lines = 0, m = 0;
+};
+
+uint64_t fnv1a64(const char* p, size_t n) {
+    uint64_t h = 1469598103934665603ull;
+    for (size_t k = 0; k < n; ++k) h = (h ^ (unsigned char)p[k]) * 1099511628211ull;
+    return h;
+}
+
+// Parse the text into interval records (file order) on the device.
+int bed_records(gSuperIntervals* si, const char* text, size_t len, int options, BedRecords& B, cBedStats* stats) {
+    cudaStream_t st = si->st;
+    const int64_t L = (int64_t)len;
+    if (len && !text) return fail(SI_ERR_INVALID, "null text");
+    SI_TRY(B.text.reserve(len + 16));
+    if (len) SI_CK(cudaMemcpyAsync(B.text.p, text, len, cudaMemcpyHostToDevice, st));
+    const int64_t chunks = sig::bed_chunks(L);
+    DevBuf counts, offs;
+    SI_TRY(counts.reserve(sizeof(uint32_t) * chunks));
+    SI_TRY(offs.reserve(sizeof(int64_t) * (chunks + 1)));
+    SI_TRY(B.tmp.reserve(sig::scan_temp_bytes(chunks)));
+    const unsigned char* t = B.text.as<unsigned char>();
+    SI_CK(sig::launch_nl_count(t, L, counts.as<uint32_t>(), st));
+    SI_CK(sig::exclusive_scan_u32_to_i64(counts.as<uint32_t>(), offs.as<int64_t>(), chunks, B.tmp.p, st));
+    int64_t n_nl = 0;
+    SI_CK(cudaMemcpyAsync(&n_nl, offs.as<int64_t>() + chunks, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+    SI_CK(cudaStreamSynchronize(st));
+    SI_TRY(B.nl.reserve(sizeof(int64_t) * std::max<int64_t>(n_nl, 1)));
+    if (n_nl) SI_CK(sig::launch_nl_write(t, L, offs.as<int64_t>(), B.nl.as<int64_t>(), st));
+    const int64_t n = n_nl + ((len > 0 && text[len - 1] != '\n') ? 1 : 0);
+    B.n_lines = n;
+    const int64_t nn = std::max<int64_t>(n, 1);
+    SI_TRY(B.status.reserve(nn));
+    SI_TRY(B.valid.reserve(4 * nn));
+    SI_TRY(B.hash.reserve(8 * nn));
+    SI_TRY(B.start.reserve(8 * nn));
+    SI_TRY(B.end.reserve(8 * nn));
+    SI_TRY(B.noff.reserve(8 * nn));
+    SI_TRY(B.nlen.reserve(4 * nn));
+    const int64_t lo = si->bits == 64 ? INT64_MIN : INT32_MIN, hi = si->bits == 64 ? INT64_MAX : INT32_MAX;
+    SI_CK(sig::launch_bed_parse(t, L, B.nl.as<int64_t>(), n_nl, n, (options & SI_BED_HALF_OPEN) ? 1 : 0, lo, hi,
+                                B.status.as<uint8_t>(), B.valid.as<uint32_t>(), B.hash.as<uint64_t>(),
+                                B.start.as<int64_t>(), B.end.as<int64_t>(), B.noff.as<int64_t>(),
+                                B.nlen.as<int32_t>(), st));
+    if (stats) {
+        std::vector<uint8_t> hs_(n);
+        if (n) SI_CK(cudaMemcpyAsync(hs_.data(), B.status.p, n, cudaMemcpyDeviceToHost, st));
+        SI_CK(cudaStreamSynchronize(st));
+        size_t c[5] = {0, 0, 0, 0, 0};
+        for (uint8_t v : hs_) ++c[v < 5 ? v : 2];
+        stats->lines = (size_t)n;
+        stats->intervals = c[0];
+        stats->skipped_headers = c[1];
+        stats->malformed = c[2];
+        stats->filtered = c[3];
+        stats->out_of_range = c[4];
+        stats->unknown_contig = 0;
+    }
+    SI_TRY(B.voffs.reserve(sizeof(int64_t) * (n + 1)));
+    SI_TRY(B.tmp.reserve(sig::scan_temp_bytes(nn)));
+    SI_CK(sig::exclusive_scan_u32_to_i64(B.valid.as<uint32_t>(), B.voffs.as<int64_t>(), n, B.tmp.p, st));
+    int64_t m = 0;
+    SI_CK(cudaMemcpyAsync(&m, B.voffs.as<int64_t>() + n, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+    SI_CK(cudaStreamSynchronize(st));
+    if (m >= ((int64_t)1 << 31) - 1) return fail(SI_ERR_TOO_LARGE, "%lld intervals exceed the position space", (long long)m);
+    B.m = m;
+    const int64_t mm = std::max<int64_t>(m, 1);
+    SI_TRY(B.h_lo.reserve(4 * mm));
+    SI_TRY(B.h_hi.reserve(4 * mm));
+    SI_TRY(B.rec.reserve(4 * mm));
+    SI_TRY(B.r_start.reserve(8 * mm));
+    SI_TRY(B.r_end.reserve(8 * mm));
+    SI_TRY(B.r_noff.reserve(8 * mm));
+    SI_TRY(B.r_nlen.reserve(4 * mm));
+    SI_TRY(B.r_line.reserve(8 * mm));
+    SI_CK(sig::launch_bed_compact(B.valid.as<uint32_t>(), B.voffs.as<int64_t>(), n, B.hash.as<uint64_t>(),
+                                  B.start.as<int64_t>(), B.end.as<int64_t>(), B.noff.as<int64_t>(),
+                                  B.nlen.as<int32_t>(), B.h_lo.as<uint32_t>(), B.h_hi.as<uint32_t>(),
+                                  B.rec.as<uint32_t>(), B.r_start.as<int64_t>(), B.r_end.as<int64_t>(),
+                                  B.r_noff.as<int64_t>(), B.r_nlen.as<int32_t>(), B.r_line.as<int64_t>(), st));
+    return SI_OK;
+}
+
+template <typename S>
+int bed_ingest(gSuperIntervals* si, const char* text, size_t len, int options, cBedStats* stats) {
+    cudaStream_t st = si->st;
+    BedRecords B;
+    SI_TRY(bed_records(si, text, len, options, B, stats));
+    const int64_t m = B.m;
+    hs<S>(si).clear();
+    he<S>(si).clear();
+    si->hdata.clear();
+    si->hseg.clear();
+    si->contig_names.clear();
+    si->built = false;
+    if (m == 0) return SI_OK;
+    // 1. dictionary: sort records by name hash (stable: file order inside a hash group)
+    DevBuf lo2, hi2, rec2, stmp;
+    SI_TRY(lo2.reserve(4 * m));
+    SI_TRY(hi2.reserve(4 * m));
+    SI_TRY(rec2.reserve(4 * m));
+    SI_TRY(stmp.reserve(sig::radix_temp_bytes(m, 2)));
+    uint32_t* kp[2] = {B.h_lo.as<uint32_t>(), B.h_hi.as<uint32_t>()};
+    uint32_t* ka[2] = {lo2.as<uint32_t>(), hi2.as<uint32_t>()};
+    bool alt = false;
+    SI_CK(sig::radix_sort(kp, ka, B.rec.as<uint32_t>(), rec2.as<uint32_t>(), 2, m, stmp.p, stmp.bytes, &alt, nullptr,
+                          st));
+    const uint32_t* slo = alt ? ka[0] : kp[0];
+    const uint32_t* shi = alt ? ka[1] : kp[1];
+    const uint32_t* perm = alt ? rec2.as<uint32_t>() : B.rec.as<uint32_t>();
+    DevBuf head, ex, gid;
+    SI_TRY(head.reserve(4 * m));
+    SI_TRY(ex.reserve(4 * (m + 1)));
+    SI_TRY(gid.reserve(4 * m));
+    SI_TRY(B.tmp.reserve(sig::scan_temp_bytes(m)));
+    SI_CK(sig::launch_hash_heads(slo, shi, m, head.as<uint32_t>(), st));
+    SI_CK(sig::exclusive_scan_u32_to_u32(head.as<uint32_t>(), ex.as<uint32_t>(), m, B.tmp.p, st));
+    uint32_t G32 = 0;
+    SI_CK(cudaMemcpyAsync(&G32, ex.as<uint32_t>() + m, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    SI_CK(cudaStreamSynchronize(st));
+    const int64_t G = G32;
+    DevBuf first, gkey, coll;
+    SI_TRY(first.reserve(4 * G));
+    SI_TRY(gkey.reserve(4 * G));
+    SI_TRY(coll.reserve(sizeof(int)));
+    SI_CK(cudaMemsetAsync(coll.p, 0, sizeof(int), st));
+    SI_CK(sig::launch_hash_groups(B.text.as<unsigned char>(), head.as<uint32_t>(), ex.as<uint32_t>(), perm, m,
+                                  B.r_noff.as<int64_t>(), B.r_nlen.as<int32_t>(), gid.as<uint32_t>(),
+                                  first.as<uint32_t>(), gkey.as<uint32_t>(), coll.as<int>(), st));
+    int collision = 0;
+    SI_CK(cudaMemcpyAsync(&collision, coll.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+    SI_CK(cudaStreamSynchronize(st));
+    if (collision) return fail(SI_ERR_INVALID, "two contig names share a 64-bit name hash");
+    // 2. contig ids in order of first appearance
+    DevBuf gk2, gp, gp2, gtmp;
+    SI_TRY(gk2.reserve(4 * G));
+    SI_TRY(gp.reserve(4 * G));
+    SI_TRY(gp2.reserve(4 * G));
+    SI_TRY(gtmp.reserve(sig::radix_temp_bytes(G, 1)));
+    SI_CK(sig::launch_iota_u32(gp.as<uint32_t>(), G, st));
+    uint32_t* gkp[1] = {gkey.as<uint32_t>()};
+    uint32_t* gka[1] = {gk2.as<uint32_t>()};
+    bool galt = false;
+    SI_CK(sig::radix_sort(gkp, gka, gp.as<uint32_t>(), gp2.as<uint32_t>(), 1, G, gtmp.p, gtmp.bytes, &galt, nullptr,
+                          st));
+    const uint32_t* sorted_groups = galt ? gp2.as<uint32_t>() : gp.as<uint32_t>();
+    // the sorted keys are each contig's first record, in contig order
+    const uint32_t* first_rec = galt ? gka[0] : gkp[0];
+    DevBuf rank, cid;
+    SI_TRY(rank.reserve(4 * G));
+    SI_TRY(cid.reserve(4 * m));
+    SI_CK(sig::launch_record_contig(sorted_groups, G, rank.as<uint32_t>(), gid.as<uint32_t>(), perm, m,
+                                    cid.as<uint32_t>(), st));
+    // 3. per-contig buckets, file order inside a contig
+    DevBuf cid2, ord, ord2, otmp;
+    SI_TRY(cid2.reserve(4 * m));
+    SI_TRY(ord.reserve(4 * m));
+    SI_TRY(ord2.reserve(4 * m));
+    SI_TRY(otmp.reserve(sig::radix_temp_bytes(m, 1)));
+    SI_CK(sig::launch_iota_u32(ord.as<uint32_t>(), m, st));
+    uint32_t* ckp[1] = {cid.as<uint32_t>()};
+    uint32_t* cka[1] = {cid2.as<uint32_t>()};
+    bool calt = false;
+    SI_CK(sig::radix_sort(ckp, cka, ord.as<uint32_t>(), ord2.as<uint32_t>(), 1, m, otmp.p, otmp.bytes, &calt, nullptr,
+                          st));
+    const uint32_t* cid_sorted = calt ? cka[0] : ckp[0];
+    const uint32_t* order = calt ? ord2.as<uint32_t>() : ord.as<uint32_t>();
+    DevBuf os, oe, ol, seg, noff, nlen;
+    SI_TRY(os.reserve(sizeof(S) * m));
+    SI_TRY(oe.reserve(sizeof(S) * m));
+    SI_TRY(ol.reserve(4 * m));
+    SI_TRY(seg.reserve(8 * (G + 1)));
+    SI_TRY(noff.reserve(8 * G));
+    SI_TRY(nlen.reserve(4 * G));
+    SI_CK(sig::launch_bed_out<S>(cid_sorted, order, m, B.r_start.as<int64_t>(), B.r_end.as<int64_t>(),
+                                 B.r_line.as<int64_t>(), os.as<S>(), oe.as<S>(), ol.as<int32_t>(),
+                                 seg.as<int64_t>(), st));
+    SI_CK(sig::launch_contig_names(first_rec, B.r_noff.as<int64_t>(), B.r_nlen.as<int32_t>(), G, noff.as<int64_t>(),
+                                   nlen.as<int32_t>(), st));
+    hs<S>(si).resize(m);
+    he<S>(si).resize(m);
+    si->hdata.resize(m);
+    std::vector<int64_t> segv(G + 1);
+    std::vector<int64_t> hoff(G);
+    std::vector<int32_t> hlen(G);
+    SI_CK(cudaMemcpyAsync(hs<S>(si).data(), os.p, sizeof(S) * m, cudaMemcpyDeviceToHost, st));
+    SI_CK(cudaMemcpyAsync(he<S>(si).data(), oe.p, sizeof(S) * m, cudaMemcpyDeviceToHost, st));
+    SI_CK(cudaMemcpyAsync(si->hdata.data(), ol.p, 4 * m, cudaMemcpyDeviceToHost, st));
+    SI_CK(cudaMemcpyAsync(segv.data(), seg.p, 8 * G, cudaMemcpyDeviceToHost, st));
+    SI_CK(cudaMemcpyAsync(hoff.data(), noff.p, 8 * G, cudaMemcpyDeviceToHost, st));
+    SI_CK(cudaMemcpyAsync(hlen.data(), nlen.p, 4 * G, cudaMemcpyDeviceToHost, st));
+    SI_CK(cudaStreamSynchronize(st));
+    segv[G] = m;
+    if (G > 1) si->hseg = segv;
+    si->contig_names.resize(G);
+    for (int64_t c = 0; c < G; ++c) si->contig_names[c].assign(text + hoff[c], (size_t)hlen[c]);
+    return SI_OK;
+}
+
+template <typename S>
+int bed_queries(gSuperIntervals* si, const char* text, size_t len, int options, S* qs, S* qe, int32_t* qc,
+                int64_t* line, size_t cap, size_t* n_out, cBedStats* stats) {
+    cudaStream_t st = si->st;
+    const int G = (int)si->contig_names.size();
+    if (G == 0) return fail(SI_ERR_INVALID, "the handle has no contig names: ingest a BED file first");
+    BedRecords B;
+    SI_TRY(bed_records(si, text, len, options, B, stats));
+    const int64_t m = B.m;
+    if (n_out) *n_out = 0;
+    // contig table: (hash, id) sorted by hash, and the names as one blob
+    std::vector<std::pair<uint64_t, int32_t>> tab(G);
+    std::vector<int64_t> at(G + 1, 0);
+    std::string blob;
+    for (int c = 0; c < G; ++c) {
+        const std::string& nm = si->contig_names[c];
+        tab[c] = {fnv1a64(nm.data(), nm.size()), c};
+        at[c] = (int64_t)blob.size();
+        blob += nm;
+    }
+    at[G] = (int64_t)blob.size();
+    std::sort(tab.begin(), tab.end());
+    for (int c = 1; c < G; ++c)
+        if (tab[c].first == tab[c - 1].first) return fail(SI_ERR_INVALID, "two contig names share a 64-bit name hash");
+    std::vector<uint64_t> th(G);
+    std::vector<int32_t> tid(G);
+    for (int c = 0; c < G; ++c) {
+        th[c] = tab[c].first;
+        tid[c] = tab[c].second;
+    }
+    DevBuf dh, did, dnames, dat, dqc, flag, offs;
+    SI_TRY(dh.reserve(8 * G));
+    SI_TRY(did.reserve(4 * G));
+    SI_TRY(dnames.reserve(std::max<size_t>(blob.size(), 1)));
+    SI_TRY(dat.reserve(8 * (G + 1)));
+    SI_CK(cudaMemcpyAsync(dh.p, th.data(), 8 * G, cudaMemcpyHostToDevice, st));
+    SI_CK(cudaMemcpyAsync(did.p, tid.data(), 4 * G, cudaMemcpyHostToDevice, st));
+    if (!blob.empty()) SI_CK(cudaMemcpyAsync(dnames.p, blob.data(), blob.size(), cudaMemcpyHostToDevice, st));
+    SI_CK(cudaMemcpyAsync(dat.p, at.data(), 8 * (G + 1), cudaMemcpyHostToDevice, st));
+    const int64_t mm = std::max<int64_t>(m, 1);
+    SI_TRY(dqc.reserve(4 * mm));
+    SI_TRY(flag.reserve(4 * mm));
+    SI_TRY(offs.reserve(8 * (m + 1)));
+    SI_CK(sig::launch_bed_lookup(B.text.as<unsigned char>(), B.h_lo.as<uint32_t>(), B.h_hi.as<uint32_t>(),
+                                 B.r_noff.as<int64_t>(), B.r_nlen.as<int32_t>(), m, dh.as<uint64_t>(),
+                                 did.as<int32_t>(), G, dnames.as<unsigned char>(), dat.as<int64_t>(),
+                                 dqc.as<int32_t>(), st));
+    SI_CK(sig::launch_known(dqc.as<int32_t>(), m, flag.as<uint32_t>(), st));
+    SI_TRY(B.tmp.reserve(sig::scan_temp_bytes(mm)));
+    SI_CK(sig::exclusive_scan_u32_to_i64(flag.as<uint32_t>(), offs.as<int64_t>(), m, B.tmp.p, st));
+    int64_t k = 0;
+    SI_CK(cudaMemcpyAsync(&k, offs.as<int64_t>() + m, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+    SI_CK(cudaStreamSynchronize(st));
+    if (stats) stats->unknown_contig = (size_t)(m - k);
+    if (n_out) *n_out = (size_t)k;
+    if ((size_t)k > cap) return fail(SI_ERR_CAPACITY, "%lld queries, capacity %zu", (long long)k, cap);
+    if (k == 0) return SI_OK;
+    if (!qs || !qe || !qc) return fail(SI_ERR_INVALID, "null output buffer");
+    DevBuf dqs, dqe, dqc2, dl;
+    SI_TRY(dqs.reserve(sizeof(S) * k));
+    SI_TRY(dqe.reserve(sizeof(S) * k));
+    SI_TRY(dqc2.reserve(4 * k));
+    SI_TRY(dl.reserve(8 * k));
+    SI_CK(sig::launch_query_out<S>(dqc.as<int32_t>(), offs.as<int64_t>(), m, B.r_start.as<int64_t>(),
+                                   B.r_end.as<int64_t>(), B.r_line.as<int64_t>(), dqs.as<S>(), dqe.as<S>(),
+                                   dqc2.as<int32_t>(), dl.as<int64_t>(), st));
+    SI_CK(cudaMemcpyAsync(qs, dqs.p, sizeof(S) * k, cudaMemcpyDeviceToHost, st));
+    SI_CK(cudaMemcpyAsync(qe, dqe.p, sizeof(S) * k, cudaMemcpyDeviceToHost, st));
+    SI_CK(cudaMemcpyAsync(qc, dqc2.p, 4 * k, cudaMemcpyDeviceToHost, st));
+    if (line) SI_CK(cudaMemcpyAsync(line, dl.p, 8 * k, cudaMemcpyDeviceToHost, st));
+    SI_CK(cudaStreamSynchronize(st));
+    return SI_OK;
+}
+
+}  // namespace
+
+extern "C" int ingestBedGpu(gSuperIntervals* si, const char* text, size_t len, int options, cBedStats* stats) {
+    if (!si) return fail(SI_ERR_INVALID, "null handle");
+    SI_TRY(set_dev(si));
+    if (si->bits == 64) return bed_ingest<int64_t>(si, text, len, options, stats);
+    return bed_ingest<int32_t>(si, text, len, options, stats);
+}
+
+extern "C" int bedQueriesGpu(gSuperIntervals* si, const char* text, size_t len, int options, void* qs, void* qe,
+                             int32_t* qcontig, int64_t* line, size_t capacity, size_t* n, cBedStats* stats) {
+    if (!si) return fail(SI_ERR_INVALID, "null handle");
+    SI_TRY(set_dev(si));
+    if (si->bits == 64)
+        return bed_queries<int64_t>(si, text, len, options, (int64_t*)qs, (int64_t*)qe, qcontig, line, capacity, n,
+                                    stats);
+    return bed_queries<int32_t>(si, text, len, options, (int32_t*)qs, (int32_t*)qe, qcontig, line, capacity, n,
+                                stats);
+}
+
+extern "C" int contigNameGpu(const gSuperIntervals* si, size_t contig, char* buf, size_t cap, size_t* len) {
+    if (!si) return fail(SI_ERR_INVALID, "null handle");
+    if (contig >= si->contig_names.size())
+        return fail(SI_ERR_INVALID, "contig %zu has no name (%zu named)", contig, si->contig_names.size());
+    const std::string& nm = si->contig_names[contig];
+    if (len) *len = nm.size();
+    if (!buf || cap < nm.size() + 1) return fail(SI_ERR_CAPACITY, "name needs %zu bytes", nm.size() + 1);
+    memcpy(buf, nm.data(), nm.size());
+    buf[nm.size()] = 0;
+    return SI_OK;
 }

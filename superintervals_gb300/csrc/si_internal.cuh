@@ -60,6 +60,43 @@ cudaError_t exclusive_scan_u32_to_i64(const uint32_t* in, int64_t* out, int64_t 
 cudaError_t exclusive_scan_u32_to_u32(const uint32_t* in, uint32_t* out, int64_t n, void* temp,
                                       cudaStream_t st);
 
+// ---------------------------------------------------------------- BED ingest (si_bed.cu)
+int64_t bed_chunks(int64_t len);
+cudaError_t launch_nl_count(const unsigned char* text, int64_t len, uint32_t* counts, cudaStream_t st);
+cudaError_t launch_nl_write(const unsigned char* text, int64_t len, const int64_t* offs, int64_t* nl,
+                            cudaStream_t st);
+cudaError_t launch_bed_parse(const unsigned char* t, int64_t len, const int64_t* nl, int64_t n_nl, int64_t n_lines,
+                             int half_open, int64_t lo_lim, int64_t hi_lim, uint8_t* status, uint32_t* valid,
+                             uint64_t* hash, int64_t* start, int64_t* end, int64_t* name_off, int32_t* name_len,
+                             cudaStream_t st);
+cudaError_t launch_bed_compact(const uint32_t* valid, const int64_t* offs, int64_t n_lines, const uint64_t* hash,
+                               const int64_t* start, const int64_t* end, const int64_t* name_off,
+                               const int32_t* name_len, uint32_t* h_lo, uint32_t* h_hi, uint32_t* rec_id,
+                               int64_t* r_start, int64_t* r_end, int64_t* r_noff, int32_t* r_nlen, int64_t* r_line,
+                               cudaStream_t st);
+cudaError_t launch_hash_heads(const uint32_t* lo, const uint32_t* hi, int64_t m, uint32_t* head, cudaStream_t st);
+cudaError_t launch_hash_groups(const unsigned char* t, const uint32_t* head, const uint32_t* ex,
+                               const uint32_t* perm, int64_t m, const int64_t* r_noff, const int32_t* r_nlen,
+                               uint32_t* gid, uint32_t* first, uint32_t* grp_key, int* collision, cudaStream_t st);
+cudaError_t launch_record_contig(const uint32_t* sorted_groups, int64_t G, uint32_t* rank, const uint32_t* gid,
+                                 const uint32_t* perm, int64_t m, uint32_t* cid, cudaStream_t st);
+template <typename S>
+cudaError_t launch_bed_out(const uint32_t* cid_sorted, const uint32_t* order, int64_t m, const int64_t* r_start,
+                           const int64_t* r_end, const int64_t* r_line, S* os, S* oe, int32_t* oline, int64_t* seg,
+                           cudaStream_t st);
+cudaError_t launch_bed_lookup(const unsigned char* t, const uint32_t* h_lo, const uint32_t* h_hi,
+                              const int64_t* r_noff, const int32_t* r_nlen, int64_t m, const uint64_t* ctg_hash,
+                              const int32_t* ctg_id, int G, const unsigned char* names, const int64_t* name_at,
+                              int32_t* qc, cudaStream_t st);
+cudaError_t launch_iota_u32(uint32_t* out, int64_t n, cudaStream_t st);
+cudaError_t launch_known(const int32_t* qc, int64_t m, uint32_t* flag, cudaStream_t st);
+template <typename S>
+cudaError_t launch_query_out(const int32_t* qc, const int64_t* offs, int64_t m, const int64_t* r_start,
+                             const int64_t* r_end, const int64_t* r_line, S* qs, S* qe, int32_t* qc_out,
+                             int64_t* line_out, cudaStream_t st);
+cudaError_t launch_contig_names(const uint32_t* first_rec, const int64_t* r_noff, const int32_t* r_nlen, int64_t G,
+                                int64_t* off, int32_t* len, cudaStream_t st);
+
 // ---------------------------------------------------------------- sort
 // Stable LSD radix sort of n records whose key is K 32-bit words (word 0 least
 // significant) with one 32-bit payload.  keys[w] / payload are double

@@ -103,6 +103,49 @@ class GpuIndex:
         check(self.lib.getIndexArraysGpu(self.h, _p(s), _p(e), _p(d), _p(b)))
         return s, e, d, b
 
+    # -- BED ingest (examples/bed-intersect-si.rs:63-120), parsed on the GPU ---------
+    @staticmethod
+    def _stats(st):
+        return {k: int(getattr(st, k)) for k, _ in _capi.cBedStats._fields_}
+
+    def ingest_bed(self, text: bytes, half_open: bool = True) -> dict:
+        """Stage the intervals of BED text (one contig per chrom, first-appearance
+        order, payload = line number); call build() afterwards.  Returns line counts."""
+        st = _capi.cBedStats()
+        check(self.lib.ingestBedGpu(self.h, text, len(text), _capi.BED_HALF_OPEN if half_open else 0,
+                                    C.byref(st)))
+        return self._stats(st)
+
+    def contig_names(self) -> list:
+        out, n = [], C.c_size_t(0)
+        for c in range(self.n_contigs()):
+            if self.lib.contigNameGpu(self.h, c, None, 0, C.byref(n)) == _capi.SI_ERR_INVALID:
+                return []
+            buf = C.create_string_buffer(n.value + 1)
+            check(self.lib.contigNameGpu(self.h, c, buf, n.value + 1, C.byref(n)))
+            out.append(buf.value.decode("latin-1"))
+        return out
+
+    def bed_queries(self, text: bytes, half_open: bool = True):
+        """Queries from BED text on this index's contigs: (qs, qe, qc, line, stats)."""
+        st = _capi.cBedStats()
+        n = C.c_size_t(0)
+        flag = _capi.BED_HALF_OPEN if half_open else 0
+        bufs = [np.empty(1, self.dtype), np.empty(1, self.dtype), np.empty(1, np.int32), np.empty(1, np.int64)]
+        for cap in (0, None):
+            if cap is None:
+                cap = n.value
+                bufs = [np.empty(cap, self.dtype), np.empty(cap, self.dtype), np.empty(cap, np.int32),
+                        np.empty(cap, np.int64)]
+            r = self.lib.bedQueriesGpu(self.h, text, len(text), flag, *[_p(b) for b in bufs], cap, C.byref(n),
+                                       C.byref(st))
+            if r == _capi.SI_ERR_CAPACITY:
+                continue
+            check(r)
+            break
+        k = n.value
+        return bufs[0][:k], bufs[1][:k], bufs[2][:k], bufs[3][:k], self._stats(st)
+
     # -- index image (the Rust crate's serde counterpart, superintervals.rs:35-44) --
     def to_bytes(self) -> bytes:
         """The built index as one flat byte image."""

@@ -465,7 +465,7 @@ def test_index_image_roundtrip(api, tmp_path):
     assert np.array_equal(c.count(wl.q_starts, wl.q_ends, wl.q_contig),
                           a.count(wl.q_starts, wl.q_ends, wl.q_contig))
     bad = bytearray(img)
-    bad[-5] ^= 0x40                                     # inside the branch array
+    bad[-8 - 5] ^= 0x40                                 # inside the branch array (before the name count)
     with pytest.raises(api.SIError):
         api.GpuIndex(32).from_bytes(bytes(bad))
     with pytest.raises(api.SIError):
