@@ -38,6 +38,8 @@ sys.path.insert(0, ROOT)
 
 METRIC = ("overlap queries/s + result pairs/s on 1 GB300; % HBM peak; batched+learned vs plain")
 METRIC_SERVE = "serving loop on 1 GB300: queries/s (saturated) and p50/p99 request latency at the offered rate"
+ROW_OPS = ["intersect", "difference", "coverage", "keys", "bed_ingest"]
+ROW_DEFAULT_SCALE = 0.25   # full-size intersection pieces (25.5e9 x 12 B) would not fit in HBM
 METRIC_UB = "upper-bound queries/s on 1 GB300: learned two-stage index vs binary search, bit-identical"
 PEAK_FALLBACK_GBS = 6800.0
 
@@ -55,9 +57,10 @@ def parse():
     ap.add_argument("--scale", type=float, default=1.0, help="shrink N and Q (tests only)")
     ap.add_argument("--path", default="batched", choices=["batched", "plain", "auto"])
     ap.add_argument("--ub", default="learned", choices=["learned", "eytzinger", "binary"])
-    ap.add_argument("--op", default=None, choices=["search_idxs", "upper_bound"],
-                    help="search_idxs (default) or upper_bound (default for config4, whose "
-                         "full-size result, ~2.9e13 pairs, cannot be materialised)")
+    ap.add_argument("--op", default=None, choices=["search_idxs", "upper_bound"] + ROW_OPS,
+                    help="search_idxs (default); upper_bound (default for config4, whose full-size "
+                         "result, ~2.9e13 pairs, cannot be materialised); or one of the operations "
+                         "built on the path (intersect, difference, coverage, keys, bed_ingest)")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default batched-path tunables")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
@@ -495,6 +498,234 @@ def ub_line(args, res, world):
     return line
 
 
+# ----------------------------------------------------------------------------- operations on the path
+def run_gpu_rows(args, op, rank, world, dist):
+    """intersection / difference / coverage / search_keys over a device-resident batch of the
+    configuration-3 workload (scaled), through the device-buffer C-ABI calls."""
+    from superintervals_gb300 import _capi
+    from superintervals_gb300.interval_map import GpuIndex
+    lib = _capi.load()
+    scale = args.scale if args.scale != 1.0 else ROW_DEFAULT_SCALE
+    wl = make_workload(args.config, scale, rank)
+    s_bytes = wl.dtype.itemsize
+    idx = GpuIndex(64 if s_bytes == 8 else 32, 0)
+    idx.add_arrays(wl.starts, wl.ends, wl.data, seg=wl.seg if len(wl.seg) > 2 else None)
+    idx.build()
+    idx.set_path(_capi.PATH_AUTO)
+    idx.set_upper_bound(_capi.UB_LEARNED)
+    st = idx.stream
+    nq = wl.nq
+
+    def dalloc(nbytes):
+        p = C.c_void_p()
+        _capi.check(lib.deviceMallocGpu(C.byref(p), max(int(nbytes), 1)))
+        return p
+    bufs = []
+
+    def upload(a):
+        a = np.ascontiguousarray(a)
+        p = dalloc(a.nbytes)
+        _capi.check(lib.memcpyGpu(p, C.c_void_p(a.ctypes.data), a.nbytes, st))
+        bufs.append(p)
+        return p
+    d_qs, d_qe = upload(wl.q_starts), upload(wl.q_ends)
+    d_qc = upload(wl.q_contig) if wl.q_contig is not None else None
+    d_off = dalloc(8 * (nq + 1))
+    bufs.append(d_off)
+    total = C.c_size_t(0)
+    out = [None, None, None]
+
+    def call(cap):
+        if op == "intersect":
+            return lib.intersectDeviceGpu(idx.h, d_qs, d_qe, d_qc, nq, 0, d_off, out[0], out[1], out[2], cap,
+                                          C.byref(total), st)
+        if op == "difference":
+            return lib.differenceDeviceGpu(idx.h, d_qs, d_qe, d_qc, nq, d_off, out[0], out[1], cap, C.byref(total),
+                                           st)
+        if op == "keys":
+            return lib.searchKeysDeviceGpu(idx.h, d_qs, d_qe, d_qc, nq, 1, d_off, out[0], out[1], out[2], cap,
+                                           C.byref(total), st)
+        return lib.coverageDeviceGpu(idx.h, d_qs, d_qe, d_qc, nq, out[0], out[1], st)
+    if op == "coverage":
+        out[0], out[1] = dalloc(8 * nq), dalloc(s_bytes * nq)
+        P = nq
+    else:
+        r = call(0)
+        if r not in (_capi.SI_OK, _capi.SI_ERR_CAPACITY):
+            _capi.check(r)
+        P = int(total.value)
+        out[0], out[1], out[2] = dalloc(s_bytes * max(P, 1)), dalloc(s_bytes * max(P, 1)), dalloc(4 * max(P, 1))
+    bufs += [b for b in out if b]
+    hits = int(idx.count(wl.q_starts, wl.q_ends, wl.q_contig).astype(np.int64).sum())
+    ev = [C.c_void_p(), C.c_void_p()]
+    for e in ev:
+        _capi.check(lib.eventCreateGpu(C.byref(e)))
+
+    def step():
+        _capi.check(call(P))
+    for _ in range(args.warmup):
+        _capi.check(lib.flushL2Gpu(st))
+        step()
+    k0 = lib.getLaunchCountGpu()
+    total_ms = 0.0
+    with ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) as clk:
+        for _ in range(args.steps):
+            _capi.check(lib.flushL2Gpu(st))
+            _capi.check(lib.eventRecordGpu(ev[0], st))
+            step()
+            _capi.check(lib.eventRecordGpu(ev[1], st))
+            _capi.check(lib.streamSynchronizeGpu(st))
+            ms = C.c_float()
+            _capi.check(lib.eventElapsedMsGpu(ev[0], ev[1], C.byref(ms)))
+            total_ms += ms.value
+    launches = lib.getLaunchCountGpu() - k0
+    total_ms = max_over_ranks(total_ms, dist)
+    for b in bufs:
+        lib.deviceFreeGpu(b)
+    idx.close()
+    return {"wl": wl, "scale": scale, "nq": nq, "out": P, "hits": hits, "s_bytes": s_bytes,
+            "ms_per_step": total_ms / args.steps, "launches": launches, "clocks": clk.summary()}
+
+
+def rows_algorithmic_bytes(op, Q, H, P, s):
+    """Bytes the operation must move: every query read once and, per hit, the hit interval
+    read and the output written."""
+    if op == "intersect":
+        return Q * (2 * s + 8) + H * (2 * s) + P * (2 * s + 4), "Q(2s+8) + H(2s) + P(2s+4)"
+    if op == "difference":
+        return Q * (2 * s + 8) + H * (2 * s) + P * (2 * s), "Q(2s+8) + H(2s) + P(2s)"
+    if op == "keys":
+        return Q * (2 * s + 8) + H * (2 * s + 4) * 2, "Q(2s+8) + 2H(2s+4)"
+    return Q * (3 * s + 8) + H * (2 * s), "Q(3s+8) + H(2s)"
+
+
+def rows_cpu(op, wl, seconds, nth):
+    """The oracle's restatement of the operation on the host (contig 0's queries)."""
+    from oracle.oracle import ORDER_IDXS_CPP, Oracle
+    o = Oracle()
+    lo, hi = int(wl.seg[0]), int(wl.seg[1])
+    m = o.build(wl.starts[lo:hi], wl.ends[lo:hi], wl.data[lo:hi])
+    qc = wl.q_contig if wl.q_contig is not None else np.zeros(wl.nq, np.int32)
+    sel = np.nonzero(qc == 0)[0]
+    qs, qe = wl.q_starts[sel], wl.q_ends[sel]
+
+    def run(k):
+        if op == "intersect":
+            o.intersection(m, qs[:k], qe[:k], ORDER_IDXS_CPP)
+        elif op == "difference":
+            o.difference(m, qs[:k], qe[:k])
+        elif op == "coverage":
+            o.coverage(m, qs[:k], qe[:k])
+        else:
+            o.search_batch(m, qs[:k], qe[:k], order=1, values=True, nthreads=nth)
+    probe = min(len(sel), 2000)
+    t0 = time.perf_counter()
+    run(probe)
+    dt = max(time.perf_counter() - t0, 1e-6)
+    k = int(min(len(sel), max(probe, probe * seconds / dt)))
+    t0 = time.perf_counter()
+    run(k)
+    dt = time.perf_counter() - t0
+    threads = nth if op == "keys" else 1
+    return {"q_per_s": k / dt, "sample_q": k, "threads": threads}
+
+
+def rows_line(args, op, res, world):
+    Q, H, P, s = res["nq"], res["hits"], res["out"], res["s_bytes"]
+    ms = res["ms_per_step"]
+    peak, peak_kind = measured_peak()
+    algo, formula = rows_algorithmic_bytes(op, Q, H, 0 if op == "coverage" else P, s)
+    wl = res["wl"]
+    line = {"metric": f"{op} queries/s on 1 GB300 (device-resident)", "value": world * Q / (ms / 1e3),
+            "unit": "queries/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "int64" if s == 8 else "int32", "data": "synthetic (seeded)",
+            "config": dict(workload_desc(args.config, wl), op=op, scale=res["scale"],
+                           hits=H, outputs=P if op != "coverage" else Q),
+            "roofline": {"bound": "hbm", "achieved": algo / (ms / 1e3) / 1e9, "peak": peak, "unit": "GB/s",
+                         "frac": algo / (ms / 1e3) / 1e9 / peak, "traffic": None, "peak_kind": peak_kind,
+                         "algorithmic_bytes": algo, "formula": formula + " (Q queries, H hits, P outputs)"},
+            "gpu_launches": res["launches"], "clocks": res["clocks"]}
+    if not args.no_cpu:
+        nth = host_threads()
+        c = rows_cpu(op, wl, args.cpu_seconds, nth)
+        line["cpu_baseline"] = {"value": c["q_per_s"], "unit": "queries/s", "cores": c["threads"], "kind": "port",
+                                "sample": f"{c['sample_q']} queries of contig 0, {op}, {c['threads']} thread(s)"}
+    return line
+
+
+def bed_text(wl, seed=5):
+    """BED text of the workload's intervals (chrom names of the contig table, half-open ends),
+    in a seeded random line order."""
+    r = np.random.Generator(np.random.PCG64(seed))
+    order = r.permutation(wl.n)
+    G = len(wl.seg) - 1
+    cid = np.repeat(np.arange(G), np.diff(wl.seg))[order]
+    names = np.array([c[0].encode() for c in wl.contigs], dtype=object)
+    s = wl.starts[order].astype(np.int64)
+    e = wl.ends[order].astype(np.int64) + 1
+    cols = [names[cid], np.char.mod(b"%d", s).astype(object), np.char.mod(b"%d", e).astype(object)]
+    return b"\n".join(b"\t".join(t) for t in zip(*cols)) + b"\n"
+
+
+def run_bed(args, rank, world, dist):
+    """BED text (pinned host memory) -> GPU parse + contig dictionary + bucketing -> built index."""
+    from superintervals_gb300 import _capi
+    from superintervals_gb300.interval_map import GpuIndex
+    lib = _capi.load()
+    scale = args.scale if args.scale != 1.0 else ROW_DEFAULT_SCALE
+    wl = make_workload(args.config, scale, rank)
+    text = bed_text(wl)
+    hp = C.c_void_p()
+    _capi.check(lib.hostMallocPinnedGpu(C.byref(hp), len(text)))
+    C.memmove(hp, text, len(text))
+    idx = GpuIndex(32, 0)
+    stats = _capi.cBedStats()
+
+    def step():
+        _capi.check(lib.ingestBedGpu(idx.h, C.cast(hp, C.c_char_p), len(text), _capi.BED_HALF_OPEN,
+                                     C.byref(stats)))
+        _capi.check(lib.indexSuperIntervalsGpu(idx.h))
+    for _ in range(max(1, args.warmup)):
+        step()
+    k0 = lib.getLaunchCountGpu()
+    with ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) as clk:
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            step()
+        dt = max_over_ranks((time.perf_counter() - t0) / args.steps, dist)
+    res = {"wl": wl, "scale": scale, "bytes": len(text), "intervals": int(stats.intervals), "s": dt,
+           "launches": lib.getLaunchCountGpu() - k0, "clocks": clk.summary(), "names": idx.contig_names(),
+           "text": text}
+    lib.hostFreePinnedGpu(hp)
+    idx.close()
+    return res
+
+
+def bed_line(args, res, world):
+    from oracle.bed import parse_bed
+    wl = res["wl"]
+    line = {"metric": "BED intervals ingested + indexed per second on 1 GB300 (text in pinned host memory)",
+            "value": world * res["intervals"] / res["s"], "unit": "intervals/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * res["s"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic (seeded)",
+            "config": {"workload": f"BED text of {wl.name}", "scale": res["scale"], "text_bytes": res["bytes"],
+                       "contigs": len(res["names"]), "op": "ingestBedGpu + indexSuperIntervalsGpu"},
+            "text_GB_per_s": res["bytes"] / res["s"] / 1e9, "gpu_launches": res["launches"], "clocks": res["clocks"],
+            "e2e": {"value": world * res["intervals"] / res["s"], "unit": "intervals/s",
+                    "h2d_bytes_per_step": res["bytes"], "d2h_bytes_per_step": 12 * res["intervals"]}}
+    if not args.no_cpu:
+        text = res["text"]
+        cut = text.find(b"\n", min(len(text) - 1, 8_000_000)) + 1 or len(text)
+        t0 = time.perf_counter()
+        _, _, st = parse_bed(text[:cut])
+        dt = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": st["intervals"] / dt, "unit": "intervals/s", "cores": 1, "kind": "port",
+                                "sample": f"first {cut} bytes ({st['intervals']} lines) parsed by oracle/bed.py "
+                                          "(parse only, no index build)"}
+    return line
+
+
 # ----------------------------------------------------------------------------- serving loop
 def serving_workload(args):
     from superintervals_gb300 import workloads as W
@@ -703,6 +934,34 @@ def main():
     rank, world, dist = init_dist(args)
     cfg = args.config
     op = args.op or ("upper_bound" if cfg == "config4" else "search_idxs")
+    if args.impl == "reference" and op in ROW_OPS:
+        if rank != 0:
+            return
+        scale = args.scale if args.scale != 1.0 else ROW_DEFAULT_SCALE
+        wl = make_workload(cfg, scale, 0)
+        nth = host_threads()
+        if op == "bed_ingest":
+            from oracle.bed import parse_bed
+            text = bed_text(wl)
+            cut = text.find(b"\n", min(len(text) - 1, 8_000_000)) + 1 or len(text)
+            t0 = time.perf_counter()
+            _, _, stt = parse_bed(text[:cut])
+            dt = time.perf_counter() - t0
+            val, unit, cores = stt["intervals"] / dt, "intervals/s", 1
+            sample = f"first {cut} bytes parsed by oracle/bed.py"
+        else:
+            c = rows_cpu(op, wl, args.cpu_seconds, nth)
+            val, unit, cores = c["q_per_s"], "queries/s", c["threads"]
+            sample = f"{c['sample_q']} queries of contig 0, {op}"
+            dt = c["sample_q"] / max(val, 1e-9)
+        line = {"metric": f"{op} on the host (reference algorithm)", "value": val, "unit": unit,
+                "impl": "reference", "n_gpus": 1, "steps": 1, "warmup": 0, "ms_per_step": 1e3 * dt,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": str(wl.dtype),
+                "data": "synthetic (seeded)", "config": dict(workload_desc(cfg, wl), op=op, scale=scale),
+                "cpu_baseline": {"value": val, "unit": unit, "cores": cores, "kind": "port", "sample": sample},
+                "e2e": {"value": val, "unit": unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+        return
     if args.impl == "reference" and cfg == "config5":
         if rank != 0:
             return
@@ -777,6 +1036,16 @@ def main():
         res = run_serving(args, rank, world, dist)
         if rank == 0:
             print(json.dumps(serving_line(args, res, world)), flush=True)
+        return
+    if op == "bed_ingest":
+        res = run_bed(args, rank, world, dist)
+        if rank == 0:
+            print(json.dumps(bed_line(args, res, world)), flush=True)
+        return
+    if op in ROW_OPS:
+        res = run_gpu_rows(args, op, rank, world, dist)
+        if rank == 0:
+            print(json.dumps(rows_line(args, op, res, world)), flush=True)
         return
     if op == "upper_bound":
         res = run_gpu_ub(args, rank, world, dist)

@@ -107,3 +107,16 @@ def test_bench_serving_line_gpu():
     assert line["value"] > 0 and line["gpu_launches"] > 0
     assert 0 < line["latency_ms"]["p50"] <= line["latency_ms"]["p99"]
     assert "plain_gpu" in line and "cpu_baseline" in line and "e2e" in line
+
+
+@pytest.mark.parametrize("op", ["intersect", "difference", "coverage", "keys", "bed_ingest"])
+def test_reference_arm_rows(op):
+    (line,) = _run(["--impl", "reference", "--op", op, "--scale", "0.002", "--cpu-seconds", "0.3"])
+    assert line["impl"] == "reference" and line["value"] > 0 and line["config"]["op"] == op
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("op", ["intersect", "difference", "coverage", "keys", "bed_ingest"])
+def test_bench_rows_gpu(op):
+    (line,) = _run(["--op", op, "--scale", "0.004", "--steps", "2", "--warmup", "1", "--cpu-seconds", "0.3"])
+    assert line["value"] > 0 and line["gpu_launches"] > 0 and "cpu_baseline" in line
