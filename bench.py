@@ -42,6 +42,9 @@ ROW_OPS = ["intersect", "difference", "coverage", "keys", "bed_ingest"]
 ROW_DEFAULT_SCALE = 0.25   # full-size intersection pieces (25.5e9 x 12 B) would not fit in HBM
 METRIC_UB = "upper-bound queries/s on 1 GB300: learned two-stage index vs binary search, bit-identical"
 PEAK_FALLBACK_GBS = 6800.0
+# DRAM bytes (read + write) of one emit launch, from one ncu capture (dram__bytes_read.sum +
+# dram__bytes_write.sum) of exactly this workload: (config, scale, path) -> bytes per launch
+EMIT_TRAFFIC = {("config3", 1.0, "batched"): 124.15e9}
 
 
 def parse():
@@ -1079,8 +1082,10 @@ def main():
     emit_ms = ph[2] if ph[2] > 0 else ms
     algo = nq * (2 * s + 8) + P * (s + 4)
     achieved = algo / (emit_ms / 1000.0) / 1e9
+    traffic = EMIT_TRAFFIC.get((cfg, args.scale, args.path))
     line["roofline"] = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                        "frac": achieved / peak, "traffic": None, "kernel": "emit",
+                        "frac": achieved / peak, "traffic": traffic, "kernel": "emit",
+                        "traffic_frac": (traffic / (emit_ms / 1000.0) / 1e9 / peak) if traffic else None,
                         "peak_kind": peak_kind, "algorithmic_bytes": algo,
                         "phase_ms": {"count": ph[0], "scan": ph[1], "emit": ph[2], "prepare": ph[3]},
                         "whole_step_frac": (algo / (ms / 1000.0) / 1e9) / peak}

@@ -1030,6 +1030,48 @@ __global__ void __launch_bounds__(kThreads, 4) k_tiles(TileArgs<S> a) {
 }
 
 // ---- query keys: (class|contig, end) -------------------------------------------------
+// Smallest and largest query end as offset-binary (unsigned order = signed order).
+template <typename S>
+__global__ void k_qend_minmax(const S* __restrict__ qe, int64_t nq, unsigned long long* __restrict__ mm) {
+    unsigned long long lo = ~0ull, hi = 0ull;
+    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < nq; q += (int64_t)gridDim.x * blockDim.x) {
+        const unsigned long long v = (unsigned long long)(int64_t)qe[q] ^ 0x8000000000000000ull;
+        lo = v < lo ? v : lo;
+        hi = v > hi ? v : hi;
+    }
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) {
+        const unsigned long long a = __shfl_xor_sync(kFull, lo, d), b = __shfl_xor_sync(kFull, hi, d);
+        lo = a < lo ? a : lo;
+        hi = b > hi ? b : hi;
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicMin(&mm[0], lo);
+        atomicMax(&mm[1], hi);
+    }
+}
+
+// One 32-bit key per query: class code above the end's offset from the batch's smallest end,
+// shifted right by `shift` (tiles need queries grouped by class and contig and close in
+// position, not exactly ordered).  Also writes (start, end) interleaved for the prepare pass.
+template <typename S>
+__global__ void k_qkeys_packed(const S* __restrict__ qs, const S* __restrict__ qe, const int32_t* __restrict__ qc,
+                               int64_t nq, int64_t long_len, int G, const unsigned long long* __restrict__ mm,
+                               int shift, int ebits, uint32_t* __restrict__ key, uint32_t* __restrict__ pay,
+                               S* __restrict__ qpair) {
+    const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= nq) return;
+    const int32_t g = qc ? qc[q] : 0;
+    const S s = qs[q], e = qe[q];
+    const bool is_long = ((double)e - (double)s + 1.0) > (double)long_len;
+    const uint32_t code = (g < 0 || g >= G) ? 2u * (uint32_t)G : (uint32_t)g + (is_long ? (uint32_t)G : 0u);
+    const unsigned long long rel = ((unsigned long long)(int64_t)e ^ 0x8000000000000000ull) - mm[0];
+    key[q] = (code << ebits) | (uint32_t)(rel >> shift);
+    pay[q] = (uint32_t)q;
+    qpair[2 * q] = s;
+    qpair[2 * q + 1] = e;
+}
+
 template <typename S>
 __global__ void k_qkeys(const S* __restrict__ qs, const S* __restrict__ qe, const int32_t* __restrict__ qc,
                         int64_t nq, int64_t long_len, int G, uint32_t* w0, uint32_t* w1, uint32_t* wc,
@@ -1061,8 +1103,9 @@ constexpr int kPrepWindow = 2048;  // starts staged per block by the cooperative
 // there.  Otherwise each query searches on its own.
 template <typename S>
 __global__ void __launch_bounds__(kThreads) k_qprep(const uint32_t* __restrict__ pay,
-                                                    const uint32_t* __restrict__ wc,
+                                                    const uint32_t* __restrict__ wc, int code_shift,
                                                     const S* __restrict__ qs, const S* __restrict__ qe,
+                                                    const S* __restrict__ qpair,
                                                     int64_t nq, MapView<S> m, UbView<S> U,
                                                     S* __restrict__ sq_s, int32_t* __restrict__ sq_u,
                                                     uint32_t* __restrict__ sq_c, int32_t* __restrict__ sq_id,
@@ -1075,14 +1118,21 @@ __global__ void __launch_bounds__(kThreads) k_qprep(const uint32_t* __restrict__
     const int64_t j = jb + tid;
     const int64_t jl = (jb + kThreads < nq ? jb + kThreads : nq) - 1;  // last query of the block
     const bool valid = j < nq;
+    // the class code is the key word itself, or its top bits when the key is packed
     uint32_t orig = 0, cw = 0;
-    S v = 0;
+    S v = 0, vs = 0;
     if (valid) {
         orig = pay[j];
-        cw = wc[j];
-        v = qe[orig];
+        cw = wc[j] >> code_shift;
+        if (qpair) {
+            v = qpair[2 * (int64_t)orig + 1];
+            vs = qpair[2 * (int64_t)orig];
+        } else {
+            v = qe[orig];
+            vs = qs[orig];
+        }
     }
-    const uint32_t cfirst = wc[jb], clast = wc[jl];
+    const uint32_t cfirst = wc[jb] >> code_shift, clast = wc[jl] >> code_shift;
     const bool uniform = cfirst == clast && cfirst < 2u * (uint32_t)m.G;  // sorted: one code
     int g = (int)(cw >= (uint32_t)m.G ? cw - (uint32_t)m.G : cw);
     bool bad = false;
@@ -1144,7 +1194,7 @@ __global__ void __launch_bounds__(kThreads) k_qprep(const uint32_t* __restrict__
         const S* tr = (U.mode == 1) ? U.eytz_keys + (int64_t)g * U.eytz_n : nullptr;
         u = ub_search(U, g, m.starts + lo, n, v, tr);
     }
-    sq_s[j] = qs[orig];
+    sq_s[j] = vs;
     sq_u[j] = (int32_t)(lo + u);
     sq_c[j] = cw;
     sq_id[j] = (int32_t)orig;
@@ -1526,20 +1576,51 @@ int batched_prepare_queries(BatchedWorkspace& ws, MapView<S> m, const QueryBatch
     SI_OKR(ws.sq_u.reserve(sizeof(int32_t) * nq));
     SI_OKR(ws.sq_c.reserve(sizeof(uint32_t) * nq));
     SI_OKR(ws.sq_id.reserve(sizeof(int32_t) * nq));
+    // one packed key word when (class code, end offset >> shift) fits 24 bits with shift <= 16
+    // (three radix passes), else one word per 32 bits of end plus the class word
+    SI_OKR(ws.qminmax.reserve(2 * sizeof(unsigned long long)));
+    const unsigned long long init[2] = {~0ull, 0ull};
+    SI_CU(cudaMemcpyAsync(ws.qminmax.p, init, sizeof(init), cudaMemcpyHostToDevice, st));
+    k_qend_minmax<S><<<(unsigned)std::min<int64_t>(nblk(nq), 152 * 8), kThreads, 0, st>>>(
+        static_cast<const S*>(q.qe), nq, ws.qminmax.as<unsigned long long>());
+    note_launch();
+    unsigned long long mm[2] = {0, 0};
+    SI_CU(cudaMemcpyAsync(mm, ws.qminmax.p, sizeof(mm), cudaMemcpyDeviceToHost, st));
+    SI_CU(cudaStreamSynchronize(st));
+    const unsigned long long span = mm[1] - mm[0];
+    int code_bits = 1;
+    while (code_bits < 32 && ((uint64_t)1 << code_bits) <= (uint64_t)(2 * m.G)) ++code_bits;
+    int span_bits = 0;
+    while (span_bits < 64 && (span >> span_bits) != 0) ++span_bits;
+    const int shift = std::max(8, span_bits + code_bits - 24);
+    const bool packed = code_bits <= 16 && shift <= 16;
+    const int ebits = packed ? std::max(0, span_bits - shift) : 0;
+    int Kp = K;
     uint32_t* wc = kp[K - 1];
-    k_qkeys<S><<<nblk(nq), kThreads, 0, st>>>(static_cast<const S*>(q.qs), static_cast<const S*>(q.qe), q.qc, nq,
-                                              ws.prm.long_len, m.G, kp[0], K == 3 ? kp[1] : nullptr, wc,
-                                              ws.pay.as<uint32_t>());
+    if (packed) {
+        Kp = 1;
+        wc = kp[0];
+        SI_OKR(ws.qpair.reserve(2 * sizeof(S) * nq));
+        k_qkeys_packed<S><<<nblk(nq), kThreads, 0, st>>>(static_cast<const S*>(q.qs), static_cast<const S*>(q.qe),
+                                                         q.qc, nq, ws.prm.long_len, m.G,
+                                                         ws.qminmax.as<unsigned long long>(), shift, ebits, kp[0],
+                                                         ws.pay.as<uint32_t>(), ws.qpair.as<S>());
+    } else {
+        k_qkeys<S><<<nblk(nq), kThreads, 0, st>>>(static_cast<const S*>(q.qs), static_cast<const S*>(q.qe), q.qc,
+                                                  nq, ws.prm.long_len, m.G, kp[0], K == 3 ? kp[1] : nullptr, wc,
+                                                  ws.pay.as<uint32_t>());
+    }
     note_launch();
     SI_CU(cudaGetLastError());
     bool in_alt = false;
     int passes = 0;
-    SI_CU(radix_sort(kp, ka, ws.pay.as<uint32_t>(), ws.palt.as<uint32_t>(), K, nq, ws.sort_tmp.p, tb, &in_alt,
+    SI_CU(radix_sort(kp, ka, ws.pay.as<uint32_t>(), ws.palt.as<uint32_t>(), Kp, nq, ws.sort_tmp.p, tb, &in_alt,
                      &passes, st));
     const uint32_t* spay = in_alt ? ws.palt.as<uint32_t>() : ws.pay.as<uint32_t>();
-    const uint32_t* swc = in_alt ? ka[K - 1] : kp[K - 1];
+    const uint32_t* swc = in_alt ? ka[Kp - 1] : kp[Kp - 1];
     UbView<S> U = make_ub<S>(ws, ub_mode);
-    k_qprep<S><<<nblk(nq), kThreads, 0, st>>>(spay, swc, static_cast<const S*>(q.qs), static_cast<const S*>(q.qe),
+    k_qprep<S><<<nblk(nq), kThreads, 0, st>>>(spay, swc, packed ? ebits : 0, static_cast<const S*>(q.qs),
+                                              static_cast<const S*>(q.qe), packed ? ws.qpair.as<S>() : nullptr,
                                               nq, m, U, ws.sq_s.as<S>(), ws.sq_u.as<int32_t>(),
                                               ws.sq_c.as<uint32_t>(), ws.sq_id.as<int32_t>(), d_err);
     note_launch();

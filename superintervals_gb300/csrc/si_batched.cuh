@@ -54,6 +54,8 @@ struct BatchedWorkspace {
     UpperBoundModel ub;
     // query sort
     DBuf kw[3], kalt[3], pay, palt, sort_tmp;
+    DBuf qpair;                  // (start, end) per query, interleaved: one sector per gather
+    DBuf qminmax;                // smallest and largest query end (key packing)
     // sorted query records
     DBuf sq_s, sq_u, sq_c, sq_id;
     DBuf heads;                  // head-run length per query (original order)

@@ -420,6 +420,7 @@ int run_count(gSuperIntervals* si, const sig::QueryBatch& q, uint32_t* d_counts,
     SI_CK(cudaMemsetAsync(si->w_err.p, 0, sizeof(int), st));
     if (si->n == 0) {
         SI_CK(cudaMemsetAsync(d_counts, 0, sizeof(uint32_t) * std::max<int64_t>(q.nq, 1), st));
+        SI_CK(sig::launch_check_contigs(q.qc, q.nq, si->G, si->w_err.as<int>(), st));
         return SI_OK;
     }
     if (use_batched(si, q.nq)) {
@@ -491,9 +492,7 @@ int upload_queries(gSuperIntervals* si, const S* qs, const S* qe, const int32_t*
     q.qe = si->wq_e.p;
     q.qc = nullptr;
     if (qc) {
-        for (size_t i = 0; i < nq; ++i)
-            if (qc[i] < 0 || qc[i] >= si->G)
-                return fail(SI_ERR_INVALID, "query %zu names contig %d outside [0, %d)", i, qc[i], si->G);
+        // contig ids are checked on the device by the kernels that read them (error word)
         SI_TRY(si->wq_c.reserve(sizeof(int32_t) * std::max<size_t>(nq, 1)));
         if (nq) SI_CK(cudaMemcpyAsync(si->wq_c.p, qc, sizeof(int32_t) * nq, cudaMemcpyHostToDevice, si->st));
         q.qc = si->wq_c.as<int32_t>();
@@ -610,7 +609,8 @@ int any_host(gSuperIntervals* si, const S* qs, const S* qe, const int32_t* qc, s
     SI_CK(cudaMemsetAsync(si->w_err.p, 0, sizeof(int), si->st));
     if (si->n == 0) {
         memset(out, 0, nq);
-        return SI_OK;
+        SI_CK(sig::launch_check_contigs(q.qc, q.nq, si->G, si->w_err.as<int>(), si->st));
+        return read_dev_err(si);
     }
     SI_TRY(si->w_out.reserve(std::max<size_t>(nq, 1)));
     SI_CK(sig::launch_any_plain<S>(view<S>(si), q, si->w_out.as<uint8_t>(), si->w_err.as<int>(), si->st));
@@ -1552,6 +1552,9 @@ int lists_or_empty(gSuperIntervals* si, const sig::QueryBatch& q, int order, cud
         SI_TRY(si->so_hoff.reserve(sizeof(int64_t) * (q.nq + 1)));
         SI_TRY(si->so_hits.reserve(sizeof(int32_t)));
         SI_CK(cudaMemsetAsync(si->so_hoff.p, 0, sizeof(int64_t) * (q.nq + 1), st));
+        SI_CK(cudaMemsetAsync(si->w_err.p, 0, sizeof(int), st));
+        SI_CK(sig::launch_check_contigs(q.qc, q.nq, si->G, si->w_err.as<int>(), st));
+        SI_TRY(read_dev_err(si, st));
         *P = 0;
     }
     return SI_OK;

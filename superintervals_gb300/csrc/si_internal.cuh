@@ -221,6 +221,10 @@ cudaError_t launch_coverage(MapView<S> m, QueryBatch q, const int64_t* hoff, con
 template <typename S>
 cudaError_t launch_any_inverted(MapView<S> m, int* flag, cudaStream_t st);
 
+// error word = kDevBadContig when a contig id is outside [0, G) (for empty indexes, where no
+// other kernel reads the ids)
+cudaError_t launch_check_contigs(const int32_t* qc, int64_t nq, int G, int* d_err, cudaStream_t st);
+
 // plain one-query-per-thread path: upper_bound + branch walk per query
 template <typename S>
 cudaError_t launch_count_plain(MapView<S> m, QueryBatch q, uint32_t* counts, int* d_err,

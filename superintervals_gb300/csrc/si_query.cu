@@ -155,7 +155,19 @@ inline unsigned blocks_for(int64_t n) {
     return (unsigned)std::max<int64_t>(1, ceil_div(n, kThreads));
 }
 
+__global__ void k_check_contigs(const int32_t* __restrict__ qc, int64_t nq, int G, int* d_err) {
+    const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q < nq && (qc[q] < 0 || qc[q] >= G)) atomicCAS(d_err, kDevOk, kDevBadContig);
+}
+
 }  // namespace
+
+cudaError_t launch_check_contigs(const int32_t* qc, int64_t nq, int G, int* d_err, cudaStream_t st) {
+    if (!qc || nq <= 0) return cudaSuccess;
+    k_check_contigs<<<blocks_for(nq), kThreads, 0, st>>>(qc, nq, G, d_err);
+    note_launch();
+    return cudaGetLastError();
+}
 
 template <typename S>
 cudaError_t launch_count_plain(MapView<S> m, QueryBatch q, uint32_t* counts, int* d_err,
