@@ -321,6 +321,15 @@ def run_gpu(args, rank, world, dist):
         res["e2e_s"] = max_over_ranks(e2e_s, dist)
         res["h2d_bytes"] = wl.q_starts.nbytes + wl.q_ends.nbytes + (wl.q_contig.nbytes if hq_c else 0)
         res["d2h_bytes"] = 8 * (nq + 1) + 4 * P
+        # the host link this box gives: one large device-to-host copy into the same pinned buffer
+        link = min(4 * P, 8 << 30)
+        if link >= (64 << 20):
+            d_tmp = dalloc(link)
+            t0 = time.perf_counter()
+            _capi.check(lib.memcpyGpu(h_out, d_tmp, link, st))
+            _capi.check(lib.streamSynchronizeGpu(st))
+            res["d2h_link_GBps"] = link / (time.perf_counter() - t0) / 1e9
+            lib.deviceFreeGpu(d_tmp)
         for p in (hq_s, hq_e, hq_c, h_off, h_out):
             if p:
                 lib.hostFreePinnedGpu(p)
@@ -1096,7 +1105,8 @@ def main():
     if "e2e_s" in res:
         line["e2e"] = {"value": world * nq / res["e2e_s"], "unit": "queries/s",
                        "h2d_bytes_per_step": res["h2d_bytes"], "d2h_bytes_per_step": res["d2h_bytes"],
-                       "pairs_per_s": world * P / res["e2e_s"]}
+                       "pairs_per_s": world * P / res["e2e_s"], "d2h_link_GBps": res.get("d2h_link_GBps"),
+                       "ms_per_step": 1e3 * res["e2e_s"]}
     if not args.no_cpu:
         nth = host_threads()
         c = cpu_run(wl, args.cpu_seconds, nth)
