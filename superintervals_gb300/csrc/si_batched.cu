@@ -132,6 +132,7 @@ struct TileArgs {
     Pyr<S> P;
     Pyr<S> PL;               // pyramid over the long-interval list (intervals >= long_split long)
     const int32_t* long_pos; // its global positions, in position order
+    const int64_t* blk_cut;  // per tile of 256 queries: (p_cut, long-list end) or -1; null: none
     const int64_t* long_seg; // first list index of each contig
     int64_t long_split;
     const S* starts;
@@ -672,7 +673,20 @@ __global__ void __launch_bounds__(kThreads, 4) k_tiles(TileArgs<S> a) {
                     // positions below p_cut hold intervals starting more than long_split before L;
                     // those that reach L are at least long_split long, so they are gathered from
                     // the long-interval list instead of the whole position range
-                    if (warp == 0) {
+                    // precomputed by the prepare pass for a tile that is one block of sorted queries
+                    // of one contig (valid when it lies inside [lo, umax + 1])
+                    int64_t pre_pc = -1, pre_ch = -1;
+                    if (a.blk_cut && r0 == 0 && r1 == nt) {
+                        pre_pc = a.blk_cut[2 * t];
+                        pre_ch = a.blk_cut[2 * t + 1];
+                        if (pre_pc < lo || pre_pc > umax + 1) pre_pc = -1;
+                    }
+                    if (pre_pc >= 0) {
+                        if (tid == 0) {
+                            s_cut[0] = pre_pc;
+                            s_cut[1] = pre_ch;
+                        }
+                    } else if (warp == 0) {
                         const int64_t pc =
                             umax < lo ? lo : warp_first_near<S>(a.starts, lo, umax + 1, L, a.long_split, lane);
                         const int64_t ch = warp_first_pos_geq(a.long_pos, a.long_seg[g], a.long_seg[g + 1], pc, lane);
@@ -1109,9 +1123,12 @@ __global__ void __launch_bounds__(kThreads) k_qprep(const uint32_t* __restrict__
                                                     int64_t nq, MapView<S> m, UbView<S> U,
                                                     S* __restrict__ sq_s, int32_t* __restrict__ sq_u,
                                                     uint32_t* __restrict__ sq_c, int32_t* __restrict__ sq_id,
-                                                    int* d_err) {
+                                                    int* d_err, int64_t long_split,
+                                                    const int32_t* __restrict__ long_pos,
+                                                    const int64_t* __restrict__ long_seg,
+                                                    int64_t* __restrict__ blk_cut) {
     __shared__ S win[kPrepWindow];
-    __shared__ S s_mn[kWarpsPerCta], s_mx[kWarpsPerCta];
+    __shared__ S s_mn[kWarpsPerCta], s_mx[kWarpsPerCta], s_mq[kWarpsPerCta];
     __shared__ int64_t s_a, s_b;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int64_t jb = (int64_t)blockIdx.x * kThreads;
@@ -1147,20 +1164,40 @@ __global__ void __launch_bounds__(kThreads) k_qprep(const uint32_t* __restrict__
     const int64_t n = m.seg[g + 1] - lo;
     int64_t u = -1;
     bool done = false;
+    if (blk_cut && tid == 0 && !uniform) blk_cut[2 * blockIdx.x] = -1;
     if (uniform) {
-        S mn = valid ? v : Lim<S>::hi, mx = valid ? v : Lim<S>::lo;
+        S mn = valid ? v : Lim<S>::hi, mx = valid ? v : Lim<S>::lo, mq = valid ? vs : Lim<S>::hi;
 #pragma unroll
         for (int d = 16; d > 0; d >>= 1) {
             const S o = __shfl_xor_sync(kFull, mn, d);
             mn = o < mn ? o : mn;
             const S p = __shfl_xor_sync(kFull, mx, d);
             mx = p > mx ? p : mx;
+            const S r = __shfl_xor_sync(kFull, mq, d);
+            mq = r < mq ? r : mq;
         }
         if (lane == 0) {
             s_mn[warp] = mn;
             s_mx[warp] = mx;
+            s_mq[warp] = mq;
         }
         __syncthreads();
+        if (blk_cut && warp == 1) {
+            // for the tile of these queries (warp 1, beside warp 0's searches): p_cut = first
+            // position whose start is within long_split of the smallest qs, and the first
+            // long-list index at or after it
+            int64_t pc = -1, ch = -1;
+            if (cfirst < (uint32_t)m.G && n > 0) {
+                S L = s_mq[0];
+                for (int w = 1; w < kWarpsPerCta; ++w) L = s_mq[w] < L ? s_mq[w] : L;
+                pc = warp_first_near<S>(m.starts, lo, lo + n, L, long_split, lane);
+                ch = warp_first_pos_geq(long_pos, long_seg[g], long_seg[g + 1], pc, lane);
+            }
+            if (lane == 0) {
+                blk_cut[2 * blockIdx.x] = pc;
+                blk_cut[2 * blockIdx.x + 1] = ch;
+            }
+        }
         if (tid < 2 && n > 0) {
             S x = tid == 0 ? s_mn[0] : s_mx[0];  // thread 0: smallest end, thread 1: largest
             for (int w = 1; w < kWarpsPerCta; ++w)
@@ -1619,10 +1656,12 @@ int batched_prepare_queries(BatchedWorkspace& ws, MapView<S> m, const QueryBatch
     const uint32_t* spay = in_alt ? ws.palt.as<uint32_t>() : ws.pay.as<uint32_t>();
     const uint32_t* swc = in_alt ? ka[Kp - 1] : kp[Kp - 1];
     UbView<S> U = make_ub<S>(ws, ub_mode);
+    SI_OKR(ws.blk_cut.reserve(2 * sizeof(int64_t) * (size_t)nblk(nq)));
     k_qprep<S><<<nblk(nq), kThreads, 0, st>>>(spay, swc, packed ? ebits : 0, static_cast<const S*>(q.qs),
                                               static_cast<const S*>(q.qe), packed ? ws.qpair.as<S>() : nullptr,
                                               nq, m, U, ws.sq_s.as<S>(), ws.sq_u.as<int32_t>(),
-                                              ws.sq_c.as<uint32_t>(), ws.sq_id.as<int32_t>(), d_err);
+                                              ws.sq_c.as<uint32_t>(), ws.sq_id.as<int32_t>(), d_err, ws.long_split,
+                                              ws.long_pos, ws.long_seg, ws.long_pos ? ws.blk_cut.as<int64_t>() : nullptr);
     note_launch();
     SI_CU(cudaGetLastError());
     ws.launches += 2 + 3 * passes + 1;
@@ -1646,6 +1685,7 @@ static int run_tiles(BatchedWorkspace& ws, MapView<S> m, Levels<S> L, int H, int
     a.PL.H = ws.long_H;
     a.long_pos = ws.long_pos;
     a.long_seg = ws.long_seg;
+    a.blk_cut = (ws.prm.tile_q == kThreads && ws.blk_cut.p) ? ws.blk_cut.as<int64_t>() : nullptr;
     a.long_split = ws.long_split;
     a.starts = m.starts;
     a.split_len = ws.prm.split_len;
