@@ -1263,8 +1263,9 @@ __global__ void k_ub_plain(const S* __restrict__ qe, const int32_t* __restrict__
 }
 
 // ---- learned upper-bound model: GPU least squares ---------------------------------------
-// Per contig: root regression of position on key (centred), then per leaf a regression over
-// the contiguous key range the root sends to it, then the leaf's max error.
+// Per contig: the sorted starts cut into equal-count leaves whose first keys form the root;
+// per leaf a least-squares line of position on key (centred on the contig's mean key), then
+// the leaf's max errors.
 
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
@@ -1283,51 +1284,31 @@ __device__ double block_sum(double v, double* red) {
     return t;
 }
 
-// acc[g] += {sum x, sum x^2-ish}: pass 1 sums keys, pass 2 sums centred products.
+// acc[g] += sum of the contig's keys (their mean conditions the leaf fits).
 template <typename S>
-__global__ void k_root_sums(const S* __restrict__ starts, const int64_t* __restrict__ seg, int G,
-                            const double* __restrict__ mean_x, double* __restrict__ acc, int pass) {
+__global__ void k_key_sums(const S* __restrict__ starts, const int64_t* __restrict__ seg, int G,
+                           double* __restrict__ acc) {
     __shared__ double red[32];
     for (int g = blockIdx.y; g < G; g += gridDim.y) {
         const int64_t lo = seg[g], n = seg[g + 1] - lo;
-        const double my = 0.5 * (double)(n - 1);
-        double a0 = 0, a1 = 0;
-        for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
-            const double x = (double)starts[lo + k];
-            if (pass == 0) {
-                a0 += x;
-            } else {
-                const double dx = x - mean_x[g], dy = (double)k - my;
-                a0 += dx * dy;
-                a1 += dx * dx;
-            }
-        }
+        double a0 = 0;
+        for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x)
+            a0 += (double)starts[lo + k];
         a0 = block_sum(a0, red);
-        a1 = block_sum(a1, red);
-        if (threadIdx.x == 0) {
-            atomicAdd(&acc[2 * g], a0);
-            atomicAdd(&acc[2 * g + 1], a1);
-        }
+        if (threadIdx.x == 0) atomicAdd(&acc[g], a0);
     }
 }
 
-// leaf boundaries: bnd[base_g + l] = first local position whose root leaf >= l
+// The root of the learned model: each leaf's first key.
 template <typename S>
-__global__ void k_leaf_bounds(const S* __restrict__ starts, const int64_t* __restrict__ seg, int G,
-                              const double2* __restrict__ root, const double* __restrict__ mean_x,
-                              const int32_t* __restrict__ leaf_base, int32_t* __restrict__ bnd) {
-    const int g = blockIdx.y;
+__global__ void k_leaf_keys(const S* __restrict__ starts, const int64_t* __restrict__ seg,
+                            const int32_t* __restrict__ leaf_contig, const int32_t* __restrict__ leaf_pos, int total,
+                            S* __restrict__ leaf_key) {
+    const int L = blockIdx.x * blockDim.x + threadIdx.x;
+    if (L >= total) return;
+    const int g = leaf_contig[L];
     const int64_t lo = seg[g], n = seg[g + 1] - lo;
-    const int base = leaf_base[g], nl = leaf_base[g + 1] - base;
-    for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
-        auto leaf_of = [&](int64_t kk) {
-            const double lf = root[g].x * ((double)starts[lo + kk] - mean_x[g]) + root[g].y;
-            return lf <= 0.0 ? 0 : (lf >= (double)(nl - 1) ? nl - 1 : (int)lf);
-        };
-        const int lk = leaf_of(k);
-        const int lp = (k == 0) ? -1 : leaf_of(k - 1);
-        for (int l = lp + 1; l <= lk; ++l) bnd[base + l] = (int32_t)k;
-    }
+    leaf_key[L] = n > 0 ? starts[lo + leaf_pos[L]] : Lim<S>::lo;
 }
 
 template <typename S>
@@ -1440,8 +1421,9 @@ template <typename S>
 UbView<S> make_ub(const BatchedWorkspace& ws, int mode) {
     UbView<S> U;
     U.mode = mode;
-    U.root = ws.ub.root.as<double2>();
     U.leaf_base = ws.ub.leaf_base.as<int32_t>();
+    U.leaf_key = ws.ub.leaf_key.as<S>();
+    U.leaf_pos = ws.ub.leaf_pos.as<int32_t>();
     U.leaves = ws.ub.leaves.as<LeafModel>();
     U.key_mean = ws.ub.key_mean.as<double>();
     U.eytz_keys = ws.ub.eytz_keys.as<S>();
@@ -1474,29 +1456,34 @@ int build_learned(BatchedWorkspace& ws, MapView<S> m, cudaStream_t st) {
     std::vector<int64_t> seg(G + 1);
     SI_CU(cudaMemcpyAsync(seg.data(), m.seg, sizeof(int64_t) * (G + 1), cudaMemcpyDeviceToHost, st));
     SI_CU(cudaStreamSynchronize(st));
-    std::vector<int32_t> base(G + 1, 0), leaf_contig;
+    // equal-count leaves: up to 4096 per contig, at least 64 keys each
+    std::vector<int32_t> base(G + 1, 0), leaf_contig, leaf_pos;
     for (int g = 0; g < G; ++g) {
         const int64_t n = seg[g + 1] - seg[g];
         const int nl = (int)std::min<int64_t>(4096, std::max<int64_t>(1, n / 64));
         base[g + 1] = base[g] + nl;
-        for (int l = 0; l < nl; ++l) leaf_contig.push_back(g);
+        for (int l = 0; l < nl; ++l) {
+            leaf_contig.push_back(g);
+            leaf_pos.push_back((int32_t)((int64_t)l * n / nl));
+        }
     }
     const int total = base[G];
     ws.ub.total_leaves = total;
-    DBuf acc, lc, bnd;
+    DBuf acc, lc;
     SI_OKR(acc.reserve(sizeof(double) * 2 * G));
     SI_OKR(ws.ub.key_mean.reserve(sizeof(double) * G));
-    SI_OKR(ws.ub.root.reserve(sizeof(double2) * G));
     SI_OKR(ws.ub.leaf_base.reserve(sizeof(int32_t) * (G + 1)));
     SI_OKR(ws.ub.leaves.reserve(sizeof(LeafModel) * std::max(total, 1)));
+    SI_OKR(ws.ub.leaf_pos.reserve(sizeof(int32_t) * std::max(total, 1)));
+    SI_OKR(ws.ub.leaf_key.reserve(sizeof(S) * std::max(total, 1)));
     SI_OKR(lc.reserve(sizeof(int32_t) * std::max(total, 1)));
-    SI_OKR(bnd.reserve(sizeof(int32_t) * std::max(total, 1)));
     SI_CU(cudaMemcpyAsync(ws.ub.leaf_base.p, base.data(), sizeof(int32_t) * (G + 1), cudaMemcpyHostToDevice, st));
     SI_CU(cudaMemcpyAsync(lc.p, leaf_contig.data(), sizeof(int32_t) * total, cudaMemcpyHostToDevice, st));
-    // pass 1: mean key per contig
+    SI_CU(cudaMemcpyAsync(ws.ub.leaf_pos.p, leaf_pos.data(), sizeof(int32_t) * total, cudaMemcpyHostToDevice, st));
+    // mean key per contig (conditioning of the leaf fits)
     SI_CU(cudaMemsetAsync(acc.p, 0, sizeof(double) * 2 * G, st));
     dim3 grid(64, (unsigned)std::min(G, 65535));
-    k_root_sums<S><<<grid, kThreads, 0, st>>>(m.starts, m.seg, G, nullptr, acc.as<double>(), 0);
+    k_key_sums<S><<<grid, kThreads, 0, st>>>(m.starts, m.seg, G, acc.as<double>());
     note_launch();
     SI_CU(cudaGetLastError());
     std::vector<double> a(2 * G), mean(G);
@@ -1504,49 +1491,21 @@ int build_learned(BatchedWorkspace& ws, MapView<S> m, cudaStream_t st) {
     SI_CU(cudaStreamSynchronize(st));
     for (int g = 0; g < G; ++g) {
         const int64_t n = seg[g + 1] - seg[g];
-        mean[g] = n > 0 ? a[2 * g] / (double)n : 0.0;
+        mean[g] = n > 0 ? a[g] / (double)n : 0.0;
     }
     SI_CU(cudaMemcpyAsync(ws.ub.key_mean.p, mean.data(), sizeof(double) * G, cudaMemcpyHostToDevice, st));
-    // pass 2: centred products -> root slope; root maps key to leaf coordinate
-    SI_CU(cudaMemsetAsync(acc.p, 0, sizeof(double) * 2 * G, st));
-    k_root_sums<S><<<grid, kThreads, 0, st>>>(m.starts, m.seg, G, ws.ub.key_mean.as<double>(), acc.as<double>(), 1);
+    // the root (first key of every leaf), then each leaf's least-squares line and max errors
+    k_leaf_keys<S><<<nblk(total), kThreads, 0, st>>>(m.starts, m.seg, lc.as<int32_t>(), ws.ub.leaf_pos.as<int32_t>(),
+                                                     total, ws.ub.leaf_key.as<S>());
     note_launch();
     SI_CU(cudaGetLastError());
-    SI_CU(cudaMemcpyAsync(a.data(), acc.p, sizeof(double) * 2 * G, cudaMemcpyDeviceToHost, st));
-    SI_CU(cudaStreamSynchronize(st));
-    std::vector<double2> root(G);
-    for (int g = 0; g < G; ++g) {
-        const int64_t n = seg[g + 1] - seg[g];
-        const int nl = base[g + 1] - base[g];
-        const double slope_pos = (a[2 * g + 1] > 0 && a[2 * g] > 0) ? a[2 * g] / a[2 * g + 1] : 0.0;
-        const double scale = n > 0 ? (double)nl / (double)n : 0.0;
-        // position ~ my + slope * (x - mean); leaf = position * nl / n
-        root[g] = make_double2(slope_pos * scale, 0.5 * (double)(n - 1) * scale);
-    }
-    SI_CU(cudaMemcpyAsync(ws.ub.root.p, root.data(), sizeof(double2) * G, cudaMemcpyHostToDevice, st));
-    SI_CU(cudaMemsetAsync(bnd.p, 0x7f, sizeof(int32_t) * total, st));
-    k_leaf_bounds<S><<<dim3(256, G), kThreads, 0, st>>>(m.starts, m.seg, G, ws.ub.root.as<double2>(),
-                                                        ws.ub.key_mean.as<double>(), ws.ub.leaf_base.as<int32_t>(),
-                                                        bnd.as<int32_t>());
-    note_launch();
-    SI_CU(cudaGetLastError());
-    // leaves never reached by any key keep INT32_MAX-ish: clamp to the contig size on the host
-    std::vector<int32_t> hb(total);
-    SI_CU(cudaMemcpyAsync(hb.data(), bnd.p, sizeof(int32_t) * total, cudaMemcpyDeviceToHost, st));
-    SI_CU(cudaStreamSynchronize(st));
-    for (int g = 0; g < G; ++g) {
-        const int32_t n = (int32_t)(seg[g + 1] - seg[g]);
-        for (int l = base[g]; l < base[g + 1]; ++l)
-            if (hb[l] > n) hb[l] = n;
-    }
-    SI_CU(cudaMemcpyAsync(bnd.p, hb.data(), sizeof(int32_t) * total, cudaMemcpyHostToDevice, st));
     k_leaf_fit<S><<<(unsigned)std::min(total, 152 * 32), kThreads, 0, st>>>(
-        m.starts, m.seg, lc.as<int32_t>(), ws.ub.leaf_base.as<int32_t>(), bnd.as<int32_t>(),
+        m.starts, m.seg, lc.as<int32_t>(), ws.ub.leaf_base.as<int32_t>(), ws.ub.leaf_pos.as<int32_t>(),
         ws.ub.key_mean.as<double>(), ws.ub.leaves.as<LeafModel>(), total);
     note_launch();
     SI_CU(cudaGetLastError());
     SI_CU(cudaStreamSynchronize(st));
-    ws.launches += 5;
+    ws.launches += 3;
     return SI_OK;
 }
 

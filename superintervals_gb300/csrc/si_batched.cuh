@@ -36,8 +36,9 @@ struct UpperBoundModel {
     int mode = 0;                // SI_UB_*
     int G = 0;
     // learned: two-stage piecewise-linear model per contig
-    DBuf root;                   // double2 per contig: (slope, intercept) of key -> leaf
     DBuf leaf_base;              // int32 per contig+1: first leaf of each contig
+    DBuf leaf_key;               // S per leaf: its first key (the root, equal-count leaves)
+    DBuf leaf_pos;               // int32 per leaf: its first contig-local position
     DBuf leaves;                 // LeafModel per leaf
     DBuf key_mean;               // double per contig: key offset for conditioning
     int total_leaves = 0;

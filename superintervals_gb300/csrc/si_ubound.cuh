@@ -6,10 +6,15 @@
 //              (Eytzinger) tree -- the layout of IntervalMapEytz (hpp:1457-1535), here only
 //              as an accelerator: the tree picks a bucket of sorted positions, a bounded
 //              halving search inside the bucket gives the answer;
-//   learned    a two-stage piecewise-linear model (root model -> one of up to 4096 leaf
-//              segments -> predicted position) with each leaf's stored max error; a bounded
-//              search inside the error window, then a two-read check of the answer, with the
-//              full halving search as fallback whenever the check fails.
+//   learned    a two-stage piecewise-linear model.  Stage 1 (root): the contig's sorted starts
+//              cut into up to 4096 leaves of equal count; the leaves' first keys form a
+//              piecewise-linear map from key to leaf, searched per query.  Stage 2: each leaf
+//              a least-squares line (key -> position) with its stored max errors.  The answer
+//              lies inside the chosen leaf's position range, so the error window is clamped
+//              to it; a two-read check of the answer falls back to a halving search over the
+//              leaf whenever it fails (exact either way).  Equal-count leaves keep every leaf
+//              small where keys are clustered (a root line over the key range would put a
+//              whole hotspot into one leaf).
 #pragma once
 #include "si_internal.cuh"
 
@@ -27,8 +32,9 @@ template <typename S>
 struct UbView {
     int mode;                    // SI_UB_*: 0 binary, 1 eytzinger, 2 learned
     // learned
-    const double2* root;         // per contig: (slope, intercept) key -> leaf coordinate
-    const int32_t* leaf_base;    // per contig+1
+    const int32_t* leaf_base;    // per contig+1: first leaf of each contig
+    const S* leaf_key;           // per leaf: its first key (the root)
+    const int32_t* leaf_pos;     // per leaf: its first contig-local position
     const LeafModel* leaves;
     const double* key_mean;      // per contig: key origin
     // eytzinger
@@ -85,23 +91,31 @@ __device__ __forceinline__ int64_t ub_search(const UbView<S>& U, int g, const S*
     }
     if (U.mode == 2 && U.leaves) {
         if (v < starts[0]) return -1;
-        const double x = (double)v - U.key_mean[g];
-        const double2 rt = U.root[g];
         const int base = U.leaf_base[g];
         const int nl = U.leaf_base[g + 1] - base;
-        double lf = rt.x * x + rt.y;
-        int l = lf <= 0.0 ? 0 : (lf >= (double)(nl - 1) ? nl - 1 : (int)lf);
-        const LeafModel M = U.leaves[base + l];
-        const double pred = M.y0 + M.slope * (x - M.x0);
-        double plo = pred - (double)M.err_lo - 1.0, phi = pred + (double)M.err_hi + 1.0;
-        int64_t a = plo <= 0.0 ? 0 : (plo >= (double)(n - 1) ? n - 1 : (int64_t)plo);
-        int64_t b = phi <= 0.0 ? 0 : (phi >= (double)(n - 1) ? n - 1 : (int64_t)phi + 1);
-        if (b > n - 1) b = n - 1;
+        // root: the last leaf whose first key is <= v (leaf 0 starts at starts[0] <= v)
+        const S* __restrict__ lk = U.leaf_key + base;
+        int l0 = 0, len = nl;
+        while (len > 1) {
+            const int half = len >> 1;
+            l0 += (lk[l0 + half] <= v) ? (len - half) : 0;
+            len = half;
+        }
+        if (lk[l0] > v) --l0;  // >= 0: lk[0] = starts[0] <= v
+        // the answer lies in the leaf: starts[pa] <= v < starts[first position of leaf l0 + 1]
+        const int64_t pa = U.leaf_pos[base + l0];
+        const int64_t pb = (l0 + 1 < nl ? (int64_t)U.leaf_pos[base + l0 + 1] : n) - 1;
+        const LeafModel M = U.leaves[base + l0];
+        const double pred = M.y0 + M.slope * ((double)v - U.key_mean[g] - M.x0);
+        const double plo = pred - (double)M.err_lo - 1.0, phi = pred + (double)M.err_hi + 1.0;
+        int64_t a = plo <= (double)pa ? pa : (plo >= (double)pb ? pb : (int64_t)plo);
+        int64_t b = phi >= (double)pb ? pb : (phi <= (double)pa ? pa : (int64_t)phi + 1);
+        if (b > pb) b = pb;
         const int64_t r = ub_range(starts, a, b, v);
-        const bool ok_lo = (r < 0) ? (v < starts[0]) : (starts[r] <= v);
+        const bool ok_lo = r >= pa && starts[r] <= v;
         const bool ok_hi = (r + 1 >= n) || (starts[r + 1] > v);
         if (ok_lo && ok_hi) return r;
-        // the model's window missed: full search (exact either way)
+        return ub_range(starts, pa, pb, v);  // the window missed: the whole leaf
     }
     return ub_range(starts, (int64_t)0, n - 1, v);
 }
