@@ -4,22 +4,25 @@
 // loop over IntervalMap::search_idxs, hpp:879-905).  Queries that lie close together on a contig
 // hit nearly the same intervals, so here they are answered together:
 //
-//  1. prepare: queries are radix-sorted by (class, contig, end); each sorted query gets its
-//     upper bound (binary / Eytzinger / learned, si_ubound.cuh).  "class" puts queries longer
-//     than a threshold after the short ones.
-//  2. tiles: a CTA takes `tile_q` consecutive sorted short queries of one contig.  One warp
-//     gathers the candidate set C = { k <= max ub : ends[k] >= min qs } of the tile into
-//     shared memory, in descending position order, by walking the max-of-32 pyramid of ends
-//     (whole 32-chunk groups at a time, coalesced 128-byte loads, chunk runs whose max end is
-//     below the threshold skipped).  C holds every hit of every query of the tile.  Then each
-//     warp filters C for one query at a time (k <= ub_q and ends[k] >= qs_q) with ballots:
-//     the count pass counts and records the query's head-run length (the run of consecutive
-//     hits ending at ub), the emit pass writes the head run arithmetically (ascending for the
+//  1. prepare: queries are radix-sorted by one packed key (class, contig, end offset);
+//     each sorted query gets its upper bound (binary / Eytzinger / learned, si_ubound.cuh)
+//     through a block-cooperative search.  "class" puts queries longer than a threshold
+//     after the short ones.
+//  2. tiles: a CTA takes `tile_q` consecutive sorted short queries of one contig.  Their
+//     candidate set C = { k <= max ub : ends[k] >= min qs } holds every hit of every query of
+//     the tile; it is gathered into shared memory, in descending position order, by a
+//     block-wide top-down BFS over the max-of-32 pyramid of ends for the positions near the
+//     tile, and over the pyramid of the long-interval list (intervals at least 65536 long)
+//     for the positions further back.  C is split by interval length: near-start candidates
+//     are filtered per query, long ones are nearly all hits.  The count pass counts (one
+//     query per thread) and records the query's head-run length (the run of consecutive hits
+//     ending at ub); the emit pass writes the head run arithmetically (ascending for the
 //     C++ search_idxs order, hpp:892-895; descending for search_values / the C API) and then
-//     the remaining hits in descending order -- exactly the reference's output.
-//  3. long queries (and tiles whose C overflows shared memory) take the per-query walk: one
-//     warp per query walks the pyramid with the query's own threshold and counts / writes hits
-//     directly, 32 positions per step.
+//     the remaining hits in descending order (one query per warp, ballot compaction) --
+//     exactly the reference's output.
+//  3. long queries share the tile's long-interval candidates and scan their own window
+//     directly; tiles whose C overflows shared memory take the per-query walk over the
+//     pyramid (one warp per query, 32 positions per step).
 // Tiles and long queries are handed out by an atomic work counter (persistent CTAs), so uneven
 // per-query result counts do not leave SMs idle.
 #include <algorithm>

@@ -272,7 +272,7 @@ int build_impl(gSuperIntervals* si) {
         if (segv[g + 1] < segv[g]) return fail(SI_ERR_INVALID, "contig offsets decrease at %d", g);
     si->built = false;
     si->inverted = -1;
-    si->bws.long_ends = nullptr;  // set again once the long-interval pyramid exists
+    si->bws.long_ends = nullptr;  // set again once the long-interval list exists
     if (si->gexec) {              // a captured graph holds the old buffers
         cudaGraphExecDestroy(si->gexec);
         si->gexec = nullptr;
