@@ -164,6 +164,11 @@ def measured_peak():
 
 
 # ----------------------------------------------------------------------------- GPU arm
+def local_device() -> int:
+    """This rank's GPU (one process per GPU under torchrun)."""
+    return int(os.environ.get("LOCAL_RANK", "0"))
+
+
 def max_over_ranks(x: float, dist) -> float:
     """The slowest rank's time (the whole job ends when it does); x itself at N = 1."""
     if not dist:
@@ -180,7 +185,7 @@ def run_gpu(args, rank, world, dist):
     lib = _capi.load()
     wl = make_workload(args.config, args.scale, rank)
     s_bytes = wl.dtype.itemsize
-    idx = GpuIndex(64 if s_bytes == 8 else 32, 0)
+    idx = GpuIndex(64 if s_bytes == 8 else 32, local_device())
     idx.add_arrays(wl.starts, wl.ends, wl.data, seg=wl.seg if len(wl.seg) > 2 else None)
     t0 = time.perf_counter()
     idx.build()
@@ -353,7 +358,7 @@ def run_gpu_ub(args, rank, world, dist):
     lib = _capi.load()
     wl = make_workload(args.config, args.scale, rank)
     s_bytes = wl.dtype.itemsize
-    idx = GpuIndex(64 if s_bytes == 8 else 32, 0)
+    idx = GpuIndex(64 if s_bytes == 8 else 32, local_device())
     idx.add_arrays(wl.starts, wl.ends, wl.data, seg=wl.seg if len(wl.seg) > 2 else None)
     t0 = time.perf_counter()
     idx.build()
@@ -521,7 +526,7 @@ def run_gpu_rows(args, op, rank, world, dist):
     scale = args.scale if args.scale != 1.0 else ROW_DEFAULT_SCALE
     wl = make_workload(args.config, scale, rank)
     s_bytes = wl.dtype.itemsize
-    idx = GpuIndex(64 if s_bytes == 8 else 32, 0)
+    idx = GpuIndex(64 if s_bytes == 8 else 32, local_device())
     idx.add_arrays(wl.starts, wl.ends, wl.data, seg=wl.seg if len(wl.seg) > 2 else None)
     idx.build()
     idx.set_path(_capi.PATH_AUTO)
@@ -692,7 +697,7 @@ def run_bed(args, rank, world, dist):
     hp = C.c_void_p()
     _capi.check(lib.hostMallocPinnedGpu(C.byref(hp), len(text)))
     C.memmove(hp, text, len(text))
-    idx = GpuIndex(32, 0)
+    idx = GpuIndex(32, local_device())
     stats = _capi.cBedStats()
 
     def step():
@@ -760,7 +765,7 @@ def run_serving(args, rank, world, dist):
     from superintervals_gb300.interval_map import GpuIndex
     lib = _capi.load()
     wl, arrival, sizes, qc, qs, qe = serving_workload(args)
-    idx = GpuIndex(32, 0)
+    idx = GpuIndex(32, local_device())
     idx.add_arrays(wl.starts, wl.ends, wl.data, seg=wl.seg)
     t0 = time.perf_counter()
     idx.build()
