@@ -807,7 +807,7 @@ def run_serving(args, rank, world, dist):
                 continue
             # admission: arrived requests, at most max_batch queries, and no more than half of
             # the free device memory at the current hits-per-query estimate
-            _capi.check(lib.deviceMemInfoGpu(0, C.byref(free_b), C.byref(tot_b)))
+            _capi.check(lib.deviceMemInfoGpu(local_device(), C.byref(free_b), C.byref(tot_b)))
             per_q = 48 + 4 * hits_per_q
             room = min(max_batch, int(0.5 * free_b.value / per_q))
             r1 = r + 1
