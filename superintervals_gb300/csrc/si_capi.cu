@@ -1405,19 +1405,45 @@ int setop_device(gSuperIntervals* si, const sig::QueryBatch& q, int op, int orde
         SI_CK(cudaMemsetAsync(si->w_err.p, 0, sizeof(int), st));
     }
     bool sequential = false;
-    if (op == 1 && si->n > 0) {
-        if (si->inverted < 0) {
-            SI_TRY(si->so_flag.reserve(sizeof(int)));
-            SI_CK(sig::launch_any_inverted<S>(view<S>(si), si->so_flag.as<int>(), st));
-            int f = 0;
-            SI_CK(cudaMemcpyAsync(&f, si->so_flag.p, sizeof(int), cudaMemcpyDeviceToHost, st));
-            SI_CK(cudaStreamSynchronize(st));
-            si->inverted = f ? 1 : 0;
-        }
-        sequential = si->inverted == 1;
+    if (si->n > 0 && si->inverted < 0) {  // does some interval have start > end (once per build)
+        SI_TRY(si->so_flag.reserve(2 * sizeof(int)));
+        SI_CK(sig::launch_any_inverted<S>(view<S>(si), si->so_flag.as<int>(), st));
+        int f = 0;
+        SI_CK(cudaMemcpyAsync(&f, si->so_flag.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+        SI_CK(cudaStreamSynchronize(st));
+        si->inverted = f ? 1 : 0;
     }
+    if (op == 1) sequential = si->inverted == 1;
     const int64_t* hoff = si->so_hoff.as<int64_t>();
     const int32_t* hits = si->so_hits.as<int32_t>();
+    if (op == 0 && si->inverted == 0) {
+        // with start <= end for every interval and every query, each hit gives one piece:
+        // the pieces' offsets are the hits' offsets and no counting pass is needed
+        SI_TRY(si->so_flag.reserve(2 * sizeof(int)));
+        sig::MapView<S> qv = view<S>(si);
+        qv.starts = static_cast<const S*>(q.qs);
+        qv.ends = static_cast<const S*>(q.qe);
+        qv.n = q.nq;
+        SI_CK(sig::launch_any_inverted<S>(qv, si->so_flag.as<int>() + 1, st));
+        int qinv = 0;
+        int64_t P = 0;
+        SI_CK(cudaMemcpyAsync(&qinv, si->so_flag.as<int>() + 1, sizeof(int), cudaMemcpyDeviceToHost, st));
+        SI_CK(cudaMemcpyAsync(&P, hoff + q.nq, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+        SI_CK(cudaStreamSynchronize(st));
+        if (!qinv) {
+            SI_CK(cudaMemcpyAsync(d_off, hoff, sizeof(int64_t) * (q.nq + 1), cudaMemcpyDeviceToDevice, st));
+            if (total) *total = (size_t)P;
+            if ((size_t)P > cap) {
+                SI_CK(cudaStreamSynchronize(st));
+                return fail(SI_ERR_CAPACITY, "output needs %lld pieces, capacity %zu", (long long)P, cap);
+            }
+            if (P > 0 && (!d_os || !d_oe || !d_ob)) return fail(SI_ERR_INVALID, "null output buffer");
+            if (P > 0)
+                SI_CK(sig::launch_isect<S>(view<S>(si), q, hoff, hits, nullptr, d_off, d_os, d_oe, d_ob,
+                                           si->w_err.as<int>(), st));
+            return read_dev_err(si, st);
+        }
+    }
     SI_TRY(si->w_counts.reserve(sizeof(uint32_t) * q.nq));
     SI_TRY(si->w_tmp.reserve(sig::scan_temp_bytes(q.nq)));
     uint32_t* cnt = si->w_counts.as<uint32_t>();
