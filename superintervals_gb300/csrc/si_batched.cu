@@ -138,6 +138,7 @@ struct TileArgs {
     const int64_t* blk_cut;  // per tile of 256 queries: (p_cut, long-list end) or -1; null: none
     const int64_t* long_seg; // first list index of each contig
     int64_t long_split;
+    const S* end_sorted;     // each contig's ends ascending (no interval has start > end), or null
     const S* starts;
     int64_t split_len;
     const int32_t* data;
@@ -204,7 +205,19 @@ __device__ void walk_query(const TileArgs<S>& a, S qs, int64_t u, int64_t lo, in
         }
         return;
     }
-    const int64_t h = a.heads_in[id];
+    int64_t h = 0;
+    if (a.end_sorted) {
+        // short queries were counted from ranks, without their head run: find it here
+        for (int64_t top = u; top >= lo; top -= 32) {
+            const int64_t p = top - lane;
+            const unsigned m = __ballot_sync(kFull, p >= lo && a.P.ends[p] >= qs);
+            const int run = (m == kFull) ? 32 : __ffs(~m) - 1;
+            h += run;
+            if (run < 32) break;
+        }
+    } else {
+        h = a.heads_in[id];
+    }
     const int64_t base = a.offsets[id] - a.out_base;
     const int64_t capq = a.offsets[id + 1] - a.offsets[id];
     if (h > capq) {
@@ -394,14 +407,15 @@ __device__ __forceinline__ int64_t warp_first_near(const S* __restrict__ starts,
     return m ? a + __ffs(m) - 1 : b;
 }
 
-// First index in [a, b) of an ascending position list whose position is >= key (b when none).
+// First index in [a, b) of an ascending array whose element is >= key (b when none).
 // Warp-cooperative 32-ary search over global memory.  Warp-uniform.
-__device__ __forceinline__ int64_t warp_first_pos_geq(const int32_t* __restrict__ pos, int64_t a, int64_t b,
-                                                      int64_t key, int lane) {
+template <typename T, typename K>
+__device__ __forceinline__ int64_t warp_first_geq(const T* __restrict__ arr, int64_t a, int64_t b, K key,
+                                                  int lane) {
     while (b - a > 32) {
         const int64_t step = (b - a + 31) >> 5;
         const int64_t idx = a + lane * step;
-        const unsigned m = __ballot_sync(kFull, idx < b && (int64_t)pos[idx] >= key);
+        const unsigned m = __ballot_sync(kFull, idx < b && (K)arr[idx] >= key);
         if (!m) {
             const int64_t last = min((int64_t)31, (b - 1 - a) / step);
             a = a + last * step + 1;
@@ -414,8 +428,14 @@ __device__ __forceinline__ int64_t warp_first_pos_geq(const int32_t* __restrict_
         }
     }
     const int64_t idx = a + lane;
-    const unsigned m = __ballot_sync(kFull, idx < b && (int64_t)pos[idx] >= key);
+    const unsigned m = __ballot_sync(kFull, idx < b && (K)arr[idx] >= key);
     return m ? a + __ffs(m) - 1 : b;
+}
+
+// First index in [a, b) of an ascending position list whose position is >= key (b when none).
+__device__ __forceinline__ int64_t warp_first_pos_geq(const int32_t* __restrict__ pos, int64_t a, int64_t b,
+                                                      int64_t key, int lane) {
+    return warp_first_geq<int32_t, int64_t>(pos, a, b, key, lane);
 }
 
 // First index of a DESCENDING position list whose position is < key (n when none).
@@ -520,6 +540,70 @@ __device__ void long_query(const TileArgs<S>& a, S qs, int64_t u, int64_t lo, in
     }
 }
 
+// Count of every query of a run of short queries of one contig [lo, hi), from two ranks.
+// With start <= end for every interval and qs <= qe, an interval that ends before qs also
+// starts at or before qe, so
+//   count = #(start <= qe) - #(end < qs) = (u - lo + 1) - (rank of qs among the contig's ends).
+// The run's ranks lie between those of its smallest and largest qs: the block finds the two
+// with one warp each, stages the ends between them in shared memory (win, cap slots) when
+// they fit, and resolves each query there.  Block-wide; heads are left to the emit pass.
+template <typename S>
+__device__ void rank_count_run(const TileArgs<S>& a, int r0, int r1, int64_t lo, int64_t hi, const S* q_s,
+                               const int32_t* q_u, const int32_t* q_id, S* win, S* s_red, S* s_red2,
+                               int64_t* s_cut, int tid, int lane, int warp) {
+    S mn = Lim<S>::hi, mx = Lim<S>::lo;
+    for (int i = r0 + tid; i < r1; i += kThreads) {
+        mn = q_s[i] < mn ? q_s[i] : mn;
+        mx = q_s[i] > mx ? q_s[i] : mx;
+    }
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) {
+        const S o = __shfl_xor_sync(kFull, mn, d);
+        mn = o < mn ? o : mn;
+        const S p = __shfl_xor_sync(kFull, mx, d);
+        mx = p > mx ? p : mx;
+    }
+    if (lane == 0) {
+        s_red[warp] = mn;
+        s_red2[warp] = mx;
+    }
+    __syncthreads();
+    if (warp < 2) {  // warp 0: rank of the smallest qs, warp 1: of the largest
+        S key = warp == 0 ? s_red[0] : s_red2[0];
+#pragma unroll
+        for (int w = 1; w < kWarpsPerCta; ++w)
+            key = warp == 0 ? (s_red[w] < key ? s_red[w] : key) : (s_red2[w] > key ? s_red2[w] : key);
+        const int64_t r = warp_first_geq<S, S>(a.end_sorted, lo, hi, key, lane);
+        if (lane == 0) s_cut[warp] = r;
+    }
+    __syncthreads();
+    const int64_t A = s_cut[0], B = s_cut[1];
+    const bool staged = B - A <= (int64_t)a.cap;
+    if (staged)
+        for (int64_t k = tid; k < B - A; k += kThreads) win[k] = a.end_sorted[A + k];
+    __syncthreads();
+    for (int i = r0 + tid; i < r1; i += kThreads) {
+        const S qs = q_s[i];
+        int64_t b0 = 0, b1 = B - A;  // first index of the window whose end is >= qs
+        if (staged) {
+            while (b0 < b1) {
+                const int64_t mid = (b0 + b1) >> 1;
+                if (win[mid] < qs) b0 = mid + 1;
+                else b1 = mid;
+            }
+        } else {
+            while (b0 < b1) {
+                const int64_t mid = (b0 + b1) >> 1;
+                if (a.end_sorted[A + mid] < qs) b0 = mid + 1;
+                else b1 = mid;
+            }
+        }
+        const int64_t below = A + b0;  // lo + #(end < qs)
+        const int64_t u = q_u[i];
+        a.counts[q_id[i]] = u + 1 > below ? (uint32_t)(u + 1 - below) : 0u;
+    }
+}
+
 template <typename S, bool EMIT>
 __global__ void __launch_bounds__(kThreads, 4) k_tiles(TileArgs<S> a) {
     extern __shared__ __align__(16) unsigned char smem[];
@@ -598,7 +682,12 @@ __global__ void __launch_bounds__(kThreads, 4) k_tiles(TileArgs<S> a) {
             bool per_query = is_long && a.PL.ends == nullptr;
             const bool long_run = is_long && !per_query;
             int nc = 0, nl = 0, nlnu = 0;
-            if (!is_long) {
+            // count pass over an index without inverted intervals: short queries from ranks
+            const bool rank_run = !EMIT && !is_long && a.end_sorted != nullptr;
+            if (rank_run)
+                rank_count_run<S>(a, r0, r1, lo, a.seg[g + 1], q_s, q_u, q_id, cend, s_red, s_red2, s_cut, tid,
+                                  lane, warp);
+            if (!is_long && !rank_run) {
                 // a tile that is one run can reuse the candidate lists the count pass stored
                 const bool whole = (r0 == 0 && r1 == nt);
                 unsigned char* rec = (whole && a.cache) ? a.cache + (size_t)t * a.cache_stride : nullptr;
@@ -831,7 +920,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_tiles(TileArgs<S> a) {
                                             EMIT ? (int64_t)q_cap[i] : 0, lane);
                 }
             }
-            if (!EMIT && !per_query && !long_run) {
+            if (!EMIT && !per_query && !long_run && !rank_run) {
                 // count pass: one query per THREAD over the shared-memory lists
                 for (int i = r0 + tid; i < r1; i += kThreads) {
                     const S qs = q_s[i];
@@ -890,6 +979,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_tiles(TileArgs<S> a) {
                     const S qs = q_s[i];
                     const int32_t u = q_u[i];
                     int ta = nc, tsplit = nc, lb = nl, flags = 0;
+                    if (a.end_sorted) q_h[i] = 0;  // no candidate: no head (set below otherwise)
                     if (u >= lo && nc > 0) {
                         int b0 = 0, b1 = nc;  // first candidate at or below u
                         while (b0 < b1) {
@@ -898,12 +988,32 @@ __global__ void __launch_bounds__(kThreads, 4) k_tiles(TileArgs<S> a) {
                             else b1 = mid;
                         }
                         const int t0 = b0;
-                        const int h = q_h[i];
-                        ta = t0 + (h < nc - t0 ? h : nc - t0);
-                        int t = ta;
                         const S thr = near_threshold<S>(qs, X);
-                        while (t < nc && cstart[t] >= thr) ++t;
-                        tsplit = t;
+                        // starts do not increase along the list: first t in [from, nc) whose start
+                        // is below key
+                        auto first_start_below = [&](int from, S key) {
+                            int l0 = from, l1 = nc;
+                            while (l0 < l1) {
+                                const int mid = (l0 + l1) >> 1;
+                                if (cstart[mid] >= key) l0 = mid + 1;
+                                else l1 = mid;
+                            }
+                            return l0;
+                        };
+                        int h = q_h[i];
+                        if (a.end_sorted) {
+                            // counted from ranks: the head run (consecutive positions u, u - 1, ...
+                            // that are hits) is found here.  Positions from u down to the last start
+                            // >= qs end at or after qs (no interval has start > end), so they are all
+                            // in the list and all hits; the run then goes on while positions stay
+                            // consecutive and hit.
+                            int t = first_start_below(t0, qs);
+                            while (t < nc && cpos[t] == u - (t - t0) && cend[t] >= qs) ++t;
+                            h = t - t0;
+                            q_h[i] = h;
+                        }
+                        ta = t0 + (h < nc - t0 ? h : nc - t0);
+                        tsplit = first_start_below(ta, thr);
                         const int tb = max(tsplit, ta);
                         if (tb < nc && nl > 0) {
                             const int32_t pb = cpos[tb];
@@ -1080,7 +1190,8 @@ __global__ void k_qkeys_packed(const S* __restrict__ qs, const S* __restrict__ q
     if (q >= nq) return;
     const int32_t g = qc ? qc[q] : 0;
     const S s = qs[q], e = qe[q];
-    const bool is_long = ((double)e - (double)s + 1.0) > (double)long_len;
+    // a query with start > end takes the long-query path, which does not need start <= end
+    const bool is_long = s > e || ((double)e - (double)s + 1.0) > (double)long_len;
     const uint32_t code = (g < 0 || g >= G) ? 2u * (uint32_t)G : (uint32_t)g + (is_long ? (uint32_t)G : 0u);
     const unsigned long long rel = ((unsigned long long)(int64_t)e ^ 0x8000000000000000ull) - mm[0];
     key[q] = (code << ebits) | (uint32_t)(rel >> shift);
@@ -1096,7 +1207,7 @@ __global__ void k_qkeys(const S* __restrict__ qs, const S* __restrict__ qe, cons
     const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= nq) return;
     const int32_t g = qc ? qc[q] : 0;
-    const bool is_long = ((double)qe[q] - (double)qs[q] + 1.0) > (double)long_len;
+    const bool is_long = qs[q] > qe[q] || ((double)qe[q] - (double)qs[q] + 1.0) > (double)long_len;
     // The end key drops its lowest byte: tiles need queries grouped by class and contig and
     // close in position, not exactly ordered, and a constant digit costs no sort pass.
     if constexpr (sizeof(S) == 4) {
@@ -1649,6 +1760,7 @@ static int run_tiles(BatchedWorkspace& ws, MapView<S> m, Levels<S> L, int H, int
     a.long_seg = ws.long_seg;
     a.blk_cut = (ws.prm.tile_q == kThreads && ws.blk_cut.p) ? ws.blk_cut.as<int64_t>() : nullptr;
     a.long_split = ws.long_split;
+    a.end_sorted = static_cast<const S*>(ws.end_sorted);
     a.starts = m.starts;
     a.split_len = ws.prm.split_len;
     a.data = m.data;
@@ -1702,14 +1814,19 @@ int batched_count(BatchedWorkspace& ws, MapView<S> m, Levels<S> L, int H, const 
     if (ws.prepared_nq != nq || ws.prepared_qs != q.qs) return SI_ERR_INVALID;
     SI_OKR(ws.heads.reserve(sizeof(int32_t) * nq));
     ws.n_heads = nq;
+    ws.cache_prm_tile = ws.prm.tile_q;
+    ws.cache_prm_cap = ws.prm.cap;
+    if (ws.end_sorted) {  // short queries are counted from ranks: no tile lists to keep
+        ws.cache_ok = false;
+        return run_tiles<S>(ws, m, L, H, nq, false, counts, ws.heads.as<int32_t>(), nullptr, nullptr, 0, 0, false,
+                            nullptr, d_err, false, st);
+    }
     // room for every tile's candidate lists, so that the emit pass need not gather again;
     // without room (device budget) the emit pass simply gathers again
     ws.cache_stride = (int64_t)round_up(16 + (int64_t)ws.prm.cap * (8 + 3 * (int64_t)sizeof(S)) +
                                             (int64_t)kLnu * (4 + (int64_t)sizeof(S)), 256);
     const int64_t n_tiles = ceil_div(nq, ws.prm.tile_q);
     ws.cache_ok = ws.tile_cache.reserve((size_t)(n_tiles * ws.cache_stride)) == SI_OK;
-    ws.cache_prm_tile = ws.prm.tile_q;
-    ws.cache_prm_cap = ws.prm.cap;
     return run_tiles<S>(ws, m, L, H, nq, false, counts, ws.heads.as<int32_t>(), nullptr, nullptr, 0, 0, false,
                         nullptr, d_err, true, st);
 }

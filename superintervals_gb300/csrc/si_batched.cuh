@@ -81,6 +81,9 @@ struct BatchedWorkspace {
     const void* long_lvl[kMaxLevels] = {nullptr};
     int long_H = 0;
     int64_t long_split = 0;
+    // each contig's ends in ascending order (positions as the index), when no interval has
+    // start > end: short queries are then counted from two ranks instead of the tile lists
+    const void* end_sorted = nullptr;
 };
 
 // Interval length from which an interval enters the long-interval list.

@@ -357,6 +357,63 @@ cudaError_t launch_differs_i32(const int32_t* a, const int32_t* b, int64_t n, in
     return cudaGetLastError();
 }
 
+// Sort keys of the ends inside each contig: offset-binary end (word 0 low), contig above.
+template <typename S>
+__global__ void k_end_keys(const S* __restrict__ e, int64_t n, const int64_t* __restrict__ seg, int G,
+                           uint32_t* __restrict__ w0, uint32_t* __restrict__ w1, uint32_t* __restrict__ w2) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    if constexpr (sizeof(S) == 4) {
+        w0[i] = (uint32_t)e[i] ^ 0x80000000u;
+        if (G > 1) w1[i] = (uint32_t)seg_of(seg, G, i);
+    } else {
+        const uint64_t b = (uint64_t)e[i] ^ 0x8000000000000000ull;
+        w0[i] = (uint32_t)b;
+        w1[i] = (uint32_t)(b >> 32);
+        if (G > 1) w2[i] = (uint32_t)seg_of(seg, G, i);
+    }
+}
+
+template <typename S>
+__global__ void k_end_decode(const uint32_t* __restrict__ w0, const uint32_t* __restrict__ w1, int64_t n,
+                             int64_t n_pad, S* __restrict__ out) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_pad) return;
+    if (i >= n) {
+        out[i] = Lim<S>::hi;
+    } else if constexpr (sizeof(S) == 4) {
+        out[i] = (S)(w0[i] ^ 0x80000000u);
+    } else {
+        out[i] = (S)((((uint64_t)w1[i] << 32) | w0[i]) ^ 0x8000000000000000ull);
+    }
+}
+
+template <typename S>
+int end_key_words(int G) {
+    return (sizeof(S) == 4 ? 1 : 2) + (G > 1 ? 1 : 0);
+}
+
+template <typename S>
+cudaError_t launch_end_keys(const S* ends, int64_t n, const int64_t* seg, int G, uint32_t* const* kw,
+                            cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    const int K = end_key_words<S>(G);
+    uint32_t* w[3] = {nullptr, nullptr, nullptr};
+    for (int k = 0; k < K; ++k) w[k] = kw[k];
+    k_end_keys<S><<<blocks_for(n), kThreads, 0, st>>>(ends, n, seg, G, w[0], w[1], w[2]);
+    note_launch();
+    return cudaGetLastError();
+}
+
+template <typename S>
+cudaError_t launch_end_decode(const uint32_t* const* kw, int64_t n, int64_t n_pad, S* out, cudaStream_t st) {
+    if (n_pad <= 0) return cudaSuccess;
+    k_end_decode<S><<<blocks_for(n_pad), kThreads, 0, st>>>(kw[0], sizeof(S) == 8 ? kw[1] : nullptr, n, n_pad,
+                                                           out);
+    note_launch();
+    return cudaGetLastError();
+}
+
 template <typename S>
 cudaError_t launch_branch(const S* ends, int64_t n, int64_t n_pad, Levels<S> L, int H,
                           const int64_t* seg, int G, int32_t* branch, cudaStream_t st) {
@@ -382,7 +439,11 @@ cudaError_t launch_branch(const S* ends, int64_t n, int64_t n_pad, Levels<S> L, 
                                                 int64_t, const int64_t*, int, int32_t*, S*, int64_t*,        \
                                                 cudaStream_t);                                               \
     template cudaError_t launch_branch<S>(const S*, int64_t, int64_t, Levels<S>, int,           \
-                                          const int64_t*, int, int32_t*, cudaStream_t);
+                                          const int64_t*, int, int32_t*, cudaStream_t);        \
+    template int end_key_words<S>(int);                                                          \
+    template cudaError_t launch_end_keys<S>(const S*, int64_t, const int64_t*, int, uint32_t* const*, \
+                                            cudaStream_t);                                       \
+    template cudaError_t launch_end_decode<S>(const uint32_t* const*, int64_t, int64_t, S*, cudaStream_t);
 SIG_INST(int32_t)
 SIG_INST(int64_t)
 

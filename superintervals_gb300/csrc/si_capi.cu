@@ -137,6 +137,7 @@ struct gSuperIntervals {
     DevBuf lvl[sig::kMaxLevels];
     // long-interval list: intervals >= kLongIntervalSplit long, position order, own pyramid
     DevBuf long_pos, long_end, long_seg;
+    DevBuf end_sorted;  // each contig's ends ascending (built when no interval has start > end)
     DevBuf long_lvl[sig::kMaxLevels];
     int64_t long_sizes[sig::kMaxLevels + 1] = {0};
     int long_H = 0;
@@ -273,6 +274,7 @@ int build_impl(gSuperIntervals* si) {
     si->built = false;
     si->inverted = -1;
     si->bws.long_ends = nullptr;  // set again once the long-interval list exists
+    si->bws.end_sorted = nullptr;
     if (si->gexec) {              // a captured graph holds the old buffers
         cudaGraphExecDestroy(si->gexec);
         si->gexec = nullptr;
@@ -381,6 +383,42 @@ int build_impl(gSuperIntervals* si) {
     for (int h = 0; h < sig::kMaxLevels; ++h) si->bws.long_lvl[h] = si->long_lvl[h].p;
     si->bws.long_H = si->long_H;
     si->bws.long_split = sig::kLongIntervalSplit;
+    // intervals with start > end; when there are none, each contig's ends in ascending order,
+    // from which the batched path counts short queries (two ranks per query)
+    {
+        DevBuf flag2;
+        SI_TRY(flag2.reserve(sizeof(int)));
+        SI_CK(sig::launch_any_inverted<S>(view<S>(si), flag2.as<int>(), st));
+        int f = 0;
+        SI_CK(cudaMemcpyAsync(&f, flag2.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+        SI_CK(cudaStreamSynchronize(st));
+        si->inverted = f ? 1 : 0;
+    }
+    if (si->inverted == 0) {
+        const int K = sig::end_key_words<S>(G);
+        DevBuf kw[3], kalt[3], pay, palt, tmp;
+        uint32_t* kp[3];
+        uint32_t* ka[3];
+        for (int k = 0; k < K; ++k) {
+            SI_TRY(kw[k].reserve(sizeof(uint32_t) * n));
+            SI_TRY(kalt[k].reserve(sizeof(uint32_t) * n));
+            kp[k] = kw[k].as<uint32_t>();
+            ka[k] = kalt[k].as<uint32_t>();
+        }
+        SI_TRY(pay.reserve(sizeof(uint32_t) * n));
+        SI_TRY(palt.reserve(sizeof(uint32_t) * n));
+        const size_t tb = sig::radix_temp_bytes(n, K);
+        SI_TRY(tmp.reserve(tb));
+        SI_CK(sig::launch_end_keys<S>(ends, n, si->seg.as<int64_t>(), G, kp, st));
+        bool in_alt = false;
+        int passes = 0;
+        SI_CK(sig::radix_sort(kp, ka, pay.as<uint32_t>(), palt.as<uint32_t>(), K, n, tmp.p, tb, &in_alt, &passes,
+                              st));
+        SI_TRY(si->end_sorted.reserve(sizeof(S) * n_pad));
+        SI_CK(sig::launch_end_decode<S>(in_alt ? ka : kp, n, n_pad, si->end_sorted.as<S>(), st));
+        SI_CK(cudaStreamSynchronize(st));  // the temporaries are released on scope exit
+        si->bws.end_sorted = si->end_sorted.p;
+    }
     SI_TRY(sig::batched_prepare<S>(si->bws, view<S>(si), levels<S>(si), si->H, si->lvl_sizes,
                                    si->ub_mode, st));
     SI_CK(cudaStreamSynchronize(st));

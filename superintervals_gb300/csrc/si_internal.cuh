@@ -161,8 +161,6 @@ int pyramid_levels(int64_t n_pad, int64_t* sizes);
 template <typename S>
 cudaError_t launch_pyramid(const S* ends, const int64_t* sizes, int H, S* const* lvl,
                            cudaStream_t st);
-// ends of intervals at least X long (end - start >= X), S_MIN for the others: the base of
-// the long-interval pyramid used by the batched path's long-query tiles.
 // long-interval list (end - start >= X) in position order: flags per interval; then, with
 // offs = exclusive scan of the flags (n + 1 entries), the positions and ends of the n_long
 // long intervals padded to n_long_pad, and each contig's first list index (G + 1 entries)
@@ -178,6 +176,15 @@ cudaError_t launch_differs_i32(const int32_t* a, const int32_t* b, int64_t n, in
 template <typename S>
 cudaError_t launch_branch(const S* ends, int64_t n, int64_t n_pad, Levels<S> L, int H,
                           const int64_t* seg, int G, int32_t* branch, cudaStream_t st);
+// each contig's ends in ascending order: sort keys (end_key_words<S>(G) words, for
+// radix_sort), then the sorted keys decoded into out[0, n_pad) (padding: the largest value)
+template <typename S>
+int end_key_words(int G);
+template <typename S>
+cudaError_t launch_end_keys(const S* ends, int64_t n, const int64_t* seg, int G, uint32_t* const* kw,
+                            cudaStream_t st);
+template <typename S>
+cudaError_t launch_end_decode(const uint32_t* const* kw, int64_t n, int64_t n_pad, S* out, cudaStream_t st);
 
 // ---------------------------------------------------------------- query launchers (si_query.cu)
 struct QueryBatch {
