@@ -44,7 +44,7 @@ METRIC_UB = "upper-bound queries/s on 1 GB300: learned two-stage index vs binary
 PEAK_FALLBACK_GBS = 6800.0
 # DRAM bytes (read + write) of one emit launch, from one ncu capture (dram__bytes_read.sum +
 # dram__bytes_write.sum) of exactly this workload: (config, scale, path) -> bytes per launch
-EMIT_TRAFFIC = {("config3", 1.0, "batched"): 124.15e9}
+EMIT_TRAFFIC = {("config3", 1.0, "batched"): 121.45e9}
 
 
 def parse():
@@ -58,6 +58,9 @@ def parse():
     ap.add_argument("--requests", type=int, default=600, help="config5: requests in the stream")
     ap.add_argument("--rate", type=float, default=200.0, help="config5: offered requests/s (Poisson)")
     ap.add_argument("--scale", type=float, default=1.0, help="shrink N and Q (tests only)")
+    ap.add_argument("--contigs", default=None,
+                    help="config3: only these contigs (comma-separated names), at the full "
+                         "configuration's density (small profiling cases with the same hits per query)")
     ap.add_argument("--path", default="batched", choices=["batched", "plain", "auto"])
     ap.add_argument("--ub", default="learned", choices=["learned", "eytzinger", "binary"])
     ap.add_argument("--op", default=None, choices=["search_idxs", "upper_bound"] + ROW_OPS,
@@ -75,13 +78,23 @@ def parse():
 
 
 # ----------------------------------------------------------------------------- workload
-def make_workload(cfg, scale, rank):
+def make_workload(cfg, scale, rank, contigs=None):
     from superintervals_gb300 import workloads as W
     sizes = {"config1": (100_000, 100_000), "config2": (10_000_000, 10_000_000),
              "config3": (50_000_000, 50_000_000), "config4": (100_000_000, 100_000_000)}
     n, nq = sizes[cfg]
-    n, nq = max(1000, int(n * scale)), max(1000, int(nq * scale))
-    wl = getattr(W, cfg)(n=n, nq=nq)
+    if cfg == "config3" and contigs:
+        # a subset of the contigs with its share of the intervals and queries
+        names = set(contigs.split(","))
+        sub = [c for c in W.HUMAN_CONTIGS if c[0] in names]
+        if len(sub) != len(names):
+            raise SystemExit(f"unknown contig in --contigs {contigs}")
+        share = sum(c[1] for c in sub) / sum(c[1] for c in W.HUMAN_CONTIGS)
+        n, nq = max(1000, int(n * scale * share)), max(1000, int(nq * scale * share))
+        wl = W.config3(n=n, nq=nq, contigs=sub)
+    else:
+        n, nq = max(1000, int(n * scale)), max(1000, int(nq * scale))
+        wl = getattr(W, cfg)(n=n, nq=nq)
     if rank:
         # weak scaling: every rank gets its own query batch of the same size
         rng = np.random.Generator(np.random.PCG64(1000 + rank))
@@ -183,7 +196,7 @@ def run_gpu(args, rank, world, dist):
     from superintervals_gb300 import _capi
     from superintervals_gb300.interval_map import GpuIndex
     lib = _capi.load()
-    wl = make_workload(args.config, args.scale, rank)
+    wl = make_workload(args.config, args.scale, rank, args.contigs)
     s_bytes = wl.dtype.itemsize
     idx = GpuIndex(64 if s_bytes == 8 else 32, local_device())
     idx.add_arrays(wl.starts, wl.ends, wl.data, seg=wl.seg if len(wl.seg) > 2 else None)
@@ -356,7 +369,7 @@ def run_gpu_ub(args, rank, world, dist):
     from superintervals_gb300 import _capi
     from superintervals_gb300.interval_map import GpuIndex
     lib = _capi.load()
-    wl = make_workload(args.config, args.scale, rank)
+    wl = make_workload(args.config, args.scale, rank, args.contigs)
     s_bytes = wl.dtype.itemsize
     idx = GpuIndex(64 if s_bytes == 8 else 32, local_device())
     idx.add_arrays(wl.starts, wl.ends, wl.data, seg=wl.seg if len(wl.seg) > 2 else None)
@@ -1097,7 +1110,7 @@ def main():
     emit_ms = ph[2] if ph[2] > 0 else ms
     algo = nq * (2 * s + 8) + P * (s + 4)
     achieved = algo / (emit_ms / 1000.0) / 1e9
-    traffic = EMIT_TRAFFIC.get((cfg, args.scale, args.path))
+    traffic = None if args.contigs else EMIT_TRAFFIC.get((cfg, args.scale, args.path))
     line["roofline"] = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                         "frac": achieved / peak, "traffic": traffic, "kernel": "emit",
                         "traffic_frac": (traffic / (emit_ms / 1000.0) / 1e9 / peak) if traffic else None,

@@ -659,7 +659,10 @@ __global__ void __launch_bounds__(kThreads, 4) k_tiles(TileArgs<S> a) {
                 const int64_t o = a.offsets[id];
                 q_off[i] = o - a.out_base;
                 q_cap[i] = (int32_t)(a.offsets[id + 1] - o);
-                q_h[i] = a.heads_in[id];
+                // head runs of short queries counted from ranks are found by step 1 below
+                const uint32_t cw = q_c[i];
+                const bool counted_by_rank = a.end_sorted && !(cw >= (uint32_t)a.G && cw < 2u * (uint32_t)a.G);
+                q_h[i] = counted_by_rank ? 0 : a.heads_in[id];
             }
         }
         __syncthreads();
