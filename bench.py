@@ -44,7 +44,7 @@ METRIC_UB = "upper-bound queries/s on 1 GB300: learned two-stage index vs binary
 PEAK_FALLBACK_GBS = 6800.0
 # DRAM bytes (read + write) of one emit launch, from one ncu capture (dram__bytes_read.sum +
 # dram__bytes_write.sum) of exactly this workload: (config, scale, path) -> bytes per launch
-EMIT_TRAFFIC = {("config3", 1.0, "batched"): 121.45e9}
+EMIT_TRAFFIC = {("config3", 1.0, "batched"): 115.25e9}
 
 
 def parse():

@@ -125,6 +125,20 @@ __device__ __forceinline__ void scan_desc(const Pyr<S>& P, int64_t lo, int64_t u
     }
 }
 
+// Query class codes (the sort key's top bits): g for a short query of contig g, G + g for a
+// long one, 2G + g for one with start > end (long-query path, counted by the count pass),
+// 3G for a contig id outside [0, G).
+__device__ __forceinline__ bool code_is_long(uint32_t c, int G) {
+    return c >= (uint32_t)G && c < 3u * (uint32_t)G;
+}
+__device__ __forceinline__ bool code_is_inverted(uint32_t c, int G) {
+    return c >= 2u * (uint32_t)G && c < 3u * (uint32_t)G;
+}
+__device__ __forceinline__ int code_contig(uint32_t c, int G) {
+    const uint32_t u = (uint32_t)G;
+    return (int)(c < u ? c : c < 2u * u ? c - u : c < 3u * u ? c - 2u * u : 0u);
+}
+
 __device__ __forceinline__ unsigned above_mask(int lane) {
     // bits strictly above `lane`
     return lane == 31 ? 0u : ~((2u << lane) - 1u);
@@ -498,7 +512,18 @@ __device__ void long_query(const TileArgs<S>& a, S qs, int64_t u, int64_t lo, in
         }
         return;
     }
-    const int64_t h = h_in;
+    int64_t h = h_in;
+    if (h < 0) {
+        // counted from ranks, without its head run: find it here (positions u, u - 1, ... hit)
+        h = 0;
+        for (int64_t top = u; top >= lo; top -= 32) {
+            const int64_t p = top - lane;
+            const unsigned m = __ballot_sync(kFull, p >= lo && ends[p] >= qs);
+            const int run = (m == kFull) ? 32 : __ffs(~m) - 1;
+            h += run;
+            if (run < 32) break;
+        }
+    }
     if (h > capq) {
         if (lane == 0) atomicCAS(a.d_err, kDevOk, kDevOverflow);
         return;
@@ -537,70 +562,6 @@ __device__ void long_query(const TileArgs<S>& a, S qs, int64_t u, int64_t lo, in
             dst[w + __popc(m & lt)] = a.values ? a.data[pos] : pos - (int32_t)lo;
         }
         w += k;
-    }
-}
-
-// Count of every query of a run of short queries of one contig [lo, hi), from two ranks.
-// With start <= end for every interval and qs <= qe, an interval that ends before qs also
-// starts at or before qe, so
-//   count = #(start <= qe) - #(end < qs) = (u - lo + 1) - (rank of qs among the contig's ends).
-// The run's ranks lie between those of its smallest and largest qs: the block finds the two
-// with one warp each, stages the ends between them in shared memory (win, cap slots) when
-// they fit, and resolves each query there.  Block-wide; heads are left to the emit pass.
-template <typename S>
-__device__ void rank_count_run(const TileArgs<S>& a, int r0, int r1, int64_t lo, int64_t hi, const S* q_s,
-                               const int32_t* q_u, const int32_t* q_id, S* win, S* s_red, S* s_red2,
-                               int64_t* s_cut, int tid, int lane, int warp) {
-    S mn = Lim<S>::hi, mx = Lim<S>::lo;
-    for (int i = r0 + tid; i < r1; i += kThreads) {
-        mn = q_s[i] < mn ? q_s[i] : mn;
-        mx = q_s[i] > mx ? q_s[i] : mx;
-    }
-#pragma unroll
-    for (int d = 16; d > 0; d >>= 1) {
-        const S o = __shfl_xor_sync(kFull, mn, d);
-        mn = o < mn ? o : mn;
-        const S p = __shfl_xor_sync(kFull, mx, d);
-        mx = p > mx ? p : mx;
-    }
-    if (lane == 0) {
-        s_red[warp] = mn;
-        s_red2[warp] = mx;
-    }
-    __syncthreads();
-    if (warp < 2) {  // warp 0: rank of the smallest qs, warp 1: of the largest
-        S key = warp == 0 ? s_red[0] : s_red2[0];
-#pragma unroll
-        for (int w = 1; w < kWarpsPerCta; ++w)
-            key = warp == 0 ? (s_red[w] < key ? s_red[w] : key) : (s_red2[w] > key ? s_red2[w] : key);
-        const int64_t r = warp_first_geq<S, S>(a.end_sorted, lo, hi, key, lane);
-        if (lane == 0) s_cut[warp] = r;
-    }
-    __syncthreads();
-    const int64_t A = s_cut[0], B = s_cut[1];
-    const bool staged = B - A <= (int64_t)a.cap;
-    if (staged)
-        for (int64_t k = tid; k < B - A; k += kThreads) win[k] = a.end_sorted[A + k];
-    __syncthreads();
-    for (int i = r0 + tid; i < r1; i += kThreads) {
-        const S qs = q_s[i];
-        int64_t b0 = 0, b1 = B - A;  // first index of the window whose end is >= qs
-        if (staged) {
-            while (b0 < b1) {
-                const int64_t mid = (b0 + b1) >> 1;
-                if (win[mid] < qs) b0 = mid + 1;
-                else b1 = mid;
-            }
-        } else {
-            while (b0 < b1) {
-                const int64_t mid = (b0 + b1) >> 1;
-                if (a.end_sorted[A + mid] < qs) b0 = mid + 1;
-                else b1 = mid;
-            }
-        }
-        const int64_t below = A + b0;  // lo + #(end < qs)
-        const int64_t u = q_u[i];
-        a.counts[q_id[i]] = u + 1 > below ? (uint32_t)(u + 1 - below) : 0u;
     }
 }
 
@@ -648,6 +609,11 @@ __global__ void __launch_bounds__(kThreads, 4) k_tiles(TileArgs<S> a) {
         const int t = a.n_tiles - 1 - tc;
         const int64_t j0 = (int64_t)t * T;
         const int nt = (int)((a.nq - j0) < (int64_t)T ? (a.nq - j0) : (int64_t)T);
+        if (!EMIT && a.end_sorted && a.sq_c[j0 + nt - 1] < 2u * (uint32_t)a.G) {
+            // classes are sorted and tiles are handed out from the end: this tile and every
+            // later one hold short and long queries only, counted by the prepare pass
+            return;
+        }
         for (int i = tid; i < nt; i += kThreads) {
             q_s[i] = a.sq_s[j0 + i];
             q_u[i] = a.sq_u[j0 + i];
@@ -659,10 +625,10 @@ __global__ void __launch_bounds__(kThreads, 4) k_tiles(TileArgs<S> a) {
                 const int64_t o = a.offsets[id];
                 q_off[i] = o - a.out_base;
                 q_cap[i] = (int32_t)(a.offsets[id + 1] - o);
-                // head runs of short queries counted from ranks are found by step 1 below
-                const uint32_t cw = q_c[i];
-                const bool counted_by_rank = a.end_sorted && !(cw >= (uint32_t)a.G && cw < 2u * (uint32_t)a.G);
-                q_h[i] = counted_by_rank ? 0 : a.heads_in[id];
+                // queries counted from ranks have no head run from the count pass: the emit
+                // finds it (-1)
+                const bool counted_by_rank = a.end_sorted && !code_is_inverted(q_c[i], a.G);
+                q_h[i] = counted_by_rank ? -1 : a.heads_in[id];
             }
         }
         __syncthreads();
@@ -677,19 +643,15 @@ __global__ void __launch_bounds__(kThreads, 4) k_tiles(TileArgs<S> a) {
                 else hi_i = mid;
             }
             const int r1 = lo_i;
-            // class code: g for short queries of contig g, G + g for long ones (query_code)
-            const bool is_long = cw >= (uint32_t)a.G && cw < 2u * (uint32_t)a.G;
-            int g = (int)(is_long ? cw - (uint32_t)a.G : cw);
-            if (g >= a.G) g = 0;  // invalid contigs are reported by the prepare kernel
+            const bool is_long = code_is_long(cw, a.G);
+            const int g = code_contig(cw, a.G);  // invalid contigs are reported by the prepare kernel
             const int64_t lo = a.seg[g];
             bool per_query = is_long && a.PL.ends == nullptr;
             const bool long_run = is_long && !per_query;
             int nc = 0, nl = 0, nlnu = 0;
-            // count pass over an index without inverted intervals: short queries from ranks
-            const bool rank_run = !EMIT && !is_long && a.end_sorted != nullptr;
-            if (rank_run)
-                rank_count_run<S>(a, r0, r1, lo, a.seg[g + 1], q_s, q_u, q_id, cend, s_red, s_red2, s_cut, tid,
-                                  lane, warp);
+            // count pass over an index without inverted intervals: the prepare pass counted every
+            // query but those with start > end (from ranks)
+            const bool rank_run = !EMIT && a.end_sorted != nullptr && !code_is_inverted(cw, a.G);
             if (!is_long && !rank_run) {
                 // a tile that is one run can reuse the candidate lists the count pass stored
                 const bool whole = (r0 == 0 && r1 == nt);
@@ -865,7 +827,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_tiles(TileArgs<S> a) {
                 }
                 if (per_query) nc = 0;
             }
-            if (long_run) {
+            if (long_run && !rank_run) {
                 // long queries share the tile's long-interval candidates (long pyramid)
                 S mn = Lim<S>::hi;
                 int32_t um = INT32_MIN;
@@ -906,7 +868,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_tiles(TileArgs<S> a) {
                     nc = 0;
                 }
             }
-            if (per_query || long_run) {
+            if ((per_query || long_run) && !rank_run) {
                 // per-query work differs widely in length: warps claim queries one at a time
                 if (tid == 0) s_next = r0;
                 __syncthreads();
@@ -1181,6 +1143,13 @@ __global__ void k_qend_minmax(const S* __restrict__ qe, int64_t nq, unsigned lon
     }
 }
 
+// Class code of a query (see code_is_long): a query with start > end takes the long-query path,
+// which does not need start <= end.
+__device__ __forceinline__ uint32_t query_code(int32_t g, int G, bool inverted, bool is_long) {
+    if (g < 0 || g >= G) return 3u * (uint32_t)G;
+    return (uint32_t)g + (inverted ? 2u * (uint32_t)G : is_long ? (uint32_t)G : 0u);
+}
+
 // One 32-bit key per query: class code above the end's offset from the batch's smallest end,
 // shifted right by `shift` (tiles need queries grouped by class and contig and close in
 // position, not exactly ordered).  Also writes (start, end) interleaved for the prepare pass.
@@ -1193,9 +1162,8 @@ __global__ void k_qkeys_packed(const S* __restrict__ qs, const S* __restrict__ q
     if (q >= nq) return;
     const int32_t g = qc ? qc[q] : 0;
     const S s = qs[q], e = qe[q];
-    // a query with start > end takes the long-query path, which does not need start <= end
-    const bool is_long = s > e || ((double)e - (double)s + 1.0) > (double)long_len;
-    const uint32_t code = (g < 0 || g >= G) ? 2u * (uint32_t)G : (uint32_t)g + (is_long ? (uint32_t)G : 0u);
+    const bool is_long = ((double)e - (double)s + 1.0) > (double)long_len;
+    const uint32_t code = query_code(g, G, s > e, is_long);
     const unsigned long long rel = ((unsigned long long)(int64_t)e ^ 0x8000000000000000ull) - mm[0];
     key[q] = (code << ebits) | (uint32_t)(rel >> shift);
     pay[q] = (uint32_t)q;
@@ -1210,7 +1178,7 @@ __global__ void k_qkeys(const S* __restrict__ qs, const S* __restrict__ qe, cons
     const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= nq) return;
     const int32_t g = qc ? qc[q] : 0;
-    const bool is_long = qs[q] > qe[q] || ((double)qe[q] - (double)qs[q] + 1.0) > (double)long_len;
+    const bool is_long = ((double)qe[q] - (double)qs[q] + 1.0) > (double)long_len;
     // The end key drops its lowest byte: tiles need queries grouped by class and contig and
     // close in position, not exactly ordered, and a constant digit costs no sort pass.
     if constexpr (sizeof(S) == 4) {
@@ -1220,8 +1188,7 @@ __global__ void k_qkeys(const S* __restrict__ qs, const S* __restrict__ qe, cons
         w0[q] = (uint32_t)b & ~0xffu;
         w1[q] = (uint32_t)(b >> 32);
     }
-    // class code: short queries of contig g -> g, long ones -> G + g, bad contig ids -> 2G
-    wc[q] = (g < 0 || g >= G) ? 2u * (uint32_t)G : (uint32_t)g + (is_long ? (uint32_t)G : 0u);
+    wc[q] = query_code(g, G, qs[q] > qe[q], is_long);
     pay[q] = (uint32_t)q;
 }
 
@@ -1233,7 +1200,7 @@ constexpr int kPrepWindow = 2048;  // starts staged per block by the cooperative
 // stages the starts between the two answers in shared memory and resolves every query
 // there.  Otherwise each query searches on its own.
 template <typename S>
-__global__ void __launch_bounds__(kThreads) k_qprep(const uint32_t* __restrict__ pay,
+__global__ void __launch_bounds__(kThreads, 6) k_qprep(const uint32_t* __restrict__ pay,
                                                     const uint32_t* __restrict__ wc, int code_shift,
                                                     const S* __restrict__ qs, const S* __restrict__ qe,
                                                     const S* __restrict__ qpair,
@@ -1243,10 +1210,11 @@ __global__ void __launch_bounds__(kThreads) k_qprep(const uint32_t* __restrict__
                                                     int* d_err, int64_t long_split,
                                                     const int32_t* __restrict__ long_pos,
                                                     const int64_t* __restrict__ long_seg,
-                                                    int64_t* __restrict__ blk_cut) {
+                                                    int64_t* __restrict__ blk_cut, const S* __restrict__ end_sorted,
+                                                    uint32_t* __restrict__ counts) {
     __shared__ S win[kPrepWindow];
-    __shared__ S s_mn[kWarpsPerCta], s_mx[kWarpsPerCta], s_mq[kWarpsPerCta];
-    __shared__ int64_t s_a, s_b;
+    __shared__ S s_mn[kWarpsPerCta], s_mx[kWarpsPerCta], s_mq[kWarpsPerCta], s_xq[kWarpsPerCta];
+    __shared__ int64_t s_a, s_b, s_ra, s_rb;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int64_t jb = (int64_t)blockIdx.x * kThreads;
     const int64_t j = jb + tid;
@@ -1267,23 +1235,26 @@ __global__ void __launch_bounds__(kThreads) k_qprep(const uint32_t* __restrict__
         }
     }
     const uint32_t cfirst = wc[jb] >> code_shift, clast = wc[jl] >> code_shift;
-    const bool uniform = cfirst == clast && cfirst < 2u * (uint32_t)m.G;  // sorted: one code
-    int g = (int)(cw >= (uint32_t)m.G ? cw - (uint32_t)m.G : cw);
+    const bool uniform = cfirst == clast && cfirst < 3u * (uint32_t)m.G;  // sorted: one code
+    int g = code_contig(valid ? cw : cfirst, m.G);
     bool bad = false;
-    if (valid && cw >= 2u * (uint32_t)m.G) {
+    if (valid && cw >= 3u * (uint32_t)m.G) {
         atomicCAS(d_err, kDevOk, kDevBadContig);
-        g = 0;
         bad = true;
     }
-    if (!valid) g = (int)(cfirst >= (uint32_t)m.G ? cfirst - (uint32_t)m.G : cfirst);
-    if (g >= m.G) g = 0;
     const int64_t lo = m.seg[g];
     const int64_t n = m.seg[g + 1] - lo;
     int64_t u = -1;
     bool done = false;
     if (blk_cut && tid == 0 && !uniform) blk_cut[2 * blockIdx.x] = -1;
+    // queries with start <= end (short and long classes) are counted here from two ranks when
+    // the index keeps its sorted ends: count = #(start <= qe) - #(end < qs), as no interval
+    // has start > end
+    const bool rank_count = counts != nullptr && end_sorted != nullptr;
+    const bool rank_block = rank_count && uniform && cfirst < 2u * (uint32_t)m.G && n > 0;
     if (uniform) {
         S mn = valid ? v : Lim<S>::hi, mx = valid ? v : Lim<S>::lo, mq = valid ? vs : Lim<S>::hi;
+        S xq = valid ? vs : Lim<S>::lo;
 #pragma unroll
         for (int d = 16; d > 0; d >>= 1) {
             const S o = __shfl_xor_sync(kFull, mn, d);
@@ -1292,13 +1263,27 @@ __global__ void __launch_bounds__(kThreads) k_qprep(const uint32_t* __restrict__
             mx = p > mx ? p : mx;
             const S r = __shfl_xor_sync(kFull, mq, d);
             mq = r < mq ? r : mq;
+            const S x = __shfl_xor_sync(kFull, xq, d);
+            xq = x > xq ? x : xq;
         }
         if (lane == 0) {
             s_mn[warp] = mn;
             s_mx[warp] = mx;
             s_mq[warp] = mq;
+            s_xq[warp] = xq;
         }
         __syncthreads();
+        if (rank_block && (warp == 2 || warp == 3)) {
+            // the block's ranks lie between those of its smallest (warp 2) and largest (warp 3) qs
+            S key = warp == 2 ? s_mq[0] : s_xq[0];
+            for (int w = 1; w < kWarpsPerCta; ++w)
+                key = warp == 2 ? (s_mq[w] < key ? s_mq[w] : key) : (s_xq[w] > key ? s_xq[w] : key);
+            const int64_t r = warp_first_geq<S, S>(end_sorted, lo, lo + n, key, lane);
+            if (lane == 0) {
+                if (warp == 2) s_ra = r;
+                else s_rb = r;
+            }
+        }
         if (blk_cut && warp == 1) {
             // for the tile of these queries (warp 1, beside warp 0's searches): p_cut = first
             // position whose start is within long_split of the smallest qs, and the first
@@ -1342,11 +1327,40 @@ __global__ void __launch_bounds__(kThreads) k_qprep(const uint32_t* __restrict__
         } else {
             done = true;
         }
+        if (rank_block) {
+            __syncthreads();  // win is reused for the ends between the two ranks
+            const int64_t A = s_ra, B = s_rb;
+            const bool staged = B - A <= kPrepWindow;
+            if (staged)
+                for (int64_t k = tid; k < B - A; k += kThreads) win[k] = end_sorted[A + k];
+            __syncthreads();
+            if (valid) {
+                int64_t b0 = 0, b1 = B - A;  // first index of the window whose end is >= qs
+                while (b0 < b1) {
+                    const int64_t mid = (b0 + b1) >> 1;
+                    const S e = staged ? win[mid] : end_sorted[A + mid];
+                    if (e < vs) b0 = mid + 1;
+                    else b1 = mid;
+                }
+                const int64_t below = A + b0 - lo;  // ends before qs
+                counts[orig] = (!bad && u + 1 > below) ? (uint32_t)(u + 1 - below) : 0u;
+            }
+        }
     }
     if (!valid) return;
     if (!done && !bad && n > 0) {
         const S* tr = (U.mode == 1) ? U.eytz_keys + (int64_t)g * U.eytz_n : nullptr;
         u = ub_search(U, g, m.starts + lo, n, v, tr);
+    }
+    if (rank_count && !rank_block && (bad || cw < 2u * (uint32_t)m.G)) {
+        // a block of mixed classes: each query searches its rank on its own
+        int64_t b0 = 0, b1 = bad ? 0 : n;
+        while (b0 < b1) {
+            const int64_t mid = (b0 + b1) >> 1;
+            if (end_sorted[lo + mid] < vs) b0 = mid + 1;
+            else b1 = mid;
+        }
+        counts[orig] = (!bad && u + 1 > b0) ? (uint32_t)(u + 1 - b0) : 0u;
     }
     sq_s[j] = vs;
     sq_u[j] = (int32_t)(lo + u);
@@ -1667,7 +1681,7 @@ int batched_prepare(BatchedWorkspace& ws, MapView<S> m, Levels<S>, int, const in
 
 template <typename S>
 int batched_prepare_queries(BatchedWorkspace& ws, MapView<S> m, const QueryBatch& q, int* d_err, int ub_mode,
-                            cudaStream_t st) {
+                            cudaStream_t st, uint32_t* counts) {
     const int64_t nq = q.nq;
     ws.prepared_nq = -1;
     if (nq <= 0) return SI_OK;
@@ -1702,7 +1716,7 @@ int batched_prepare_queries(BatchedWorkspace& ws, MapView<S> m, const QueryBatch
     SI_CU(cudaStreamSynchronize(st));
     const unsigned long long span = mm[1] - mm[0];
     int code_bits = 1;
-    while (code_bits < 32 && ((uint64_t)1 << code_bits) <= (uint64_t)(2 * m.G)) ++code_bits;
+    while (code_bits < 32 && ((uint64_t)1 << code_bits) <= (uint64_t)(3 * (int64_t)m.G)) ++code_bits;
     int span_bits = 0;
     while (span_bits < 64 && (span >> span_bits) != 0) ++span_bits;
     const int shift = std::max(8, span_bits + code_bits - 24);
@@ -1737,7 +1751,8 @@ int batched_prepare_queries(BatchedWorkspace& ws, MapView<S> m, const QueryBatch
                                               static_cast<const S*>(q.qe), packed ? ws.qpair.as<S>() : nullptr,
                                               nq, m, U, ws.sq_s.as<S>(), ws.sq_u.as<int32_t>(),
                                               ws.sq_c.as<uint32_t>(), ws.sq_id.as<int32_t>(), d_err, ws.long_split,
-                                              ws.long_pos, ws.long_seg, ws.long_pos ? ws.blk_cut.as<int64_t>() : nullptr);
+                                              ws.long_pos, ws.long_seg, ws.long_pos ? ws.blk_cut.as<int64_t>() : nullptr,
+                                              static_cast<const S*>(ws.end_sorted), counts);
     note_launch();
     SI_CU(cudaGetLastError());
     ws.launches += 2 + 3 * passes + 1;
@@ -1790,17 +1805,23 @@ static int run_tiles(BatchedWorkspace& ws, MapView<S> m, Levels<S> L, int H, int
     a.cache = (use_cache && ws.cache_ok) ? ws.tile_cache.as<unsigned char>() : nullptr;
     a.cache_stride = ws.cache_stride;
     const size_t sm = tile_smem(ws.prm, sizeof(S));
-    int dev = 0, nsm = 152, per_sm = 1;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-    if (emit) {
-        SI_CU(cudaFuncSetAttribute(k_tiles<S, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-        SI_CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tiles<S, true>, kThreads, sm));
-    } else {
-        SI_CU(cudaFuncSetAttribute(k_tiles<S, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-        SI_CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tiles<S, false>, kThreads, sm));
+    // the kernel attribute and the occupancy are set / asked once per shared-memory size
+    const int e = emit ? 1 : 0;
+    if (ws.occ_smem[e] != sm) {
+        int dev = 0, nsm = 152, per_sm = 1;
+        SI_CU(cudaGetDevice(&dev));
+        SI_CU(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+        if (emit) {
+            SI_CU(cudaFuncSetAttribute(k_tiles<S, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+            SI_CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tiles<S, true>, kThreads, sm));
+        } else {
+            SI_CU(cudaFuncSetAttribute(k_tiles<S, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+            SI_CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tiles<S, false>, kThreads, sm));
+        }
+        ws.occ_blocks[e] = nsm * std::max(per_sm, 1);
+        ws.occ_smem[e] = sm;
     }
-    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)nsm * std::max(per_sm, 1), a.n_tiles));
+    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)ws.occ_blocks[e], a.n_tiles));
     if (emit) k_tiles<S, true><<<grid, kThreads, sm, st>>>(a);
     else k_tiles<S, false><<<grid, kThreads, sm, st>>>(a);
     note_launch();
@@ -1868,7 +1889,7 @@ int upper_bounds(BatchedWorkspace& ws, MapView<S> m, const QueryBatch& q, int ub
     template int batched_prepare<S>(BatchedWorkspace&, MapView<S>, Levels<S>, int, const int64_t*, int,            \
                                     cudaStream_t);                                                              \
     template int batched_prepare_queries<S>(BatchedWorkspace&, MapView<S>, const QueryBatch&, int*, int,          \
-                                            cudaStream_t);                                                      \
+                                            cudaStream_t, uint32_t*);                                                      \
     template int batched_count<S>(BatchedWorkspace&, MapView<S>, Levels<S>, int, const QueryBatch&, uint32_t*,   \
                                   int*, cudaStream_t);                                                          \
     template int batched_emit<S>(BatchedWorkspace&, MapView<S>, Levels<S>, int, const QueryBatch&, int64_t,      \

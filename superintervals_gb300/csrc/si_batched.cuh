@@ -73,6 +73,10 @@ struct BatchedWorkspace {
     bool cache_ok = false;
     int64_t cache_stride = 0;
     int cache_prm_tile = 0, cache_prm_cap = 0;
+    // tiles kernels (count, emit): dynamic shared memory their attribute was set for, and
+    // resident blocks on the device at that size
+    size_t occ_smem[2] = {0, 0};
+    int occ_blocks[2] = {0, 0};
     // long-interval list: global positions and ends of the intervals at least long_split long,
     // in position order, its max pyramid (long_H levels) and each contig's first list index
     const void* long_ends = nullptr;
@@ -92,10 +96,12 @@ constexpr int64_t kLongIntervalSplit = 65536;
 template <typename S>
 int batched_prepare(BatchedWorkspace& ws, MapView<S> m, Levels<S> L, int H, const int64_t* lvl_sizes,
                     int ub_mode, cudaStream_t st);
-// Sorts the queries by (class, contig, end) and finds each one's upper bound.
+// Sorts the queries by (class, contig, end) and finds each one's upper bound.  With counts and
+// an index that keeps its sorted ends (no interval has start > end), also writes the count of
+// every short query (the count pass then handles the long ones only).
 template <typename S>
 int batched_prepare_queries(BatchedWorkspace& ws, MapView<S> m, const QueryBatch& q, int* d_err,
-                            int ub_mode, cudaStream_t st);
+                            int ub_mode, cudaStream_t st, uint32_t* counts = nullptr);
 template <typename S>
 int batched_count(BatchedWorkspace& ws, MapView<S> m, Levels<S> L, int H, const QueryBatch& q,
                   uint32_t* counts, int* d_err, cudaStream_t st);

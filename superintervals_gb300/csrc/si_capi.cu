@@ -464,7 +464,8 @@ int run_count(gSuperIntervals* si, const sig::QueryBatch& q, uint32_t* d_counts,
     if (use_batched(si, q.nq)) {
         {
             PhaseTimer pt(si, 3, st);
-            int r = sig::batched_prepare_queries<S>(si->bws, view<S>(si), q, si->w_err.as<int>(), si->ub_mode, st);
+            int r = sig::batched_prepare_queries<S>(si->bws, view<S>(si), q, si->w_err.as<int>(), si->ub_mode, st,
+                                                    d_counts);
             if (r != SI_OK) return fail(r, "batched query preparation failed (status %d)", r);
         }
         PhaseTimer pt(si, 0, st);

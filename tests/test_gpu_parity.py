@@ -123,6 +123,24 @@ def test_config3_long_queries_scaled(api, oracle, path):
     _oracle_case(api, oracle, W.config3(n=200_000, nq=50_000, long_queries=True), path, orders=(0,))
 
 
+@pytest.mark.parametrize("inverted_intervals", [False, True])
+def test_query_classes_both_count_modes(api, oracle, inverted_intervals):
+    """Short, long and start > end queries in one batch.  Without inverted intervals the
+    batched path counts every query with start <= end from two ranks (and the count pass
+    only the start > end ones); with some, it counts all of them from the tile lists."""
+    from superintervals_gb300 import workloads as W
+    wl = W.config3(n=200_000, nq=60_000, long_queries=True)
+    r = np.random.default_rng(5)
+    flip = r.random(wl.nq) < 0.03
+    wl.q_starts[flip], wl.q_ends[flip] = wl.q_ends[flip].copy(), wl.q_starts[flip].copy()
+    assert (wl.q_starts > wl.q_ends).any()
+    if inverted_intervals:
+        inv = r.random(wl.n) < 0.005
+        wl.starts[inv], wl.ends[inv] = wl.ends[inv].copy(), wl.starts[inv].copy()
+        assert (wl.starts > wl.ends).any()
+    _oracle_case(api, oracle, wl, "batched", orders=(0, 1))
+
+
 @pytest.mark.parametrize("path", PATHS)
 @pytest.mark.parametrize("seed,dt", [(21, np.int32), (22, np.int64), (23, np.int32)])
 def test_random_nested(api, oracle, seed, dt, path):
