@@ -322,7 +322,8 @@ def run_gpu(args, rank, world, dist):
             C.memmove(hq_c, wl.q_contig.ctypes.data, wl.q_contig.nbytes)
         h_off = pinned(8 * (nq + 1))
         h_out = pinned(4 * max(P, 1))
-        idx.set_output_budget(max(4 * P, 1 << 20))
+        # the library's default output budget: the result comes back in chunks, the emit of
+        # one overlapping the device-to-host copy of the previous one
 
         def e2e_step():
             _capi.check(lib.searchBatchIntoGpu(idx.h, hq_s, hq_e, hq_c, nq, 0, 0, h_off, h_out, P,

@@ -173,6 +173,7 @@ struct TileArgs {
     // emit pass
     const int32_t* heads_in;
     const int64_t* offsets;
+    int64_t id_lo, id_hi;    // emit only the queries with ids in [id_lo, id_hi)
     int64_t out_base;
     int order;
     bool values;
@@ -622,13 +623,19 @@ __global__ void __launch_bounds__(kThreads, 4) k_tiles(TileArgs<S> a) {
             if (EMIT) {
                 // the tile's random per-query reads, issued together instead of per query
                 const int32_t id = q_id[i];
-                const int64_t o = a.offsets[id];
-                q_off[i] = o - a.out_base;
-                q_cap[i] = (int32_t)(a.offsets[id + 1] - o);
-                // queries counted from ranks have no head run from the count pass: the emit
-                // finds it (-1)
-                const bool counted_by_rank = a.end_sorted && !code_is_inverted(q_c[i], a.G);
-                q_h[i] = counted_by_rank ? -1 : a.heads_in[id];
+                if (id < a.id_lo || id >= a.id_hi) {
+                    q_off[i] = 0;
+                    q_cap[i] = -1;  // outside the emitted window: skipped
+                    q_h[i] = 0;
+                } else {
+                    const int64_t o = a.offsets[id];
+                    q_off[i] = o - a.out_base;
+                    q_cap[i] = (int32_t)(a.offsets[id + 1] - o);
+                    // queries counted from ranks have no head run from the count pass: the emit
+                    // finds it (-1)
+                    const bool counted_by_rank = a.end_sorted && !code_is_inverted(q_c[i], a.G);
+                    q_h[i] = counted_by_rank ? -1 : a.heads_in[id];
+                }
             }
         }
         __syncthreads();
@@ -877,6 +884,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_tiles(TileArgs<S> a) {
                     if (lane == 0) i = atomicAdd(&s_next, 1);
                     i = __shfl_sync(kFull, i, 0);
                     if (i >= r1) break;
+                    if (EMIT && q_cap[i] < 0) continue;  // outside the emitted window
                     if (per_query)
                         walk_query<S, EMIT>(a, q_s[i], (int64_t)q_u[i], lo, q_id[i], lane);
                     else
@@ -1020,6 +1028,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_tiles(TileArgs<S> a) {
                 const int64_t u = q_u[i];
                 const int64_t h = q_h[i];
                 const int64_t capq = q_cap[i];
+                if (capq < 0) continue;  // outside the emitted window
                 int32_t* dst = a.out + q_off[i];
                 if (h > capq) {
                     if (lane == 0) atomicCAS(a.d_err, kDevOk, kDevOverflow);
@@ -1766,7 +1775,7 @@ template <typename S>
 static int run_tiles(BatchedWorkspace& ws, MapView<S> m, Levels<S> L, int H, int64_t nq, bool emit,
                      uint32_t* counts, int32_t* heads, const int32_t* heads_in, const int64_t* offsets,
                      int64_t out_base, int order, bool values, int32_t* out, int* d_err, bool use_cache,
-                     cudaStream_t st) {
+                     cudaStream_t st, int64_t id_lo = 0, int64_t id_hi = INT64_MAX) {
     SI_OKR(ws.counters.reserve(sizeof(int) * 4));
     SI_CU(cudaMemsetAsync(ws.counters.p, 0, sizeof(int) * 4, st));
     TileArgs<S> a;
@@ -1797,6 +1806,8 @@ static int run_tiles(BatchedWorkspace& ws, MapView<S> m, Levels<S> L, int H, int
     a.heads = heads;
     a.heads_in = heads_in;
     a.offsets = offsets;
+    a.id_lo = id_lo;
+    a.id_hi = id_hi;
     a.out_base = out_base;
     a.order = order;
     a.values = values;
@@ -1863,11 +1874,20 @@ int batched_emit(BatchedWorkspace& ws, MapView<S> m, Levels<S> L, int H, const Q
     if (nq <= 0) return SI_OK;
     if (q_offset < 0 || q_offset + nq > ws.n_heads) return SI_ERR_INVALID;
     const bool same = (q_offset == 0 && ws.prepared_nq == nq && ws.prepared_qs == q.qs);
+    // a slice of the batch prepared last: its tiles are kept (sorted neighbours share candidate
+    // lists) and only the slice's ids are emitted, instead of sorting the slice on its own,
+    // whose queries would lie far apart
+    const bool window = !same && ws.prepared_qs != nullptr && ws.prepared_nq >= q_offset + nq &&
+                        static_cast<const S*>(q.qs) - q_offset == static_cast<const S*>(ws.prepared_qs);
+    const bool cache_fits = ws.cache_ok && ws.cache_prm_tile == ws.prm.tile_q && ws.cache_prm_cap == ws.prm.cap;
+    if (window)
+        return run_tiles<S>(ws, m, L, H, ws.prepared_nq, true, nullptr, nullptr, ws.heads.as<int32_t>(),
+                            offsets - q_offset, out_base, order, values, out, d_err, cache_fits, st, q_offset,
+                            q_offset + nq);
     if (!same) SI_OKR(batched_prepare_queries<S>(ws, m, q, d_err, ub_mode, st));
-    const bool cache = same && ws.cache_ok && ws.cache_prm_tile == ws.prm.tile_q && ws.cache_prm_cap == ws.prm.cap;
     // sorted ids are relative to q; heads / offsets are shifted to the slice
     return run_tiles<S>(ws, m, L, H, nq, true, nullptr, nullptr, ws.heads.as<int32_t>() + q_offset, offsets,
-                        out_base, order, values, out, d_err, cache, st);
+                        out_base, order, values, out, d_err, same && cache_fits, st);
 }
 
 template <typename S>

@@ -145,6 +145,11 @@ struct gSuperIntervals {
     bool input_was_sorted = false;
     // query workspace
     DevBuf wq_s, wq_e, wq_c, w_counts, w_offsets, w_out, w_tmp, w_err;
+    // host-buffer searches of several chunks: a second result buffer and a copy stream, so
+    // that the emit of one chunk overlaps the device-to-host copy of the previous one
+    DevBuf w_out2;
+    cudaStream_t copy_st = nullptr;
+    cudaEvent_t ev_emitted[2] = {nullptr, nullptr}, ev_copied[2] = {nullptr, nullptr};
     sig::BatchedWorkspace bws;
     // set operations: hit lists, staged pieces, and whether some interval has start > end
     DevBuf so_hoff, so_hits, so_off, so_os, so_oe, so_ob, so_flag;
@@ -589,13 +594,13 @@ int search_host(gSuperIntervals* si, const S* qs, const S* qe, const int32_t* qc
     if (P == 0) return read_dev_err(si);
     // Results are staged in device memory and copied in bulk: the emit writes every query's
     // list at a scattered place, and such writes over the host link run several times slower
-    // than one large copy.
-    // chunked emit against the device output budget
+    // than one large copy.  The output is cut into chunks of queries whose lists fit the
+    // device output budget; with more than one chunk, chunks alternate between two device
+    // buffers and the emit of one overlaps the copy of the one before (copy stream).
     const int64_t budget = std::max<int64_t>((int64_t)(si->out_budget / sizeof(int32_t)), 1 << 20);
     const int64_t buf = std::min<int64_t>(P, budget);
-    size_t qa = 0;
-    while (qa < nq) {
-        size_t qb = qa;
+    std::vector<size_t> cuts{0};
+    for (size_t qa = 0; qa < nq;) {
         // largest qb with off[qb] - off[qa] <= buf (at least one query)
         const int64_t limit = h_off[qa] + buf;
         size_t lo = qa + 1, hi = nq;
@@ -604,21 +609,50 @@ int search_host(gSuperIntervals* si, const S* qs, const S* qe, const int32_t* qc
             if (h_off[mid] <= limit) lo = mid;
             else hi = mid - 1;
         }
-        qb = lo;
+        cuts.push_back(lo);
+        qa = lo;
+    }
+    const size_t n_chunks = cuts.size() - 1;
+    int64_t max_need = 1;
+    for (size_t c = 0; c < n_chunks; ++c) max_need = std::max<int64_t>(max_need, h_off[cuts[c + 1]] - h_off[cuts[c]]);
+    SI_TRY(si->w_out.reserve(sizeof(int32_t) * max_need));
+    if (n_chunks > 1) {
+        SI_TRY(si->w_out2.reserve(sizeof(int32_t) * max_need));
+        if (!si->copy_st) SI_CK(cudaStreamCreateWithFlags(&si->copy_st, cudaStreamNonBlocking));
+        for (int b = 0; b < 2; ++b) {
+            if (!si->ev_emitted[b]) SI_CK(cudaEventCreateWithFlags(&si->ev_emitted[b], cudaEventDisableTiming));
+            if (!si->ev_copied[b]) SI_CK(cudaEventCreateWithFlags(&si->ev_copied[b], cudaEventDisableTiming));
+        }
+    }
+    for (size_t c = 0; c < n_chunks; ++c) {
+        const size_t qa = cuts[c], qb = cuts[c + 1];
         const int64_t need = h_off[qb] - h_off[qa];
-        SI_TRY(si->w_out.reserve(sizeof(int32_t) * std::max<int64_t>(need, 1)));
+        const int b = (int)(c & 1);
+        int32_t* dbuf = b ? si->w_out2.as<int32_t>() : si->w_out.as<int32_t>();
+        // the buffer's previous copy (chunk c - 2) must be done before the emit overwrites it
+        if (c >= 2) SI_CK(cudaStreamWaitEvent(st, si->ev_copied[b], 0));
         sig::QueryBatch sub = q;
         sub.qs = static_cast<const S*>(q.qs) + qa;
         sub.qe = static_cast<const S*>(q.qe) + qa;
         sub.qc = q.qc ? q.qc + qa : nullptr;
         sub.nq = (int64_t)(qb - qa);
-        SI_TRY(run_emit<S>(si, sub, (int64_t)qa, d_off + qa, h_off[qa], order, values, si->w_out.as<int32_t>(), st));
+        SI_TRY(run_emit<S>(si, sub, (int64_t)qa, d_off + qa, h_off[qa], order, values, dbuf, st));
+        if (n_chunks == 1) {
+            if (need)
+                SI_CK(cudaMemcpyAsync(h_out + h_off[qa], dbuf, sizeof(int32_t) * need, cudaMemcpyDeviceToHost, st));
+            continue;
+        }
+        SI_CK(cudaEventRecord(si->ev_emitted[b], st));
+        SI_CK(cudaStreamWaitEvent(si->copy_st, si->ev_emitted[b], 0));
         if (need)
-            SI_CK(cudaMemcpyAsync(h_out + h_off[qa], si->w_out.p, sizeof(int32_t) * need,
-                                  cudaMemcpyDeviceToHost, st));
-        SI_CK(cudaStreamSynchronize(st));
-        qa = qb;
+            SI_CK(cudaMemcpyAsync(h_out + h_off[qa], dbuf, sizeof(int32_t) * need, cudaMemcpyDeviceToHost,
+                                  si->copy_st));
+        SI_CK(cudaEventRecord(si->ev_copied[b], si->copy_st));
     }
+    // the compute stream waits for the last copy (the copy stream runs in order), so later
+    // work on it sees the results
+    if (n_chunks > 1) SI_CK(cudaStreamWaitEvent(st, si->ev_copied[(n_chunks - 1) & 1], 0));
+    SI_CK(cudaStreamSynchronize(st));
     return read_dev_err(si);
 }
 
@@ -717,6 +751,14 @@ void destroySuperIntervalsGpu(gSuperIntervals* si) {
     cudaStreamSynchronize(si->st);
     if (si->ev0) cudaEventDestroy(si->ev0);
     if (si->ev1) cudaEventDestroy(si->ev1);
+    if (si->copy_st) {
+        cudaStreamSynchronize(si->copy_st);
+        cudaStreamDestroy(si->copy_st);
+    }
+    for (int b = 0; b < 2; ++b) {
+        if (si->ev_emitted[b]) cudaEventDestroy(si->ev_emitted[b]);
+        if (si->ev_copied[b]) cudaEventDestroy(si->ev_copied[b]);
+    }
     if (si->gexec) cudaGraphExecDestroy(si->gexec);
     cudaStream_t st = si->st;
     delete si;  // releases device buffers
