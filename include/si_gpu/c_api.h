@@ -173,8 +173,9 @@ int getBatchedParamsGpu(const gSuperIntervals* si, int* tile_queries, int* tile_
 int autotuneBatchedGpu(gSuperIntervals* si, const void* d_qs, const void* d_qe,
                        const int32_t* d_qcontig, size_t nq, size_t sample, int flags, char* report,
                        size_t report_len);
-/* Device bytes one search call may use for its result buffer; larger results
- * are emitted in query chunks against it. */
+/* Device bytes one host-buffer search call may use for a result chunk (4 GiB by
+ * default); larger results are emitted in query chunks against it, two chunk
+ * buffers alternating so that emit and device-to-host copy overlap. */
 int setOutputBudgetGpu(gSuperIntervals* si, size_t bytes);
 /* Per-phase device time of the query pipeline, measured with CUDA events on
  * the stream the phase runs on while profiling is on (it synchronizes after
