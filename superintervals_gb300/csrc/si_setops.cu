@@ -151,6 +151,8 @@ __global__ void __launch_bounds__(kThreads) k_diff(MapView<S> m, const S* __rest
             }
             continue;
         }
+        // the writing pass skips the queries without a piece (often nearly all of them)
+        if (EMIT && ooff[q + 1] == ooff[q]) continue;
         const int64_t a = hoff[q], b = hoff[q + 1], mq = b - a;
         const S s0 = qs[q], e0 = qe[q];
         const int64_t lo = m.seg[g];
@@ -203,6 +205,8 @@ __global__ void __launch_bounds__(kThreads) k_diff(MapView<S> m, const S* __rest
             c += __popc(gb);
             cursor = smax(cursor, __shfl_sync(kFull, incl, 31));
             closed = closed || clb != 0;
+            // covered up to qe: the later hits (starting at or before qe) open no gap
+            if (closed || cursor > e0) break;
         }
         if (!closed && cursor <= e0) {
             if (EMIT && lane == 0) {
