@@ -628,7 +628,9 @@ def rows_algorithmic_bytes(op, Q, H, P, s):
         return Q * (2 * s + 8) + H * (2 * s) + P * (2 * s), "Q(2s+8) + H(2s) + P(2s)"
     if op == "keys":
         return Q * (2 * s + 8) + H * (2 * s + 4) * 2, "Q(2s+8) + 2H(2s+4)"
-    return Q * (3 * s + 8) + H * (2 * s), "Q(3s+8) + H(2s)"
+    # coverage comes from ranks and prefix sums (no hit lists) when no interval and no query has
+    # start > end: per query, its read and the count and coverage written
+    return Q * (3 * s + 12), "Q(3s+12): query read, count and coverage written (no per-hit traffic)"
 
 
 def rows_cpu(op, wl, seconds, nth):

@@ -1377,6 +1377,129 @@ __global__ void __launch_bounds__(kThreads, 6) k_qprep(const uint32_t* __restric
     sq_id[j] = (int32_t)orig;
 }
 
+// First index k in [lo, hi) of the ascending array arr with arr[k] >= key (strict: > key), for
+// every thread's key of a block of 256 sorted queries.  A uniform block (one contig, keys
+// close together) finds the ranks of its smallest and largest key with one warp each, stages
+// the entries between them in shared memory (win, kPrepWindow slots) when they fit and
+// resolves each key there; otherwise each key searches [lo, hi) on its own.  Block-wide.
+template <typename S>
+__device__ int64_t block_rank(const S* __restrict__ arr, int64_t lo, int64_t hi, S key, bool strict, bool valid,
+                              bool uniform, S* win, S* s_kmin, S* s_kmax, int64_t* s_r, int tid, int lane,
+                              int warp) {
+    // strict: arr > key, i.e. arr >= key + 1 (no key + 1 above the largest value)
+    const bool none = strict && key == Lim<S>::hi;
+    const S k2 = (strict && !none) ? (S)(key + 1) : key;
+    if (!uniform) {
+        if (!valid || none) return hi;
+        int64_t b0 = lo, b1 = hi;
+        while (b0 < b1) {
+            const int64_t mid = (b0 + b1) >> 1;
+            if (arr[mid] < k2) b0 = mid + 1;
+            else b1 = mid;
+        }
+        return b0;
+    }
+    S mn = (valid && !none) ? k2 : Lim<S>::hi, mx = (valid && !none) ? k2 : Lim<S>::lo;
+    const bool any_none = __syncthreads_or(valid && none);
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) {
+        const S o = __shfl_xor_sync(kFull, mn, d);
+        mn = o < mn ? o : mn;
+        const S p = __shfl_xor_sync(kFull, mx, d);
+        mx = p > mx ? p : mx;
+    }
+    if (lane == 0) {
+        s_kmin[warp] = mn;
+        s_kmax[warp] = mx;
+    }
+    __syncthreads();
+    if (warp < 2) {
+        S k = warp == 0 ? s_kmin[0] : s_kmax[0];
+        for (int w = 1; w < kWarpsPerCta; ++w)
+            k = warp == 0 ? (s_kmin[w] < k ? s_kmin[w] : k) : (s_kmax[w] > k ? s_kmax[w] : k);
+        const int64_t r = warp_first_geq<S, S>(arr, lo, hi, k, lane);
+        if (lane == 0) s_r[warp] = r;
+    }
+    __syncthreads();
+    const int64_t A = s_r[0], B = any_none ? hi : s_r[1];
+    const bool staged = B - A <= kPrepWindow;
+    if (staged)
+        for (int64_t k = tid; k < B - A; k += kThreads) win[k] = arr[A + k];
+    __syncthreads();
+    int64_t r = hi;
+    if (valid && !none) {
+        int64_t b0 = 0, b1 = B - A;
+        while (b0 < b1) {
+            const int64_t mid = (b0 + b1) >> 1;
+            const S e = staged ? win[mid] : arr[A + mid];
+            if (e < k2) b0 = mid + 1;
+            else b1 = mid;
+        }
+        r = A + b0;
+    }
+    __syncthreads();  // win and the reductions are reused by the next call
+    return r;
+}
+
+// coverage of sorted queries from ranks and prefix sums, for an index without intervals with
+// start > end and queries with start <= end.  Over the hits {start <= qe} minus {end < qs}:
+//   count = a_u - r_qs
+//   sum min(end, qe) = PE[r_qe] - PE[r_qs] + qe * (a_u - r_qe)
+//   sum max(start, qs) = PS[a_u] - PS[ls] + qs * (ls - r_qs)
+// with a_u = 1 + the upper bound of qe, r_qs / r_qe the first sorted ends >= qs / > qe, ls the
+// first start >= qs, and PS / PE the exclusive prefix sums (mod 2^64) of the starts and of
+// the sorted ends.  The coverage, sum min - sum max, wraps as the coordinate type does.
+template <typename S>
+__global__ void __launch_bounds__(kThreads) k_cov_ranks(const S* __restrict__ sq_s, const int32_t* __restrict__ sq_u,
+                                                        const uint32_t* __restrict__ sq_c,
+                                                        const int32_t* __restrict__ sq_id, const S* __restrict__ qe,
+                                                        int64_t nq, MapView<S> m, const S* __restrict__ end_sorted,
+                                                        const uint64_t* __restrict__ ps_start,
+                                                        const uint64_t* __restrict__ ps_end,
+                                                        uint64_t* __restrict__ count, S* __restrict__ cov) {
+    __shared__ S win[kPrepWindow];
+    __shared__ S s_kmin[kWarpsPerCta], s_kmax[kWarpsPerCta];
+    __shared__ int64_t s_r[2];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int64_t jb = (int64_t)blockIdx.x * kThreads, j = jb + tid;
+    const int64_t jl = (jb + kThreads < nq ? jb + kThreads : nq) - 1;
+    const bool valid = j < nq;
+    const uint32_t cfirst = sq_c[jb], clast = sq_c[jl];
+    const bool uniform = cfirst == clast && cfirst < 2u * (uint32_t)m.G;  // one contig, start <= end
+    const uint32_t cw = valid ? sq_c[j] : cfirst;
+    const bool bad = cw >= 2u * (uint32_t)m.G;  // bad contig (reported by the prepare pass)
+    const int g = code_contig(cw, m.G);
+    const int64_t lo = m.seg[g], hi = m.seg[g + 1];
+    S s0 = 0, e0 = 0;
+    int64_t u = lo - 1;
+    int32_t id = 0;
+    if (valid) {
+        s0 = sq_s[j];
+        u = sq_u[j];
+        id = sq_id[j];
+        e0 = qe[id];
+    }
+    const bool live = valid && !bad;
+    const int64_t r_qs = block_rank<S>(end_sorted, lo, hi, s0, false, live, uniform, win, s_kmin, s_kmax, s_r, tid,
+                                       lane, warp);
+    const int64_t r_qe = block_rank<S>(end_sorted, lo, hi, e0, true, live, uniform, win, s_kmin, s_kmax, s_r, tid,
+                                       lane, warp);
+    const int64_t ls = block_rank<S>(m.starts, lo, hi, s0, false, live, uniform, win, s_kmin, s_kmax, s_r, tid,
+                                     lane, warp);
+    if (!valid) return;
+    if (!live) {
+        count[id] = 0;
+        cov[id] = 0;
+        return;
+    }
+    const int64_t a_u = u + 1;
+    const uint64_t qe64 = (uint64_t)(int64_t)e0, qs64 = (uint64_t)(int64_t)s0;
+    const uint64_t smin_sum = ps_end[r_qe] - ps_end[r_qs] + qe64 * (uint64_t)(a_u - r_qe);
+    const uint64_t smax_sum = ps_start[a_u] - ps_start[ls] + qs64 * (uint64_t)(ls - r_qs);
+    count[id] = (uint64_t)(a_u - r_qs);
+    cov[id] = (S)(smin_sum - smax_sum);
+}
+
 // upper bounds in the original query order (plain path with an accelerator, tests).  With
 // one contig and the Eytzinger provider, each block first stages the tree in shared memory.
 template <typename S>
@@ -1905,6 +2028,22 @@ int upper_bounds(BatchedWorkspace& ws, MapView<S> m, const QueryBatch& q, int ub
     return SI_OK;
 }
 
+template <typename S>
+int batched_coverage(BatchedWorkspace& ws, MapView<S> m, const QueryBatch& q, const uint64_t* ps_start,
+                     const uint64_t* ps_end, uint64_t* count, S* cov, int* d_err, int ub_mode, cudaStream_t st) {
+    if (q.nq <= 0) return SI_OK;
+    if (!ws.end_sorted) return SI_ERR_INVALID;
+    SI_OKR(batched_prepare_queries<S>(ws, m, q, d_err, ub_mode, st));
+    k_cov_ranks<S><<<nblk(q.nq), kThreads, 0, st>>>(ws.sq_s.as<S>(), ws.sq_u.as<int32_t>(), ws.sq_c.as<uint32_t>(),
+                                                   ws.sq_id.as<int32_t>(), static_cast<const S*>(q.qe), q.nq, m,
+                                                   static_cast<const S*>(ws.end_sorted), ps_start, ps_end, count,
+                                                   cov);
+    note_launch();
+    SI_CU(cudaGetLastError());
+    ws.launches += 1;
+    return SI_OK;
+}
+
 #define SIG_BINST(S)                                                                                             \
     template int batched_prepare<S>(BatchedWorkspace&, MapView<S>, Levels<S>, int, const int64_t*, int,            \
                                     cudaStream_t);                                                              \
@@ -1915,7 +2054,9 @@ int upper_bounds(BatchedWorkspace& ws, MapView<S> m, const QueryBatch& q, int ub
     template int batched_emit<S>(BatchedWorkspace&, MapView<S>, Levels<S>, int, const QueryBatch&, int64_t,      \
                                  const int64_t*, int64_t, int, bool, int32_t*, int*, int, cudaStream_t);        \
     template int upper_bounds<S>(BatchedWorkspace&, MapView<S>, const QueryBatch&, int, int32_t*, int*,          \
-                                 cudaStream_t);
+                                 cudaStream_t);                                                                 \
+    template int batched_coverage<S>(BatchedWorkspace&, MapView<S>, const QueryBatch&, const uint64_t*,         \
+                                     const uint64_t*, uint64_t*, S*, int*, int, cudaStream_t);
 SIG_BINST(int32_t)
 SIG_BINST(int64_t)
 

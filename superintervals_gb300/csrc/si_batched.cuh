@@ -111,6 +111,14 @@ int batched_emit(BatchedWorkspace& ws, MapView<S> m, Levels<S> L, int H, const Q
                  int64_t q_offset, const int64_t* offsets, int64_t out_base, int order, bool values,
                  int32_t* out, int* d_err, int ub_mode, cudaStream_t st);
 
+// Coverage (count and the wrapped sum of min(end, qe) - max(start, qs)) of every query, from
+// ranks and prefix sums (ps_start / ps_end: exclusive prefix sums mod 2^64 of the starts and of
+// the sorted ends, n + 1 entries).  Needs the sorted ends (no interval with start > end) and
+// queries with start <= end.
+template <typename S>
+int batched_coverage(BatchedWorkspace& ws, MapView<S> m, const QueryBatch& q, const uint64_t* ps_start,
+                     const uint64_t* ps_end, uint64_t* count, S* cov, int* d_err, int ub_mode, cudaStream_t st);
+
 // Upper bound of every query (original order) with the handle's accelerator; used by
 // the plain path when a learned / Eytzinger mode is selected, and by tests.
 template <typename S>

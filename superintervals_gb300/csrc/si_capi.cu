@@ -138,6 +138,10 @@ struct gSuperIntervals {
     // long-interval list: intervals >= kLongIntervalSplit long, position order, own pyramid
     DevBuf long_pos, long_end, long_seg;
     DevBuf end_sorted;  // each contig's ends ascending (built when no interval has start > end)
+    // exclusive prefix sums (mod 2^64) of the starts and of the sorted ends, for coverage from
+    // ranks; built by the first such call after a build
+    DevBuf ps_start, ps_end;
+    bool cov_ready = false;
     DevBuf long_lvl[sig::kMaxLevels];
     int64_t long_sizes[sig::kMaxLevels + 1] = {0};
     int long_H = 0;
@@ -280,6 +284,7 @@ int build_impl(gSuperIntervals* si) {
     si->inverted = -1;
     si->bws.long_ends = nullptr;  // set again once the long-interval list exists
     si->bws.end_sorted = nullptr;
+    si->cov_ready = false;
     if (si->gexec) {              // a captured graph holds the old buffers
         cudaGraphExecDestroy(si->gexec);
         si->gexec = nullptr;
@@ -1704,6 +1709,47 @@ int coverage_device(gSuperIntervals* si, const sig::QueryBatch& q, uint64_t* d_c
     SI_TRY(set_dev(si));
     if (q.nq && (!q.qs || !q.qe || !d_count || !d_cov)) return fail(SI_ERR_INVALID, "null device buffer");
     if (q.nq == 0) return SI_OK;
+    if (si->n > 0 && si->inverted == 0 && si->bws.end_sorted) {
+        // no interval has start > end: when no query has start > end either, the coverage comes
+        // from ranks and prefix sums, without hit lists
+        sig::MapView<S> qv = view<S>(si);
+        qv.starts = static_cast<const S*>(q.qs);
+        qv.ends = static_cast<const S*>(q.qe);
+        qv.n = q.nq;
+        SI_TRY(si->so_flag.reserve(2 * sizeof(int)));
+        SI_CK(sig::launch_any_inverted<S>(qv, si->so_flag.as<int>() + 1, st));
+        int inv = 0;
+        SI_CK(cudaMemcpyAsync(&inv, si->so_flag.as<int>() + 1, sizeof(int), cudaMemcpyDeviceToHost, st));
+        SI_CK(cudaStreamSynchronize(st));
+        if (!inv) {
+            if (!si->cov_ready) {
+                SI_TRY(si->ps_start.reserve(sizeof(uint64_t) * (si->n + 1)));
+                SI_TRY(si->ps_end.reserve(sizeof(uint64_t) * (si->n + 1)));
+                DevBuf tmp;
+                SI_TRY(tmp.reserve(sig::scan_temp_bytes(si->n)));
+                if (sizeof(S) == 4) {
+                    SI_CK(sig::exclusive_scan_i32_to_u64((const int32_t*)si->starts.p, si->ps_start.as<uint64_t>(),
+                                                         si->n, tmp.p, st));
+                    SI_CK(sig::exclusive_scan_i32_to_u64((const int32_t*)si->end_sorted.p,
+                                                         si->ps_end.as<uint64_t>(), si->n, tmp.p, st));
+                } else {
+                    SI_CK(sig::exclusive_scan_i64_to_u64((const int64_t*)si->starts.p, si->ps_start.as<uint64_t>(),
+                                                         si->n, tmp.p, st));
+                    SI_CK(sig::exclusive_scan_i64_to_u64((const int64_t*)si->end_sorted.p,
+                                                         si->ps_end.as<uint64_t>(), si->n, tmp.p, st));
+                }
+                SI_CK(cudaStreamSynchronize(st));  // tmp is released on scope exit
+                si->cov_ready = true;
+            }
+            SI_TRY(si->w_err.reserve(sizeof(int)));
+            SI_CK(cudaMemsetAsync(si->w_err.p, 0, sizeof(int), st));
+            const int r = sig::batched_coverage<S>(si->bws, view<S>(si), q, si->ps_start.as<uint64_t>(),
+                                                   si->ps_end.as<uint64_t>(), d_count, d_cov, si->w_err.as<int>(),
+                                                   si->ub_mode, st);
+            if (r != SI_OK) return fail(r, "coverage from ranks failed (status %d)", r);
+            return read_dev_err(si, st);
+        }
+    }
     int64_t P = 0;
     SI_TRY(lists_or_empty<S>(si, q, SI_ORDER_DESC, st, &P));
     SI_CK(sig::launch_coverage<S>(view<S>(si), q, si->so_hoff.as<int64_t>(), si->so_hits.as<int32_t>(), d_count,

@@ -59,6 +59,9 @@ cudaError_t exclusive_scan_u32_to_i64(const uint32_t* in, int64_t* out, int64_t 
                                       cudaStream_t st);
 cudaError_t exclusive_scan_u32_to_u32(const uint32_t* in, uint32_t* out, int64_t n, void* temp,
                                       cudaStream_t st);
+// exclusive prefix sums mod 2^64 of signed coordinates (sign-extended), n + 1 entries
+cudaError_t exclusive_scan_i32_to_u64(const int32_t* in, uint64_t* out, int64_t n, void* temp, cudaStream_t st);
+cudaError_t exclusive_scan_i64_to_u64(const int64_t* in, uint64_t* out, int64_t n, void* temp, cudaStream_t st);
 
 // ---------------------------------------------------------------- BED ingest (si_bed.cu)
 int64_t bed_chunks(int64_t len);

@@ -139,4 +139,12 @@ cudaError_t exclusive_scan_u32_to_u32(const uint32_t* in, uint32_t* out, int64_t
     return scan_impl<uint32_t, uint32_t>(in, out, n, static_cast<char*>(temp), st);
 }
 
+cudaError_t exclusive_scan_i32_to_u64(const int32_t* in, uint64_t* out, int64_t n, void* temp, cudaStream_t st) {
+    return scan_impl<int32_t, uint64_t>(in, out, n, static_cast<char*>(temp), st);
+}
+
+cudaError_t exclusive_scan_i64_to_u64(const int64_t* in, uint64_t* out, int64_t n, void* temp, cudaStream_t st) {
+    return scan_impl<int64_t, uint64_t>(in, out, n, static_cast<char*>(temp), st);
+}
+
 }  // namespace sig

@@ -206,6 +206,42 @@ def test_keys_and_coverage_fixture_parity(api, name):
     idx.close()
 
 
+@pytest.mark.parametrize("dt", [np.int32, np.int64])
+def test_coverage_from_ranks_extremes(api, oracle, dt):
+    """Coverage from ranks and prefix sums (no interval and no query with start > end) against
+    the oracle, with coordinates at both ends of the type (wrapped sums, qe at the maximum);
+    then the same batch with some start > end queries, which takes the hit-list path."""
+    r = np.random.default_rng(31)
+    info = np.iinfo(dt)
+    n = 20_000
+    lo_part = info.min + r.integers(0, 2_000_000, n // 2)
+    hi_part = info.max - r.integers(0, 2_000_000, n // 2)
+    starts = np.concatenate([lo_part, hi_part]).astype(np.int64)
+    lens = r.integers(0, 300_000, n)
+    ends = np.minimum(starts + lens, int(info.max)).astype(dt)
+    starts = starts.astype(dt)
+    ends[:50] = info.max                                  # reaching the maximum
+    starts, ends = np.minimum(starts, ends), ends
+    nq = 6_000
+    qs = np.concatenate([info.min + r.integers(0, 2_500_000, nq // 2),
+                         info.max - r.integers(0, 2_500_000, nq // 2)]).astype(np.int64)
+    qe = np.minimum(qs + r.integers(0, 400_000, nq), int(info.max))
+    qe[:40] = info.max
+    qs, qe = qs.astype(dt), qe.astype(dt)
+    idx = _index(api, starts, ends, None, path="batched")
+    m = oracle.build(starts, ends, np.arange(n, dtype=np.int32))
+    cnt, cov = idx.coverage(qs, qe)
+    rc, rv = oracle.coverage(m, qs, qe)
+    assert np.array_equal(cnt.astype(np.int64), rc) and np.array_equal(cov, rv)
+    flip = r.random(nq) < 0.05
+    qs2, qe2 = qs.copy(), qe.copy()
+    qs2[flip], qe2[flip] = qe[flip], qs[flip]
+    cnt, cov = idx.coverage(qs2, qe2)
+    rc, rv = oracle.coverage(m, qs2, qe2)
+    assert np.array_equal(cnt.astype(np.int64), rc) and np.array_equal(cov, rv)
+    idx.close()
+
+
 def test_keys_and_coverage_multicontig(api, oracle):
     from superintervals_gb300 import workloads as W
     wl = W.config3(n=100_000, nq=20_000, contigs=W.HUMAN_CONTIGS[20:24])
