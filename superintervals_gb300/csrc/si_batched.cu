@@ -174,6 +174,7 @@ struct TileArgs {
     const int32_t* heads_in;
     const int64_t* offsets;
     int64_t id_lo, id_hi;    // emit only the queries with ids in [id_lo, id_hi)
+    int64_t out_cap;         // values the output holds: queries whose lists end past it are skipped
     int64_t out_base;
     int order;
     bool values;
@@ -628,9 +629,11 @@ __global__ void __launch_bounds__(kThreads, 4) k_tiles(TileArgs<S> a) {
                     q_cap[i] = -1;  // outside the emitted window: skipped
                     q_h[i] = 0;
                 } else {
-                    const int64_t o = a.offsets[id];
+                    const int64_t o = a.offsets[id], o1 = a.offsets[id + 1];
                     q_off[i] = o - a.out_base;
-                    q_cap[i] = (int32_t)(a.offsets[id + 1] - o);
+                    // a list ending past the output (a replayed graph with too small a capacity,
+                    // reported by the caller) is not written
+                    q_cap[i] = (o1 - a.out_base <= a.out_cap) ? (int32_t)(o1 - o) : -1;
                     // queries counted from ranks have no head run from the count pass: the emit
                     // finds it (-1)
                     const bool counted_by_rank = a.end_sorted && !code_is_inverted(q_c[i], a.G);
@@ -1159,16 +1162,32 @@ __device__ __forceinline__ uint32_t query_code(int32_t g, int G, bool inverted, 
     return (uint32_t)g + (inverted ? 2u * (uint32_t)G : is_long ? (uint32_t)G : 0u);
 }
 
+// The packed key's layout from the batch's smallest and largest end (offset-binary): the end
+// offset loses `shift` low bits so that code and end fit 24 bits; out = {shift, end bits}.
+__global__ void k_pack_params(const unsigned long long* __restrict__ mm, int code_bits, int* __restrict__ out) {
+    if (threadIdx.x != 0) return;
+    const unsigned long long span = mm[1] - mm[0];
+    int span_bits = 0;
+    while (span_bits < 64 && (span >> span_bits) != 0) ++span_bits;
+    const int shift = max(8, span_bits + code_bits - 24);
+    out[0] = shift;
+    out[1] = max(0, span_bits - shift);
+}
+
 // One 32-bit key per query: class code above the end's offset from the batch's smallest end,
 // shifted right by `shift` (tiles need queries grouped by class and contig and close in
 // position, not exactly ordered).  Also writes (start, end) interleaved for the prepare pass.
 template <typename S>
 __global__ void k_qkeys_packed(const S* __restrict__ qs, const S* __restrict__ qe, const int32_t* __restrict__ qc,
                                int64_t nq, int64_t long_len, int G, const unsigned long long* __restrict__ mm,
-                               int shift, int ebits, uint32_t* __restrict__ key, uint32_t* __restrict__ pay,
-                               S* __restrict__ qpair) {
+                               int shift, int ebits, const int* __restrict__ d_pack, uint32_t* __restrict__ key,
+                               uint32_t* __restrict__ pay, S* __restrict__ qpair) {
     const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= nq) return;
+    if (d_pack) {  // worked out on the device
+        shift = d_pack[0];
+        ebits = d_pack[1];
+    }
     const int32_t g = qc ? qc[q] : 0;
     const S s = qs[q], e = qe[q];
     const bool is_long = ((double)e - (double)s + 1.0) > (double)long_len;
@@ -1211,6 +1230,7 @@ constexpr int kPrepWindow = 2048;  // starts staged per block by the cooperative
 template <typename S>
 __global__ void __launch_bounds__(kThreads, 6) k_qprep(const uint32_t* __restrict__ pay,
                                                     const uint32_t* __restrict__ wc, int code_shift,
+                                                    const int* __restrict__ d_pack,
                                                     const S* __restrict__ qs, const S* __restrict__ qe,
                                                     const S* __restrict__ qpair,
                                                     int64_t nq, MapView<S> m, UbView<S> U,
@@ -1225,6 +1245,7 @@ __global__ void __launch_bounds__(kThreads, 6) k_qprep(const uint32_t* __restric
     __shared__ S s_mn[kWarpsPerCta], s_mx[kWarpsPerCta], s_mq[kWarpsPerCta], s_xq[kWarpsPerCta];
     __shared__ int64_t s_a, s_b, s_ra, s_rb;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    if (d_pack) code_shift = d_pack[1];  // the packed key's end bits, worked out on the device
     const int64_t jb = (int64_t)blockIdx.x * kThreads;
     const int64_t j = jb + tid;
     const int64_t jl = (jb + kThreads < nq ? jb + kThreads : nq) - 1;  // last query of the block
@@ -1838,22 +1859,35 @@ int batched_prepare_queries(BatchedWorkspace& ws, MapView<S> m, const QueryBatch
     // one packed key word when (class code, end offset >> shift) fits 24 bits with shift <= 16
     // (three radix passes), else one word per 32 bits of end plus the class word
     SI_OKR(ws.qminmax.reserve(2 * sizeof(unsigned long long)));
-    const unsigned long long init[2] = {~0ull, 0ull};
-    SI_CU(cudaMemcpyAsync(ws.qminmax.p, init, sizeof(init), cudaMemcpyHostToDevice, st));
+    SI_CU(cudaMemsetAsync(ws.qminmax.p, 0xff, sizeof(unsigned long long), st));       // min: all ones
+    SI_CU(cudaMemsetAsync(ws.qminmax.as<unsigned long long>() + 1, 0, sizeof(unsigned long long), st));
     k_qend_minmax<S><<<(unsigned)std::min<int64_t>(nblk(nq), 152 * 8), kThreads, 0, st>>>(
         static_cast<const S*>(q.qe), nq, ws.qminmax.as<unsigned long long>());
     note_launch();
-    unsigned long long mm[2] = {0, 0};
-    SI_CU(cudaMemcpyAsync(mm, ws.qminmax.p, sizeof(mm), cudaMemcpyDeviceToHost, st));
-    SI_CU(cudaStreamSynchronize(st));
-    const unsigned long long span = mm[1] - mm[0];
-    int code_bits = 1;
-    while (code_bits < 32 && ((uint64_t)1 << code_bits) <= (uint64_t)(3 * (int64_t)m.G)) ++code_bits;
-    int span_bits = 0;
-    while (span_bits < 64 && (span >> span_bits) != 0) ++span_bits;
-    const int shift = std::max(8, span_bits + code_bits - 24);
-    const bool packed = code_bits <= 16 && shift <= 16;
-    const int ebits = packed ? std::max(0, span_bits - shift) : 0;
+    const int code_bits = query_code_bits(m.G);
+    int shift = 8, ebits = 0;
+    bool packed = true;
+    const int* d_pack = nullptr;
+    if (ws.capturing) {
+        // inside a graph capture: the packing is worked out on the device (int32 coordinates and
+        // code_bits <= 8 always pack into 24 bits with shift <= 16), and the sort runs its three
+        // low byte passes without reading its histograms back
+        if (sizeof(S) != 4 || code_bits > 8) return SI_ERR_INVALID;
+        SI_OKR(ws.qpack.reserve(2 * sizeof(int)));
+        k_pack_params<<<1, 32, 0, st>>>(ws.qminmax.as<unsigned long long>(), code_bits, ws.qpack.as<int>());
+        note_launch();
+        d_pack = ws.qpack.as<int>();
+    } else {
+        unsigned long long mm[2] = {0, 0};
+        SI_CU(cudaMemcpyAsync(mm, ws.qminmax.p, sizeof(mm), cudaMemcpyDeviceToHost, st));
+        SI_CU(cudaStreamSynchronize(st));
+        const unsigned long long span = mm[1] - mm[0];
+        int span_bits = 0;
+        while (span_bits < 64 && (span >> span_bits) != 0) ++span_bits;
+        shift = std::max(8, span_bits + code_bits - 24);
+        packed = code_bits <= 16 && shift <= 16;
+        ebits = packed ? std::max(0, span_bits - shift) : 0;
+    }
     int Kp = K;
     uint32_t* wc = kp[K - 1];
     if (packed) {
@@ -1862,8 +1896,8 @@ int batched_prepare_queries(BatchedWorkspace& ws, MapView<S> m, const QueryBatch
         SI_OKR(ws.qpair.reserve(2 * sizeof(S) * nq));
         k_qkeys_packed<S><<<nblk(nq), kThreads, 0, st>>>(static_cast<const S*>(q.qs), static_cast<const S*>(q.qe),
                                                          q.qc, nq, ws.prm.long_len, m.G,
-                                                         ws.qminmax.as<unsigned long long>(), shift, ebits, kp[0],
-                                                         ws.pay.as<uint32_t>(), ws.qpair.as<S>());
+                                                         ws.qminmax.as<unsigned long long>(), shift, ebits, d_pack,
+                                                         kp[0], ws.pay.as<uint32_t>(), ws.qpair.as<S>());
     } else {
         k_qkeys<S><<<nblk(nq), kThreads, 0, st>>>(static_cast<const S*>(q.qs), static_cast<const S*>(q.qe), q.qc,
                                                   nq, ws.prm.long_len, m.G, kp[0], K == 3 ? kp[1] : nullptr, wc,
@@ -1874,12 +1908,12 @@ int batched_prepare_queries(BatchedWorkspace& ws, MapView<S> m, const QueryBatch
     bool in_alt = false;
     int passes = 0;
     SI_CU(radix_sort(kp, ka, ws.pay.as<uint32_t>(), ws.palt.as<uint32_t>(), Kp, nq, ws.sort_tmp.p, tb, &in_alt,
-                     &passes, st));
+                     &passes, st, ws.capturing ? 0x7u : 0u));
     const uint32_t* spay = in_alt ? ws.palt.as<uint32_t>() : ws.pay.as<uint32_t>();
     const uint32_t* swc = in_alt ? ka[Kp - 1] : kp[Kp - 1];
     UbView<S> U = make_ub<S>(ws, ub_mode);
     SI_OKR(ws.blk_cut.reserve(2 * sizeof(int64_t) * (size_t)nblk(nq)));
-    k_qprep<S><<<nblk(nq), kThreads, 0, st>>>(spay, swc, packed ? ebits : 0, static_cast<const S*>(q.qs),
+    k_qprep<S><<<nblk(nq), kThreads, 0, st>>>(spay, swc, packed ? ebits : 0, d_pack, static_cast<const S*>(q.qs),
                                               static_cast<const S*>(q.qe), packed ? ws.qpair.as<S>() : nullptr,
                                               nq, m, U, ws.sq_s.as<S>(), ws.sq_u.as<int32_t>(),
                                               ws.sq_c.as<uint32_t>(), ws.sq_id.as<int32_t>(), d_err, ws.long_split,
@@ -1931,6 +1965,7 @@ static int run_tiles(BatchedWorkspace& ws, MapView<S> m, Levels<S> L, int H, int
     a.offsets = offsets;
     a.id_lo = id_lo;
     a.id_hi = id_hi;
+    a.out_cap = ws.out_cap;
     a.out_base = out_base;
     a.order = order;
     a.values = values;

@@ -88,7 +88,20 @@ struct BatchedWorkspace {
     // each contig's ends in ascending order (positions as the index), when no interval has
     // start > end: short queries are then counted from two ranks instead of the tile lists
     const void* end_sorted = nullptr;
+    // graph capture of the whole path: no host round trips (device-side key packing, fixed
+    // sort passes) and an emit that skips the queries whose lists would end past out_cap
+    bool capturing = false;
+    DBuf qpack;                  // {shift, end bits} of the packed query key
+    int64_t out_cap = INT64_MAX; // values the emit's output holds
 };
+
+// Bits of the batched path's query class codes (0 .. 3G: short, long and start > end queries
+// of each contig, and contig ids outside [0, G)).
+inline int query_code_bits(int G) {
+    int b = 1;
+    while (b < 32 && ((uint64_t)1 << b) <= (uint64_t)(3 * (int64_t)G)) ++b;
+    return b;
+}
 
 // Interval length from which an interval enters the long-interval list.
 constexpr int64_t kLongIntervalSplit = 65536;

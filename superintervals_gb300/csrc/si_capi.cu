@@ -22,6 +22,9 @@ namespace {
 
 thread_local std::string g_err;
 std::atomic<size_t> g_used{0};
+// bumped by every device allocation and release of the library: a captured graph whose
+// buffers may have moved is captured again
+std::atomic<unsigned long long> g_alloc_gen{0};
 std::atomic<size_t> g_budget{0};
 
 int fail(int code, const char* fmt, ...) {
@@ -58,6 +61,7 @@ struct DevBuf {
         if (p) {
             cudaFree(p);
             g_used -= bytes;
+            ++g_alloc_gen;
         }
         p = nullptr;
         bytes = 0;
@@ -80,6 +84,7 @@ struct DevBuf {
         }
         bytes = b;
         g_used += b;
+        ++g_alloc_gen;
         return SI_OK;
     }
     template <typename T>
@@ -107,12 +112,14 @@ int dev_reserve(void** p, size_t* bytes, size_t need) {
     }
     *bytes = need;
     g_used += need;
+    ++g_alloc_gen;
     return SI_OK;
 }
 void dev_release(void** p, size_t* bytes) {
     if (*p) {
         cudaFree(*p);
         g_used -= *bytes;
+        ++g_alloc_gen;
     }
     *p = nullptr;
     *bytes = 0;
@@ -167,7 +174,7 @@ struct gSuperIntervals {
     // captured count -> scan -> emit graph and the call it was captured for
     cudaGraphExec_t gexec = nullptr;
     const void* gkey[8] = {nullptr};
-    size_t gkey_n[3] = {0, 0, 0};
+    size_t gkey_n[5] = {0, 0, 0, 0, 0};
     long long g_kernels = 0;  // kernels inside the captured graph
     // phase profiling (count, scan, emit, prepare)
     bool prof = false;
@@ -1396,6 +1403,58 @@ int capture_plain(gSuperIntervals* si, const sig::QueryBatch& q, int order, int6
     return SI_OK;
 }
 
+// The batched path (prepare -> count -> scan -> emit) captured once per call shape: int32
+// coordinates and at most 85 contigs, so that the query key packs into 24 bits with the
+// packing worked out on the device.  One eager search first sizes every workspace buffer
+// (nothing may be allocated while the capture is open).
+template <typename S>
+int capture_batched(gSuperIntervals* si, const sig::QueryBatch& q, int order, int64_t* d_offsets, int32_t* d_values,
+                    size_t capacity, cudaStream_t st) {
+    size_t tot = 0;
+    const int r0 = search_device<S>(si, q, order, false, d_offsets, d_values, capacity, &tot, st);
+    if (r0 != SI_OK && r0 != SI_ERR_CAPACITY) return r0;
+    sig::BatchedWorkspace& ws = si->bws;
+    const int64_t nq = q.nq;
+    SI_TRY(ws.qpair.reserve(2 * sizeof(S) * nq));
+    SI_TRY(ws.kw[0].reserve(sizeof(uint32_t) * nq));
+    SI_TRY(ws.kalt[0].reserve(sizeof(uint32_t) * nq));
+    SI_TRY(ws.sort_tmp.reserve(sig::radix_temp_bytes(nq, 1)));
+    SI_TRY(ws.qpack.reserve(2 * sizeof(int)));
+    const bool prof = si->prof;
+    si->prof = false;  // the phase timers synchronize: none inside the capture
+    cudaGraph_t graph = nullptr;
+    const long long k0 = g_launches.load();
+    SI_CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    ws.capturing = true;
+    ws.out_cap = (int64_t)capacity;
+    int r = run_count<S>(si, q, si->w_counts.as<uint32_t>(), st);
+    cudaError_t e = cudaSuccess;
+    if (r == SI_OK)
+        e = sig::exclusive_scan_u32_to_i64(si->w_counts.as<uint32_t>(), d_offsets, nq, si->w_tmp.p, st);
+    if (r == SI_OK && e == cudaSuccess) r = run_emit<S>(si, q, 0, d_offsets, 0, order, false, d_values, st);
+    ws.capturing = false;
+    ws.out_cap = INT64_MAX;
+    si->prof = prof;
+    cudaError_t e2 = cudaStreamEndCapture(st, &graph);
+    si->g_kernels = g_launches.load() - k0;
+    g_launches -= si->g_kernels;  // counted when the graph runs, not when it is recorded
+    if (r != SI_OK || e != cudaSuccess || e2 != cudaSuccess) {
+        if (graph) cudaGraphDestroy(graph);
+        cudaGetLastError();
+        if (r != SI_OK) return r;
+        return fail(SI_ERR_CUDA, "graph capture failed: %s", cudaGetErrorString(e != cudaSuccess ? e : e2));
+    }
+    if (si->gexec) cudaGraphExecDestroy(si->gexec);
+    si->gexec = nullptr;
+    e = cudaGraphInstantiate(&si->gexec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) {
+        si->gexec = nullptr;
+        return fail(SI_ERR_CUDA, "cudaGraphInstantiate: %s", cudaGetErrorString(e));
+    }
+    return SI_OK;
+}
+
 }  // namespace
 
 extern "C" int searchDeviceGraphGpu(gSuperIntervals* si, const void* d_qs, const void* d_qe, const int32_t* d_qc,
@@ -1416,18 +1475,27 @@ extern "C" int searchDeviceGraphGpu(gSuperIntervals* si, const void* d_qs, const
     SI_TRY(si->w_err.reserve(sizeof(int)));
     SI_TRY(si->w_counts.reserve(sizeof(uint32_t) * nq));
     SI_TRY(si->w_tmp.reserve(sig::scan_temp_bytes((int64_t)nq)));
+    // batched when the handle would take it for this batch and the key packs on the device
+    const bool batched = use_batched(si, (int64_t)nq) && si->bits == 32 && sig::query_code_bits(si->G) <= 8 &&
+                         nq < (size_t)INT32_MAX;
     const void* key[8] = {d_qs, d_qe, d_qc, d_offsets, d_values, (const void*)st, si->w_counts.p, si->w_tmp.p};
-    const size_t key_n[3] = {nq, capacity, (size_t)order};
+    const size_t key_n[5] = {nq, capacity, (size_t)order, (size_t)batched, (size_t)g_alloc_gen.load()};
     bool same = si->gexec != nullptr;
     for (int k = 0; k < 8 && same; ++k) same = key[k] == si->gkey[k];
-    for (int k = 0; k < 3 && same; ++k) same = key_n[k] == si->gkey_n[k];
+    for (int k = 0; k < 5 && same; ++k) same = key_n[k] == si->gkey_n[k];
     if (!same) {
         sig::QueryBatch q{d_qs, d_qe, d_qc, (int64_t)nq};
-        const int r = si->bits == 64 ? capture_plain<int64_t>(si, q, order, d_offsets, d_values, capacity, st)
-                                     : capture_plain<int32_t>(si, q, order, d_offsets, d_values, capacity, st);
+        int r;
+        if (batched) r = capture_batched<int32_t>(si, q, order, d_offsets, d_values, capacity, st);
+        else if (si->bits == 64) r = capture_plain<int64_t>(si, q, order, d_offsets, d_values, capacity, st);
+        else r = capture_plain<int32_t>(si, q, order, d_offsets, d_values, capacity, st);
         if (r != SI_OK) return r;
+        // every buffer the graph uses is sized now: key it on the allocations as they stand
+        si->gkey_n[4] = (size_t)g_alloc_gen.load();
         for (int k = 0; k < 8; ++k) si->gkey[k] = key[k];
-        for (int k = 0; k < 3; ++k) si->gkey_n[k] = key_n[k];
+        for (int k = 0; k < 4; ++k) si->gkey_n[k] = key_n[k];
+        si->gkey[6] = si->w_counts.p;
+        si->gkey[7] = si->w_tmp.p;
     }
     SI_CK(cudaGraphLaunch(si->gexec, st));
     int64_t P = 0;

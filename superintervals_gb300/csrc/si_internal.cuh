@@ -105,12 +105,14 @@ cudaError_t launch_contig_names(const uint32_t* first_rec, const int64_t* r_noff
 // significant) with one 32-bit payload.  keys[w] / payload are double
 // buffered with alt_keys[w] / alt_payload; the sorted result is left in the
 // buffers reported through *result_in_alt.  Passes whose digit is constant
-// over all records are skipped.
+// over all records are skipped (the digit histograms are read back to the host).  With a
+// nonzero pass_mask exactly the passes of its bits run (bit 4w + b: byte b of word w), with
+// no host round trip, so that the sort can be captured in a CUDA graph.
 constexpr int kMaxKeyWords = 5;
 size_t radix_temp_bytes(int64_t n, int K);
 cudaError_t radix_sort(uint32_t* const* keys, uint32_t* const* alt_keys, uint32_t* payload,
                        uint32_t* alt_payload, int K, int64_t n, void* temp, size_t temp_bytes,
-                       bool* result_in_alt, int* passes_run, cudaStream_t st);
+                       bool* result_in_alt, int* passes_run, cudaStream_t st, uint32_t pass_mask = 0);
 
 // ---------------------------------------------------------------- build
 template <typename S>

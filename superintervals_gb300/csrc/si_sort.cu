@@ -170,7 +170,7 @@ size_t radix_temp_bytes(int64_t n, int K) {
 
 cudaError_t radix_sort(uint32_t* const* keys, uint32_t* const* alt_keys, uint32_t* payload,
                        uint32_t* alt_payload, int K, int64_t n, void* temp, size_t temp_bytes,
-                       bool* result_in_alt, int* passes_run, cudaStream_t st) {
+                       bool* result_in_alt, int* passes_run, cudaStream_t st, uint32_t pass_mask) {
     *result_in_alt = false;
     if (passes_run) *passes_run = 0;
     if (n <= 1) return cudaSuccess;
@@ -187,18 +187,21 @@ cudaError_t radix_sort(uint32_t* const* keys, uint32_t* const* alt_keys, uint32_
     p += sizeof(uint32_t) * round_up(kRadix * tiles + 1, 64);
     void* scan_tmp = p;
 
-    cudaError_t e = cudaMemsetAsync(ghist, 0, sizeof(uint32_t) * K * 4 * kRadix, st);
-    if (e != cudaSuccess) return e;
-    KeyPtrs kp{};
-    for (int w = 0; w < K; ++w) kp.w[w] = keys[w];
-    int gblocks = (int)std::min<int64_t>(ceil_div(n, kThreads), 152 * 8);
-    k_global_hist<<<gblocks, kThreads, 0, st>>>(kp, K, n, ghist);
-    note_launch();
-    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    cudaError_t e = cudaSuccess;
     uint32_t hh[kMaxKeyWords * 4 * kRadix];
-    e = cudaMemcpyAsync(hh, ghist, sizeof(uint32_t) * K * 4 * kRadix, cudaMemcpyDeviceToHost, st);
-    if (e != cudaSuccess) return e;
-    if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return e;
+    if (!pass_mask) {
+        e = cudaMemsetAsync(ghist, 0, sizeof(uint32_t) * K * 4 * kRadix, st);
+        if (e != cudaSuccess) return e;
+        KeyPtrs kp{};
+        for (int w = 0; w < K; ++w) kp.w[w] = keys[w];
+        int gblocks = (int)std::min<int64_t>(ceil_div(n, kThreads), 152 * 8);
+        k_global_hist<<<gblocks, kThreads, 0, st>>>(kp, K, n, ghist);
+        note_launch();
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        e = cudaMemcpyAsync(hh, ghist, sizeof(uint32_t) * K * 4 * kRadix, cudaMemcpyDeviceToHost, st);
+        if (e != cudaSuccess) return e;
+        if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return e;
+    }
 
     uint32_t* cur_k[kMaxKeyWords];
     uint32_t* oth_k[kMaxKeyWords];
@@ -212,11 +215,15 @@ cudaError_t radix_sort(uint32_t* const* keys, uint32_t* const* alt_keys, uint32_
     int passes = 0;
     for (int w = 0; w < K; ++w) {
         for (int b = 0; b < 4; ++b) {
-            const uint32_t* hb = hh + (w * 4 + b) * kRadix;
-            bool constant = false;
-            for (int d = 0; d < kRadix; ++d)
-                if (hb[d] == (uint32_t)n) constant = true;
-            if (constant) continue;
+            if (pass_mask) {
+                if (!((pass_mask >> (w * 4 + b)) & 1u)) continue;
+            } else {
+                const uint32_t* hb = hh + (w * 4 + b) * kRadix;
+                bool constant = false;
+                for (int d = 0; d < kRadix; ++d)
+                    if (hb[d] == (uint32_t)n) constant = true;
+                if (constant) continue;
+            }
             k_pass_hist<<<(unsigned)tiles, kThreads, 0, st>>>(cur_k[w], 8 * b, n, H, tiles);
             note_launch();
             if ((e = cudaGetLastError()) != cudaSuccess) return e;

@@ -430,24 +430,45 @@ def test_autotuner_keeps_results_exact(api, oracle):
     idx.close()
 
 
-def test_graph_replay_matches_and_respects_capacity(api):
+@pytest.mark.parametrize("path,inverted", [("plain", False), ("batched", False), ("batched", True)])
+def test_graph_replay_matches_and_respects_capacity(api, path, inverted):
+    """searchDeviceGraphGpu: the plain path, or the whole batched path (prepare, count, scan,
+    emit) captured once and replayed, also on new query contents in the same buffers."""
     import ctypes as C
     from superintervals_gb300 import workloads as W
     wl = W.config3(n=200_000, nq=30_000)
-    idx = _index(api, wl.starts, wl.ends, wl.data, seg=wl.seg, path="plain")
+    if inverted:        # intervals with start > end: the batched path counts from its tile lists
+        inv = np.random.default_rng(4).random(wl.n) < 0.003
+        wl.starts[inv], wl.ends[inv] = wl.ends[inv].copy(), wl.starts[inv].copy()
+    idx = _index(api, wl.starts, wl.ends, wl.data, seg=wl.seg, path=path)
     d = _Dev(api, idx, wl)
     off_ref, out_ref = idx.search(wl.q_starts, wl.q_ends, wl.q_contig)
     P = int(off_ref[-1])
-    d_out = d.alloc(4 * P)
+    # a second batch of the same shape (the same queries permuted), answered eagerly first
+    perm = np.random.default_rng(8).permutation(d.nq)
+    qs2, qe2 = wl.q_starts[perm], wl.q_ends[perm]
+    qc2 = None if wl.q_contig is None else wl.q_contig[perm]
+    off2, out2 = idx.search(qs2, qe2, qc2)
+    d_out = d.alloc(4 * P + 4096)
     tot = C.c_size_t()
     launches0 = idx.lib.getLaunchCountGpu()
     for _ in range(3):   # first call captures, the others replay
-        api.check(idx.lib.searchDeviceGraphGpu(idx.h, d.qs, d.qe, d.qc, d.nq, 0, d.off, d_out, P, C.byref(tot),
-                                               None))
+        api.check(idx.lib.searchDeviceGraphGpu(idx.h, d.qs, d.qe, d.qc, d.nq, 0, d.off, d_out, P + 1024,
+                                               C.byref(tot), None))
         assert int(tot.value) == P
         assert np.array_equal(d.get(d.off, d.nq + 1, np.int64), off_ref)
         assert np.array_equal(d.get(d_out, P, np.int32), out_ref)
     assert idx.lib.getLaunchCountGpu() > launches0
+    # new queries in the same buffers: a replay, not a new capture
+    if int(off2[-1]) <= P + 1024:
+        for arr, ptr in ((qs2, d.qs), (qe2, d.qe), (qc2, d.qc)):
+            if arr is not None:
+                a = np.ascontiguousarray(arr)
+                api.check(idx.lib.memcpyGpu(ptr, C.c_void_p(a.ctypes.data), a.nbytes, idx.stream))
+        api.check(idx.lib.searchDeviceGraphGpu(idx.h, d.qs, d.qe, d.qc, d.nq, 0, d.off, d_out, P + 1024,
+                                               C.byref(tot), None))
+        assert np.array_equal(d.get(d.off, d.nq + 1, np.int64), off2)
+        assert np.array_equal(d.get(d_out, int(off2[-1]), np.int32), out2)
     # too small an output: reported, nothing written past the end
     small = P // 2
     guard = d.alloc(4 * (small + 1024))
