@@ -155,7 +155,9 @@ int setUpperBoundModeGpu(gSuperIntervals* si, int mode);
  * per-query walk, and the interval length from which a tile's candidate goes
  * to its "long" list (scanned for every query) instead of being scanned only
  * near each query.  0 keeps the current value (split_len: -1 keeps it, 0 is a
- * valid length).  Results do not depend on these values. */
+ * valid length).  tile_queries -1 (the default) picks the tile size per batch
+ * from its intervals and hits per query; a positive value fixes it.  Results
+ * do not depend on these values. */
 int setBatchedParamsGpu(gSuperIntervals* si, int tile_queries, int tile_candidates,
                         int64_t long_query_len, int64_t split_len);
 int getBatchedParamsGpu(const gSuperIntervals* si, int* tile_queries, int* tile_candidates,

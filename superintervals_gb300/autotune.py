@@ -39,7 +39,9 @@ def cache_key(index, nq: int) -> str:
 
 def apply(index, choice: dict):
     lib = index.lib
-    _capi.check(lib.setBatchedParamsGpu(index.h, int(choice["tile_queries"]), int(choice["tile_candidates"]),
+    # a choice that kept the automatic tile size (per batch) restores it (-1)
+    tile = -1 if int(choice.get("tile_auto", 0)) else int(choice["tile_queries"])
+    _capi.check(lib.setBatchedParamsGpu(index.h, tile, int(choice["tile_candidates"]),
                                         int(choice["long_query_len"]), int(choice["split_len"])))
     index.set_upper_bound(int(choice["upper_bound"]))
 

@@ -1932,7 +1932,9 @@ template <typename S>
 static int run_tiles(BatchedWorkspace& ws, MapView<S> m, Levels<S> L, int H, int64_t nq, bool emit,
                      uint32_t* counts, int32_t* heads, const int32_t* heads_in, const int64_t* offsets,
                      int64_t out_base, int order, bool values, int32_t* out, int* d_err, bool use_cache,
-                     cudaStream_t st, int64_t id_lo = 0, int64_t id_hi = INT64_MAX) {
+                     cudaStream_t st, int64_t id_lo = 0, int64_t id_hi = INT64_MAX, int tile_q = 0) {
+    BatchedParams prm = ws.prm;
+    if (tile_q) prm.tile_q = tile_q;
     SI_OKR(ws.counters.reserve(sizeof(int) * 4));
     SI_CU(cudaMemsetAsync(ws.counters.p, 0, sizeof(int) * 4, st));
     TileArgs<S> a;
@@ -1942,11 +1944,11 @@ static int run_tiles(BatchedWorkspace& ws, MapView<S> m, Levels<S> L, int H, int
     a.PL.H = ws.long_H;
     a.long_pos = ws.long_pos;
     a.long_seg = ws.long_seg;
-    a.blk_cut = (ws.prm.tile_q == kThreads && ws.blk_cut.p) ? ws.blk_cut.as<int64_t>() : nullptr;
+    a.blk_cut = (prm.tile_q == kThreads && ws.blk_cut.p) ? ws.blk_cut.as<int64_t>() : nullptr;
     a.long_split = ws.long_split;
     a.end_sorted = static_cast<const S*>(ws.end_sorted);
     a.starts = m.starts;
-    a.split_len = ws.prm.split_len;
+    a.split_len = prm.split_len;
     a.data = m.data;
     a.seg = m.seg;
     a.G = m.G;
@@ -1955,8 +1957,8 @@ static int run_tiles(BatchedWorkspace& ws, MapView<S> m, Levels<S> L, int H, int
     a.sq_c = ws.sq_c.as<uint32_t>();
     a.sq_id = ws.sq_id.as<int32_t>();
     a.nq = nq;
-    a.tile_q = ws.prm.tile_q;
-    a.cap = ws.prm.cap;
+    a.tile_q = prm.tile_q;
+    a.cap = prm.cap;
     a.n_tiles = (int)ceil_div(nq, a.tile_q);
     a.tile_counter = ws.counters.as<int>();
     a.counts = counts;
@@ -1973,7 +1975,7 @@ static int run_tiles(BatchedWorkspace& ws, MapView<S> m, Levels<S> L, int H, int
     a.d_err = d_err;
     a.cache = (use_cache && ws.cache_ok) ? ws.tile_cache.as<unsigned char>() : nullptr;
     a.cache_stride = ws.cache_stride;
-    const size_t sm = tile_smem(ws.prm, sizeof(S));
+    const size_t sm = tile_smem(prm, sizeof(S));
     // the kernel attribute and the occupancy are set / asked once per shared-memory size
     const int e = emit ? 1 : 0;
     if (ws.occ_smem[e] != sm) {
@@ -2027,7 +2029,7 @@ int batched_count(BatchedWorkspace& ws, MapView<S> m, Levels<S> L, int H, const 
 template <typename S>
 int batched_emit(BatchedWorkspace& ws, MapView<S> m, Levels<S> L, int H, const QueryBatch& q, int64_t q_offset,
                  const int64_t* offsets, int64_t out_base, int order, bool values, int32_t* out, int* d_err,
-                 int ub_mode, cudaStream_t st) {
+                 int ub_mode, cudaStream_t st, int64_t total_hits) {
     const int64_t nq = q.nq;
     if (nq <= 0) return SI_OK;
     if (q_offset < 0 || q_offset + nq > ws.n_heads) return SI_ERR_INVALID;
@@ -2038,14 +2040,25 @@ int batched_emit(BatchedWorkspace& ws, MapView<S> m, Levels<S> L, int H, const Q
     const bool window = !same && ws.prepared_qs != nullptr && ws.prepared_nq >= q_offset + nq &&
                         static_cast<const S*>(q.qs) - q_offset == static_cast<const S*>(ws.prepared_qs);
     const bool cache_fits = ws.cache_ok && ws.cache_prm_tile == ws.prm.tile_q && ws.cache_prm_cap == ws.prm.cap;
+    // Without a count-pass cache (the rank counts), the tile size is free: the largest of 256,
+    // 128, 64, 32 queries whose expected candidates, tile_q * (intervals per query) + hits per
+    // query, fill at most 3/4 of the candidate slots.  Tiles that overflow fall back to
+    // per-query walks, which costs up to 25x at sparse batches.
+    const int64_t batch_nq = (same || window) ? ws.prepared_nq : nq;
+    int tile = 0;
+    if (ws.prm.auto_tile && ws.end_sorted && total_hits >= 0 && batch_nq > 0) {
+        const double per_q = (double)m.n / (double)batch_nq, hpq = (double)total_hits / (double)batch_nq;
+        tile = kThreads;
+        while (tile > 32 && tile * per_q + hpq > 0.75 * ws.prm.cap) tile >>= 1;
+    }
     if (window)
         return run_tiles<S>(ws, m, L, H, ws.prepared_nq, true, nullptr, nullptr, ws.heads.as<int32_t>(),
-                            offsets - q_offset, out_base, order, values, out, d_err, cache_fits, st, q_offset,
-                            q_offset + nq);
+                            offsets - q_offset, out_base, order, values, out, d_err, cache_fits && !tile, st,
+                            q_offset, q_offset + nq, tile);
     if (!same) SI_OKR(batched_prepare_queries<S>(ws, m, q, d_err, ub_mode, st));
     // sorted ids are relative to q; heads / offsets are shifted to the slice
     return run_tiles<S>(ws, m, L, H, nq, true, nullptr, nullptr, ws.heads.as<int32_t>() + q_offset, offsets,
-                        out_base, order, values, out, d_err, same && cache_fits, st);
+                        out_base, order, values, out, d_err, same && cache_fits && !tile, st, 0, INT64_MAX, tile);
 }
 
 template <typename S>
@@ -2087,7 +2100,8 @@ int batched_coverage(BatchedWorkspace& ws, MapView<S> m, const QueryBatch& q, co
     template int batched_count<S>(BatchedWorkspace&, MapView<S>, Levels<S>, int, const QueryBatch&, uint32_t*,   \
                                   int*, cudaStream_t);                                                          \
     template int batched_emit<S>(BatchedWorkspace&, MapView<S>, Levels<S>, int, const QueryBatch&, int64_t,      \
-                                 const int64_t*, int64_t, int, bool, int32_t*, int*, int, cudaStream_t);        \
+                                 const int64_t*, int64_t, int, bool, int32_t*, int*, int, cudaStream_t,         \
+                                 int64_t);                                                                      \
     template int upper_bounds<S>(BatchedWorkspace&, MapView<S>, const QueryBatch&, int, int32_t*, int*,          \
                                  cudaStream_t);                                                                 \
     template int batched_coverage<S>(BatchedWorkspace&, MapView<S>, const QueryBatch&, const uint64_t*,         \

@@ -29,6 +29,9 @@ struct BatchedParams {
     int64_t long_len = 16384;    // queries longer than this take the per-query walk
     int64_t split_len = 2048;    // candidates at least this long form the tile's long list
     int eytz_depth = 0;          // 0: automatic
+    // pick tile_q per batch (emit without a count-pass cache) from the batch's intervals per
+    // query and hits per query, so that a tile's candidates fit its shared memory
+    bool auto_tile = true;
 };
 
 // Per-contig upper-bound accelerators built once per index.
@@ -119,10 +122,11 @@ template <typename S>
 int batched_count(BatchedWorkspace& ws, MapView<S> m, Levels<S> L, int H, const QueryBatch& q,
                   uint32_t* counts, int* d_err, cudaStream_t st);
 // q may be a slice [q_offset, q_offset + q.nq) of the batch counted last.
+// total_hits: the result count of the whole batch prepared last (-1 unknown), for the tile size.
 template <typename S>
 int batched_emit(BatchedWorkspace& ws, MapView<S> m, Levels<S> L, int H, const QueryBatch& q,
                  int64_t q_offset, const int64_t* offsets, int64_t out_base, int order, bool values,
-                 int32_t* out, int* d_err, int ub_mode, cudaStream_t st);
+                 int32_t* out, int* d_err, int ub_mode, cudaStream_t st, int64_t total_hits = -1);
 
 // Coverage (count and the wrapped sum of min(end, qe) - max(start, qs)) of every query, from
 // ranks and prefix sums (ps_start / ps_end: exclusive prefix sums mod 2^64 of the starts and of

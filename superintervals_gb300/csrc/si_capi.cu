@@ -496,14 +496,15 @@ int run_count(gSuperIntervals* si, const sig::QueryBatch& q, uint32_t* d_counts,
 }
 
 // q may be a slice starting at query q_offset of the batch counted last.
+// total_hits: the result count of the whole batch counted last (-1 unknown; sizes the tiles)
 template <typename S>
 int run_emit(gSuperIntervals* si, const sig::QueryBatch& q, int64_t q_offset, const int64_t* d_offsets,
-             int64_t out_base, int order, bool values, int32_t* d_out, cudaStream_t st) {
+             int64_t out_base, int order, bool values, int32_t* d_out, cudaStream_t st, int64_t total_hits) {
     if (si->n == 0 || q.nq == 0) return SI_OK;
     PhaseTimer pt(si, 2, st);
     if (use_batched(si, q.nq + q_offset)) {
         int r = sig::batched_emit<S>(si->bws, view<S>(si), levels<S>(si), si->H, q, q_offset, d_offsets, out_base,
-                                     order, values, d_out, si->w_err.as<int>(), si->ub_mode, st);
+                                     order, values, d_out, si->w_err.as<int>(), si->ub_mode, st, total_hits);
         if (r != SI_OK) return fail(r, "batched emit failed (status %d)", r);
     } else {
         SI_CK(sig::launch_emit_plain<S>(view<S>(si), q, d_offsets, out_base, order, values, d_out,
@@ -530,7 +531,7 @@ int search_device(gSuperIntervals* si, const sig::QueryBatch& q, int order, bool
     SI_CK(cudaStreamSynchronize(st));
     if (total) *total = (size_t)P;
     if ((size_t)P > cap) return fail(SI_ERR_CAPACITY, "output needs %lld values, capacity %zu", (long long)P, cap);
-    SI_TRY(run_emit<S>(si, q, 0, d_offsets, 0, order, values, d_out, st));
+    SI_TRY(run_emit<S>(si, q, 0, d_offsets, 0, order, values, d_out, st, P));
     return read_dev_err(si, st);
 }
 
@@ -648,7 +649,7 @@ int search_host(gSuperIntervals* si, const S* qs, const S* qe, const int32_t* qc
         sub.qe = static_cast<const S*>(q.qe) + qa;
         sub.qc = q.qc ? q.qc + qa : nullptr;
         sub.nq = (int64_t)(qb - qa);
-        SI_TRY(run_emit<S>(si, sub, (int64_t)qa, d_off + qa, h_off[qa], order, values, dbuf, st));
+        SI_TRY(run_emit<S>(si, sub, (int64_t)qa, d_off + qa, h_off[qa], order, values, dbuf, st, P));
         if (n_chunks == 1) {
             if (need)
                 SI_CK(cudaMemcpyAsync(h_out + h_off[qa], dbuf, sizeof(int32_t) * need, cudaMemcpyDeviceToHost, st));
@@ -1104,7 +1105,12 @@ extern "C" int upperBoundDeviceGpu(gSuperIntervals* si, const void* d_qe, const 
 extern "C" int setBatchedParamsGpu(gSuperIntervals* si, int tile_q, int cap, int64_t long_len, int64_t split_len) {
     if (!si) return fail(SI_ERR_INVALID, "null handle");
     sig::BatchedParams p = si->bws.prm;
-    if (tile_q) p.tile_q = tile_q;
+    if (tile_q > 0) {
+        p.tile_q = tile_q;
+        p.auto_tile = false;
+    } else if (tile_q < 0) {
+        p.auto_tile = true;
+    }
     if (cap) p.cap = cap;
     if (long_len) p.long_len = long_len;
     if (split_len >= 0) p.split_len = split_len;
@@ -1331,9 +1337,10 @@ extern "C" int autotuneBatchedGpu(gSuperIntervals* si, const void* d_qs, const v
         for (int ub : {SI_UB_BINARY, SI_UB_EYTZINGER, SI_UB_LEARNED})
             if (ub != best_ub) try_params(best, ub);
     for (int t : {128, 256, 384, 512})
-        if (t != best.tile_q) {
+        if (t != best.tile_q || best.auto_tile) {
             sig::BatchedParams p = best;
             p.tile_q = t;
+            p.auto_tile = false;
             try_params(p, best_ub);
         }
     for (int c : {1024, 2048, 3072})
@@ -1353,10 +1360,11 @@ extern "C" int autotuneBatchedGpu(gSuperIntervals* si, const void* d_qs, const v
     si->path = saved_path;
     if (report && report_len) {
         snprintf(report, report_len,
-                 "{\"upper_bound\": %d, \"tile_queries\": %d, \"tile_candidates\": %d, \"split_len\": %lld, "
-                 "\"long_query_len\": %lld, \"sample_queries\": %zu, \"sample_ms\": %.4f, \"trials\": %d}",
-                 best_ub, best.tile_q, best.cap, (long long)best.split_len, (long long)best.long_len, ns, best_ms,
-                 trials);
+                 "{\"upper_bound\": %d, \"tile_queries\": %d, \"tile_auto\": %d, \"tile_candidates\": %d, "
+                 "\"split_len\": %lld, \"long_query_len\": %lld, \"sample_queries\": %zu, \"sample_ms\": %.4f, "
+                 "\"trials\": %d}",
+                 best_ub, best.tile_q, best.auto_tile ? 1 : 0, best.cap, (long long)best.split_len,
+                 (long long)best.long_len, ns, best_ms, trials);
     }
     return SI_OK;
 }
@@ -1431,7 +1439,8 @@ int capture_batched(gSuperIntervals* si, const sig::QueryBatch& q, int order, in
     cudaError_t e = cudaSuccess;
     if (r == SI_OK)
         e = sig::exclusive_scan_u32_to_i64(si->w_counts.as<uint32_t>(), d_offsets, nq, si->w_tmp.p, st);
-    if (r == SI_OK && e == cudaSuccess) r = run_emit<S>(si, q, 0, d_offsets, 0, order, false, d_values, st);
+    if (r == SI_OK && e == cudaSuccess)
+        r = run_emit<S>(si, q, 0, d_offsets, 0, order, false, d_values, st, (int64_t)tot);
     ws.capturing = false;
     ws.out_cap = INT64_MAX;
     si->prof = prof;
@@ -1531,7 +1540,7 @@ int hit_lists(gSuperIntervals* si, const sig::QueryBatch& q, int order, cudaStre
     SI_CK(cudaMemcpyAsync(&P, si->so_hoff.as<int64_t>() + q.nq, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
     SI_CK(cudaStreamSynchronize(st));
     SI_TRY(si->so_hits.reserve(sizeof(int32_t) * std::max<int64_t>(P, 1)));
-    SI_TRY(run_emit<S>(si, q, 0, si->so_hoff.as<int64_t>(), 0, order, false, si->so_hits.as<int32_t>(), st));
+    SI_TRY(run_emit<S>(si, q, 0, si->so_hoff.as<int64_t>(), 0, order, false, si->so_hits.as<int32_t>(), st, P));
     return read_dev_err(si, st);
 }
 

@@ -236,6 +236,26 @@ def test_upper_bound_providers_exact(api, mode):
         idx.close()
 
 
+@pytest.mark.parametrize("nq", [3_000, 40_000, 400_000])
+def test_automatic_tile_size_is_exact(api, oracle, nq):
+    """The per-batch tile size (from intervals and hits per query) against a fixed one and
+    the oracle, from sparse batches (small tiles, walks) to dense ones."""
+    from superintervals_gb300 import workloads as W
+    wl = W.config3(n=2_000_000, nq=nq)
+    idx = _index(api, wl.starts, wl.ends, wl.data, seg=wl.seg, path="batched")
+    off, out = idx.search(wl.q_starts, wl.q_ends, wl.q_contig)
+    api.check(idx.lib.setBatchedParamsGpu(idx.h, 256, 0, 0, -1))
+    off2, out2 = idx.search(wl.q_starts, wl.q_ends, wl.q_contig)
+    assert np.array_equal(off, off2) and np.array_equal(out, out2)
+    api.check(idx.lib.setBatchedParamsGpu(idx.h, -1, 0, 0, -1))
+    m = oracle.build(wl.starts, wl.ends, wl.data, seg=wl.seg)
+    sel = np.arange(0, nq, max(1, nq // 2000))
+    ro, rv = oracle.search_batch(m, wl.q_starts[sel], wl.q_ends[sel], wl.q_contig[sel], order=0, nthreads=8)
+    got = [out[off[q]:off[q + 1]].tolist() for q in sel]
+    assert got == [rv[ro[i]:ro[i + 1]].tolist() for i in range(len(sel))]
+    idx.close()
+
+
 @pytest.mark.parametrize("tile_q,cap,long_len,split", [(32, 256, 1 << 40, 2048), (64, 256, 50, 0),
                                                        (1024, 8192, 1 << 14, 1), (128, 512, 2000, 1 << 40),
                                                        (256, 2048, 1 << 14, 300)])
