@@ -35,6 +35,21 @@ def test_reference_arm_line(cfg):
     assert "cores" in line["cpu_baseline"] and "sample" in line["cpu_baseline"]
 
 
+def test_contig_subset_workload_keeps_density():
+    """--contigs: configuration 3 on a subset of contigs with its share of intervals and
+    queries (the same intervals and hits per query as the full configuration)."""
+    import bench
+    from superintervals_gb300 import workloads as W
+    full = sum(c[1] for c in W.HUMAN_CONTIGS)
+    sub = [c for c in W.HUMAN_CONTIGS if c[0] in ("chr21", "chr22")]
+    wl = bench.make_workload("config3", 0.01, 0, "chr21,chr22")
+    assert len(wl.seg) - 1 == 2
+    share = sum(c[1] for c in sub) / full
+    assert wl.n == int(50_000_000 * 0.01 * share) and wl.nq == int(50_000_000 * 0.01 * share)
+    with pytest.raises(SystemExit):
+        bench.make_workload("config3", 0.01, 0, "chr21,chrZ")
+
+
 def test_reference_arm_two_ranks_prints_once():
     """Under torchrun only rank 0 runs the host baseline and prints; rank 1 exits 0."""
     out = subprocess.run(
