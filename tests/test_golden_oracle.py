@@ -151,3 +151,48 @@ def test_oracle_setops_match_reference(oracle, name):
         _, os_, oe_, _ = oracle.intersection(m, a_s, a_e, ORDER_DESC)
         assert np.array_equal(os_, g["ref_c_isect_starts"]) and np.array_equal(oe_, g["ref_c_isect_ends"])
         assert np.array_equal(g["ref_c_diff_starts"], g["ref_diff_starts"])
+
+
+@pytest.mark.parametrize("dt", [np.int32, np.int64])
+def test_coverage_rank_identity(oracle, dt):
+    """The identity behind the GPU's coverage from ranks (no interval and no query with
+    start > end): over the hits {start <= qe} minus {end < qs},
+      count = a_u - r_qs,
+      sum min(end, qe) = PE[r_qe] - PE[r_qs] + qe (a_u - r_qe),
+      sum max(start, qs) = PS[a_u] - PS[ls] + qs (ls - r_qs),
+    with prefix sums mod 2^64 truncated to the coordinate width, equals the reference's
+    per-hit wrapped sum (hpp:979-1006), coordinate extremes included."""
+    r = np.random.default_rng(17)
+    info = np.iinfo(dt)
+    n = 3000
+    s = np.concatenate([info.min + r.integers(0, 200_000, n // 2), info.max - r.integers(0, 200_000, n // 2)])
+    ln = r.integers(0, 40_000, n)
+    e = np.where(s > info.max - ln, info.max, s + ln)    # no overflow at the top of the type
+    e[:20] = info.max
+    m = oracle.build(s.astype(dt), e.astype(dt), np.arange(n, dtype=np.int32))
+    st, en = m["starts"].astype(np.int64), m["ends"].astype(np.int64)
+    q0 = np.concatenate([info.min + r.integers(0, 250_000, 300), info.max - r.integers(0, 250_000, 300)])
+    qln = r.integers(0, 60_000, 600)
+    q1 = np.where(q0 > info.max - qln, info.max, q0 + qln)
+    q1[:10] = info.max
+    qs, qe = q0.astype(dt), q1.astype(dt)
+    assert (st <= en).all() and (qs <= qe).all()
+    rc, rv = oracle.coverage(m, qs, qe)
+    es = np.sort(en)
+    u64 = lambda a: a.astype(np.int64).view(np.uint64)  # noqa: E731  (two's complement, mod 2^64)
+    zero = np.zeros(1, np.uint64)
+    ps = np.concatenate([zero, np.cumsum(u64(st), dtype=np.uint64)])
+    pe = np.concatenate([zero, np.cumsum(u64(es), dtype=np.uint64)])
+    a_u = np.searchsorted(st, qe.astype(np.int64), side="right")
+    r_qs = np.searchsorted(es, qs.astype(np.int64), side="left")
+    r_qe = np.searchsorted(es, qe.astype(np.int64), side="right")
+    ls = np.searchsorted(st, qs.astype(np.int64), side="left")
+    with np.errstate(over="ignore"):
+        smin = pe[r_qe] - pe[r_qs] + u64(qe) * (a_u - r_qe).astype(np.uint64)
+        smax = ps[a_u] - ps[ls] + u64(qs) * (ls - r_qs).astype(np.uint64)
+        cov = (smin - smax).astype(np.uint64)
+    bits = np.dtype(dt).itemsize * 8
+    cov = (cov & np.uint64((1 << bits) - 1)) if bits < 64 else cov
+    got = cov.astype(np.uint64).view(np.int64) if bits == 64 else cov.astype(np.uint32).view(np.int32)
+    assert np.array_equal(a_u - r_qs, rc)
+    assert np.array_equal(got.astype(dt), rv)

@@ -218,16 +218,18 @@ def test_coverage_from_ranks_extremes(api, oracle, dt):
     hi_part = info.max - r.integers(0, 2_000_000, n // 2)
     starts = np.concatenate([lo_part, hi_part]).astype(np.int64)
     lens = r.integers(0, 300_000, n)
-    ends = np.minimum(starts + lens, int(info.max)).astype(dt)
+    ends = np.where(starts > info.max - lens, info.max, starts + lens).astype(dt)   # no overflow
     starts = starts.astype(dt)
     ends[:50] = info.max                                  # reaching the maximum
-    starts, ends = np.minimum(starts, ends), ends
+    assert (starts <= ends).all()
     nq = 6_000
     qs = np.concatenate([info.min + r.integers(0, 2_500_000, nq // 2),
                          info.max - r.integers(0, 2_500_000, nq // 2)]).astype(np.int64)
-    qe = np.minimum(qs + r.integers(0, 400_000, nq), int(info.max))
+    qln = r.integers(0, 400_000, nq)
+    qe = np.where(qs > info.max - qln, info.max, qs + qln)
     qe[:40] = info.max
     qs, qe = qs.astype(dt), qe.astype(dt)
+    assert (qs <= qe).all()
     idx = _index(api, starts, ends, None, path="batched")
     m = oracle.build(starts, ends, np.arange(n, dtype=np.int32))
     cnt, cov = idx.coverage(qs, qe)
