@@ -1872,11 +1872,15 @@ int batched_prepare_queries(BatchedWorkspace& ws, MapView<S> m, const QueryBatch
         // inside a graph capture: the packing is worked out on the device (int32 coordinates and
         // code_bits <= 8 always pack into 24 bits with shift <= 16), and the sort runs its three
         // low byte passes without reading its histograms back
-        if (sizeof(S) != 4 || code_bits > 8) return SI_ERR_INVALID;
-        SI_OKR(ws.qpack.reserve(2 * sizeof(int)));
-        k_pack_params<<<1, 32, 0, st>>>(ws.qminmax.as<unsigned long long>(), code_bits, ws.qpack.as<int>());
-        note_launch();
-        d_pack = ws.qpack.as<int>();
+        if constexpr (sizeof(S) != 4) {
+            return SI_ERR_INVALID;
+        } else {
+            if (code_bits > 8) return SI_ERR_INVALID;
+            SI_OKR(ws.qpack.reserve(2 * sizeof(int)));
+            k_pack_params<<<1, 32, 0, st>>>(ws.qminmax.as<unsigned long long>(), code_bits, ws.qpack.as<int>());
+            note_launch();
+            d_pack = ws.qpack.as<int>();
+        }
     } else {
         unsigned long long mm[2] = {0, 0};
         SI_CU(cudaMemcpyAsync(mm, ws.qminmax.p, sizeof(mm), cudaMemcpyDeviceToHost, st));
