@@ -637,7 +637,7 @@ int search_host(gSuperIntervals* si, const S* qs, const S* qe, const int32_t* qc
             if (!si->ev_copied[b]) SI_CK(cudaEventCreateWithFlags(&si->ev_copied[b], cudaEventDisableTiming));
         }
     }
-    for (size_t c = 0; c < n_chunks; ++c) {
+    auto chunk = [&](size_t c) -> int {
         const size_t qa = cuts[c], qb = cuts[c + 1];
         const int64_t need = h_off[qb] - h_off[qa];
         const int b = (int)(c & 1);
@@ -653,7 +653,7 @@ int search_host(gSuperIntervals* si, const S* qs, const S* qe, const int32_t* qc
         if (n_chunks == 1) {
             if (need)
                 SI_CK(cudaMemcpyAsync(h_out + h_off[qa], dbuf, sizeof(int32_t) * need, cudaMemcpyDeviceToHost, st));
-            continue;
+            return SI_OK;
         }
         SI_CK(cudaEventRecord(si->ev_emitted[b], st));
         SI_CK(cudaStreamWaitEvent(si->copy_st, si->ev_emitted[b], 0));
@@ -661,6 +661,16 @@ int search_host(gSuperIntervals* si, const S* qs, const S* qe, const int32_t* qc
             SI_CK(cudaMemcpyAsync(h_out + h_off[qa], dbuf, sizeof(int32_t) * need, cudaMemcpyDeviceToHost,
                                   si->copy_st));
         SI_CK(cudaEventRecord(si->ev_copied[b], si->copy_st));
+        return SI_OK;
+    };
+    for (size_t c = 0; c < n_chunks; ++c) {
+        const int r = chunk(c);
+        if (r != SI_OK) {
+            // copies already queued finish before the buffers can be reused by a later call
+            if (si->copy_st) cudaStreamSynchronize(si->copy_st);
+            cudaStreamSynchronize(st);
+            return r;
+        }
     }
     // the compute stream waits for the last copy (the copy stream runs in order), so later
     // work on it sees the results
