@@ -85,13 +85,10 @@ def make_workload(cfg, scale, rank, contigs=None):
     n, nq = sizes[cfg]
     if cfg == "config3" and contigs:
         # a subset of the contigs with its share of the intervals and queries
-        names = set(contigs.split(","))
-        sub = [c for c in W.HUMAN_CONTIGS if c[0] in names]
-        if len(sub) != len(names):
-            raise SystemExit(f"unknown contig in --contigs {contigs}")
-        share = sum(c[1] for c in sub) / sum(c[1] for c in W.HUMAN_CONTIGS)
-        n, nq = max(1000, int(n * scale * share)), max(1000, int(nq * scale * share))
-        wl = W.config3(n=n, nq=nq, contigs=sub)
+        try:
+            wl = W.config3_subset(contigs.split(","), scale, n, nq)
+        except ValueError as e:
+            raise SystemExit(f"--contigs {contigs}: {e}")
     else:
         n, nq = max(1000, int(n * scale)), max(1000, int(nq * scale))
         wl = getattr(W, cfg)(n=n, nq=nq)
@@ -285,6 +282,17 @@ def run_gpu(args, rank, world, dist):
            "clocks": clk.summary(), "s_bytes": s_bytes}
     if args.profile_only:
         return res
+    # the timed step's own result for the first queries, for the comparison with the oracle
+    if rank == 0 and not args.no_cpu:
+        kq = min(nq, PARITY_QUERIES)
+        h_off = np.empty(kq + 1, np.int64)
+        _capi.check(lib.memcpyGpu(C.c_void_p(h_off.ctypes.data), d_off, h_off.nbytes, st))
+        _capi.check(lib.streamSynchronizeGpu(st))
+        h_val = np.empty(int(h_off[-1]), np.int32)
+        if h_val.size:
+            _capi.check(lib.memcpyGpu(C.c_void_p(h_val.ctypes.data), d_out, h_val.nbytes, st))
+        _capi.check(lib.streamSynchronizeGpu(st))
+        res["gpu_prefix"] = (h_off, h_val)
 
     # per-phase device times (count / scan / emit / prepare) for the roofline
     _capi.check(lib.setProfilingGpu(idx.h, 1))
@@ -340,15 +348,22 @@ def run_gpu(args, rank, world, dist):
         res["e2e_s"] = max_over_ranks(e2e_s, dist)
         res["h2d_bytes"] = wl.q_starts.nbytes + wl.q_ends.nbytes + (wl.q_contig.nbytes if hq_c else 0)
         res["d2h_bytes"] = 8 * (nq + 1) + 4 * P
-        # the host link this box gives: one large device-to-host copy into the same pinned buffer
-        link = min(4 * P, 8 << 30)
-        if link >= (64 << 20):
-            d_tmp = dalloc(link)
-            for _ in range(2):      # the first copy also maps the fresh device buffer: time the second
+        # the host link this box gives, copied the way the e2e call copies its result: 4 GiB
+        # device-to-host chunks (the default output budget) into the same pinned buffer, over
+        # up to 16 GiB, best of several repeats (the first also maps the fresh device buffer)
+        chunk = min(4 * P, 4 << 30)
+        if chunk >= (64 << 20):
+            span = min(4 * P, 16 << 30)
+            d_tmp = dalloc(chunk)
+            best = None
+            for _ in range(4):
                 t0 = time.perf_counter()
-                _capi.check(lib.memcpyGpu(h_out, d_tmp, link, st))
+                for off_b in range(0, span - chunk + 1, chunk):
+                    _capi.check(lib.memcpyGpu(C.c_void_p(h_out.value + off_b), d_tmp, chunk, st))
                 _capi.check(lib.streamSynchronizeGpu(st))
-            res["d2h_link_GBps"] = link / (time.perf_counter() - t0) / 1e9
+                dt = time.perf_counter() - t0
+                best = dt if best is None else min(best, dt)
+            res["d2h_link_GBps"] = (span // chunk) * chunk / best / 1e9
             lib.deviceFreeGpu(d_tmp)
         for p in (hq_s, hq_e, hq_c, h_off, h_out):
             if p:
@@ -916,33 +931,54 @@ def serving_cpu(wl, qs, qe, qc, seconds, nth):
     sub = Workload(name="serving sample", starts=wl.starts[sel], ends=wl.ends[sel], data=wl.data[sel], seg=seg,
                    q_starts=qs[qmask][:2_000_000], q_ends=qe[qmask][:2_000_000],
                    q_contig=remap[qc[qmask]][:2_000_000], contigs=[wl.contigs[g] for g in pick])
-    c = cpu_run(sub, seconds, nth)
+    c = cpu_run(sub, seconds, nth, single=False)
     c["sample"] = (f"{c['sample_q']} queries of the request stream on {len(pick)} contigs "
                    f"({len(sel)} intervals), search_idxs C++ order ({c['pairs']} pairs), {nth} threads")
     return c
 
 
 # ----------------------------------------------------------------------------- CPU arm
-def cpu_run(wl, seconds, nthreads):
-    """The reference algorithm (oracle port, oracle/si_oracle.c) on the host
-    cores: count + emit (search_idxs, C++ order) over a bounded query sample."""
+PARITY_QUERIES = 1 << 20   # headline queries whose GPU result is compared with the oracle's
+
+
+def cpu_run(wl, seconds, nthreads, keep=0, single=True):
+    """The reference algorithm (oracle port, oracle/si_oracle.c, pinned bit-exactly to the
+    reference's outputs) on the host cores: search_idxs in the C++ order over a bounded
+    prefix of the batch, one walk per query appending to per-chunk buffers and then copied
+    into one CSR result (the form the reference's per-query search_idxs takes,
+    superintervals.hpp:879-905).  The sample is sized to about `seconds` of work and holds at
+    least the first `keep` queries, whose CSR is returned for the parity check.  With
+    `single`, the same is also timed on one thread over a smaller prefix."""
     from oracle.oracle import ORDER_IDXS_CPP, Oracle
     o = Oracle()
     m = o.build(wl.starts, wl.ends, wl.data, seg=wl.seg)
+
+    def qslice(k):
+        qc = None if wl.q_contig is None else wl.q_contig[:k]
+        return wl.q_starts[:k], wl.q_ends[:k], qc
+
     probe = min(wl.nq, 20_000)
     t0 = time.perf_counter()
-    qc = None if wl.q_contig is None else wl.q_contig[:probe]
-    o.search_batch(m, wl.q_starts[:probe], wl.q_ends[:probe], qc, order=ORDER_IDXS_CPP,
-                   nthreads=nthreads)
+    o.search_lists(m, *qslice(probe), order=ORDER_IDXS_CPP, nthreads=nthreads)
     dt = max(time.perf_counter() - t0, 1e-6)
-    k = int(min(wl.nq, max(probe, probe * seconds / dt)))
-    qc = None if wl.q_contig is None else wl.q_contig[:k]
+    k = int(min(wl.nq, max(probe, keep, probe * seconds / dt)))
     t0 = time.perf_counter()
-    off, _ = o.search_batch(m, wl.q_starts[:k], wl.q_ends[:k], qc, order=ORDER_IDXS_CPP,
-                            nthreads=nthreads)
+    off, out = o.search_lists(m, *qslice(k), order=ORDER_IDXS_CPP, nthreads=nthreads)
     dt = time.perf_counter() - t0
-    return {"q_per_s": k / dt, "pairs_per_s": float(off[-1]) / dt, "sample_q": k, "seconds": dt,
-            "pairs": int(off[-1])}
+    res = {"q_per_s": k / dt, "pairs_per_s": float(off[-1]) / dt, "sample_q": k, "seconds": dt,
+           "pairs": int(off[-1])}
+    if keep:
+        kk = min(keep, k)
+        res["kept"] = (off[:kk + 1].copy(), out[:int(off[kk])].copy())
+    del off, out
+    if single:
+        # one thread at about the per-thread rate just measured, for a quarter of `seconds`
+        k1 = int(min(k, max(probe, k / dt / max(nthreads, 1) * seconds / 4)))
+        t0 = time.perf_counter()
+        o1, _ = o.search_lists(m, *qslice(k1), order=ORDER_IDXS_CPP, nthreads=1)
+        d1 = time.perf_counter() - t0
+        res["single_thread"] = {"q_per_s": k1 / d1, "pairs_per_s": float(o1[-1]) / d1, "sample_q": k1}
+    return res
 
 
 def host_threads():
@@ -1044,12 +1080,14 @@ def main():
         wl = make_workload(cfg, args.scale, 0)
         nth = host_threads()
         for _ in range(max(0, min(args.warmup, 1))):
-            cpu_run(wl, min(2.0, args.cpu_seconds / 4), nth)
-        runs = [cpu_run(wl, args.cpu_seconds / max(1, args.steps), nth) for _ in range(args.steps)]
+            cpu_run(wl, min(2.0, args.cpu_seconds / 4), nth, single=False)
+        runs = [cpu_run(wl, args.cpu_seconds / max(1, args.steps), nth, single=(i == 0))
+                for i in range(args.steps)]
         qps = statistics.median(r["q_per_s"] for r in runs)
         pps = statistics.median(r["pairs_per_s"] for r in runs)
-        sample = (f"{runs[0]['sample_q']} of {wl.nq} queries per step "
-                  f"({runs[0]['pairs']} result pairs), search_idxs C++ order, {nth} threads")
+        sample = (f"first {runs[0]['sample_q']} of {wl.nq} queries per step "
+                  f"({runs[0]['pairs']} result pairs), search_idxs C++ order, {nth} threads, "
+                  "one walk per query")
         line = {"metric": METRIC, "value": qps, "unit": "queries/s", "impl": "reference",
                 "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
                 "ms_per_step": 1000.0 * statistics.median(r["seconds"] for r in runs),
@@ -1057,12 +1095,17 @@ def main():
                 "data": "synthetic (seeded)", "config": workload_desc(cfg, wl),
                 "pairs_per_s": pps,
                 "cpu_baseline": {"value": qps, "unit": "queries/s", "cores": nth, "kind": "port",
-                                 "sample": sample},
+                                 "sample": sample,
+                                 "single_thread": {"value": runs[0]["single_thread"]["q_per_s"],
+                                                   "pairs_per_s": runs[0]["single_thread"]["pairs_per_s"],
+                                                   "sample": f"first {runs[0]['single_thread']['sample_q']} "
+                                                             "queries, 1 thread"}},
                 "e2e": {"value": qps, "unit": "queries/s", "h2d_bytes_per_step": 0,
                         "d2h_bytes_per_step": 0},
                 "note": "reference algorithm restated in C (oracle/si_oracle.c, pinned to the "
-                        "reference's own outputs); the reference header cannot be compiled on "
-                        "the GPU host because its sources are not present there"}
+                        "reference's own outputs; 1.06x the reference header's speed on one x86 "
+                        "thread, profiles/cpu_port_vs_reference.md); the reference header cannot be "
+                        "compiled on this host: its sources are not present here"}
         print(json.dumps(line), flush=True)
         return
 
@@ -1131,11 +1174,30 @@ def main():
                        "ms_per_step": 1e3 * res["e2e_s"]}
     if not args.no_cpu:
         nth = host_threads()
-        c = cpu_run(wl, args.cpu_seconds, nth)
+        keep = len(res["gpu_prefix"][0]) - 1 if "gpu_prefix" in res else 0
+        c = cpu_run(wl, args.cpu_seconds, nth, keep=keep)
         line["cpu_baseline"] = {"value": c["q_per_s"], "unit": "queries/s", "cores": nth, "kind": "port",
-                                "sample": f"{c['sample_q']} of {nq} queries, search_idxs C++ order "
-                                          f"({c['pairs']} pairs), {nth} threads",
+                                "sample": f"first {c['sample_q']} of {nq} queries, search_idxs C++ order "
+                                          f"({c['pairs']} pairs), {nth} threads; oracle/si_oracle.c "
+                                          "one walk per query (1.06x the reference header's speed on "
+                                          "one x86 thread, profiles/cpu_port_vs_reference.md)",
                                 "pairs_per_s": c["pairs_per_s"]}
+        if "single_thread" in c:
+            st1 = c["single_thread"]
+            line["cpu_baseline"]["single_thread"] = {"value": st1["q_per_s"], "pairs_per_s": st1["pairs_per_s"],
+                                                     "sample": f"first {st1['sample_q']} queries, 1 thread"}
+        if "gpu_prefix" in res and "kept" in c:
+            g_off, g_val = res.pop("gpu_prefix")
+            o_off, o_val = c.pop("kept")
+            k = min(len(g_off), len(o_off)) - 1
+            ok = bool(np.array_equal(g_off[:k + 1], o_off[:k + 1]) and
+                      np.array_equal(g_val[:int(g_off[k])], o_val[:int(o_off[k])]))
+            line["parity_sample_ok"] = ok
+            line["parity_sample"] = (f"the timed step's CSR result for the first {k} queries "
+                                     f"({int(o_off[k])} pairs) against the oracle, bit for bit")
+            if not ok:
+                print(json.dumps(line), flush=True)
+                raise SystemExit("parity check failed: the GPU result differs from the oracle's")
     print(json.dumps(line), flush=True)
 
 

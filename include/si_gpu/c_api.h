@@ -243,7 +243,11 @@ int searchDeviceGpu(gSuperIntervals* si, const void* d_qs, const void* d_qe,
  * (larger batches return SI_ERR_TOO_LARGE).  All calls share that array: calls
  * that overlap on the GPU race and must be serialized by the caller.  The first
  * call on a device looks the array up on that device; make it before any stream
- * capture.  The index must already be built. */
+ * capture.  Every call reads the result size back into host memory and waits for
+ * `stream`, so it returns with the search finished.  A result larger than
+ * `capacity` returns SI_ERR_CAPACITY with the offsets and *total filled and
+ * nothing written to d_values, which may be NULL only with capacity 0.  The index
+ * must already be built. */
 int searchIdxsNoAllocGpu(gSuperIntervals* si, const void* d_qs, const void* d_qe,
                          const int32_t* d_qcontig, size_t nq, int order, int64_t* d_offsets,
                          int32_t* d_values, size_t capacity, size_t* total, void* stream);

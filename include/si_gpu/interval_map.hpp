@@ -114,13 +114,15 @@ public:
     Interval<S, T> at(size_t index) const { return Interval<S, T>(starts[index], ends[index], data[index]); }
 
     // ---- single queries (the reference's per-query methods), as one-query batches ----------
-    size_t count(S start, S end) const {
+    // count and has_overlaps are noexcept as in the reference (hpp:651, 865): a device failure
+    // inside them ends the process through std::terminate instead of throwing.
+    size_t count(S start, S end) const noexcept {
         if (starts.empty()) return 0;
         uint32_t c = 0;
         count_into(&start, &end, 1, &c);
         return c;
     }
-    bool has_overlaps(S start, S end) const {
+    bool has_overlaps(S start, S end) const noexcept {
         if (starts.empty()) return false;
         uint8_t r = 0;
         need();

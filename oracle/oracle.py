@@ -15,7 +15,8 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "_build", "libsi_oracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libsi_ref.so")
-REF_SRC_DEFAULT = "/root/reference/src"
+# the reference checkout's src/ directory; SI_REF_SRC overrides the default location
+REF_SRC_DEFAULT = os.environ.get("SI_REF_SRC", "/root/reference/src")
 
 ORDER_IDXS_CPP = 0   # C++ search_idxs: ascending head run, then descending
 ORDER_DESC = 1       # search_values / C-API searchIdxs: fully descending
@@ -55,6 +56,10 @@ class Oracle:
         if not os.path.isfile(path):
             build_oracle()
         self.lib = C.CDLL(path)
+        self.lib.sio_lists_copy.restype = None
+        self.lib.sio_lists_copy.argtypes = [_P, _P, _P, C.c_int]
+        self.lib.sio_lists_free.restype = None
+        self.lib.sio_lists_free.argtypes = [_P]
         for sfx in ("i32", "i64"):
             f = getattr(self.lib, f"sio_build_{sfx}")
             f.restype = C.c_int
@@ -68,6 +73,9 @@ class Oracle:
             f = getattr(self.lib, f"sio_search_batch_{sfx}")
             f.restype = None
             f.argtypes = [_P, _P, _P, _P, _P, _I64, _P, _P, _P, C.c_int, _P, _P, C.c_int]
+            f = getattr(self.lib, f"sio_search_lists_{sfx}")
+            f.restype = _P
+            f.argtypes = [_P, _P, _P, _P, _P, _I64, _P, _P, _P, C.c_int, _P, C.c_int]
             f = getattr(self.lib, f"sio_intersection_{sfx}")
             f.restype = _I64
             f.argtypes = [_I64, _P, _P, _P, _I64, _P, _P, C.c_int, _P, _P, _P, _P, _I64]
@@ -133,6 +141,31 @@ class Oracle:
             _ptr(m["seg"]), _ptr(m["starts"]), _ptr(m["ends"]), _ptr(m["branch"]),
             _ptr(m["data"]) if values else None, qs.shape[0], _ptr(qc), _ptr(qs), _ptr(qe),
             order, _ptr(off), _ptr(out), nthreads)
+        return off, out
+
+    def search_lists(self, m, qs, qe, qc=None, order=ORDER_IDXS_CPP, values=False, nthreads=1):
+        """Same result as search_batch, in one walk per query: each thread appends its
+        queries' hits to a growable buffer (as the reference's search_idxs appends to a
+        vector, hpp:879-905), then the buffers are copied into the CSR arrays.  This is the
+        form the CPU baseline times."""
+        qs = np.ascontiguousarray(qs, dtype=m["starts"].dtype)
+        qe = np.ascontiguousarray(qe, dtype=m["starts"].dtype)
+        qc = None if qc is None else np.ascontiguousarray(qc, dtype=np.int32)
+        nq = qs.shape[0]
+        counts = np.empty(nq, dtype=np.uint32)
+        h = getattr(self.lib, f"sio_search_lists_{self._sfx(qs.dtype)}")(
+            _ptr(m["seg"]), _ptr(m["starts"]), _ptr(m["ends"]), _ptr(m["branch"]),
+            _ptr(m["data"]) if values else None, nq, _ptr(qc), _ptr(qs), _ptr(qe), order,
+            _ptr(counts), nthreads)
+        if not h:
+            raise MemoryError("oracle list search: host allocation failed")
+        try:
+            off = np.zeros(nq + 1, dtype=np.int64)
+            np.cumsum(counts, out=off[1:])
+            out = np.empty(int(off[-1]), dtype=np.int32)
+            self.lib.sio_lists_copy(h, _ptr(off), _ptr(out), nthreads)
+        finally:
+            self.lib.sio_lists_free(h)
         return off, out
 
     def intersection(self, m, a_s, a_e, order=ORDER_IDXS_CPP):

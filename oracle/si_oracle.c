@@ -79,7 +79,8 @@ static void* sio_thread_main(void* p) {
     return NULL;
 }
 
-static void sio_parallel_for(int64_t n, int nthreads, sio_worker_fn fn, void* ctx) {
+static void sio_parallel_for_chunk(int64_t n, int nthreads, void (*fn)(void*, int64_t, int64_t), void* ctx,
+                                   int64_t chunk) {
     if (n <= 0) return;
     if (nthreads <= 1) {
         fn(ctx, 0, n);
@@ -87,7 +88,7 @@ static void sio_parallel_for(int64_t n, int nthreads, sio_worker_fn fn, void* ct
     }
     sio_queue q;
     q.n = n;
-    q.chunk = 2048;
+    q.chunk = chunk;
     q.next = 0;
     pthread_t* th = (pthread_t*)malloc(sizeof(pthread_t) * (size_t)nthreads);
     sio_thread_arg arg = {&q, fn, ctx};
@@ -99,6 +100,91 @@ static void sio_parallel_for(int64_t n, int nthreads, sio_worker_fn fn, void* ct
     if (started == 0) fn(ctx, 0, n);
     for (int t = 0; t < started; ++t) pthread_join(th[t], NULL);
     free(th);
+}
+
+static void sio_parallel_for(int64_t n, int nthreads, void (*fn)(void*, int64_t, int64_t), void* ctx) {
+    sio_parallel_for_chunk(n, nthreads, fn, ctx, 2048);
+}
+
+/* ------------------------------------------------------------------------- */
+/* Single-pass batch search: each worker walks its queries once and appends   */
+/* the hits to a growable buffer per chunk of queries, as the reference's    */
+/* per-query search_idxs appends to a std::vector (hpp:879-905) and its batch */
+/* loop builds one list per query (intervalmap.pyx:402-446).  The chunks are  */
+/* then copied into one CSR array.                                            */
+/* ------------------------------------------------------------------------- */
+#define SIO_LIST_CHUNK 2048
+typedef struct {
+    int32_t* vals;
+    int64_t n, cap;
+} sio_list_chunk;
+
+typedef struct {
+    int64_t nq, n_chunks;
+    sio_list_chunk* chunks;
+} sio_lists;
+
+static int sio_list_reserve(sio_list_chunk* c, int64_t need) {
+    if (c->n + need <= c->cap) return 1;
+    int64_t cap = c->cap ? c->cap : 4096;
+    while (cap < c->n + need) cap *= 2;
+    int32_t* p = (int32_t*)realloc(c->vals, sizeof(int32_t) * (size_t)cap);
+    if (!p) return 0;
+    c->vals = p;
+    c->cap = cap;
+    return 1;
+}
+
+int64_t sio_lists_total(const void* h) {
+    const sio_lists* L = (const sio_lists*)h;
+    int64_t t = 0;
+    for (int64_t k = 0; k < L->n_chunks; ++k) t += L->chunks[k].n;
+    return t;
+}
+
+typedef struct {
+    const sio_lists* L;
+    const int64_t* offsets;
+    int32_t* out;
+} sio_copy_ctx;
+
+static void sio_copy_worker(void* p, int64_t b, int64_t e) {
+    sio_copy_ctx* c = (sio_copy_ctx*)p;
+    for (int64_t k = b; k < e; ++k) {
+        const sio_list_chunk* ch = &c->L->chunks[k];
+        if (ch->n) memcpy(c->out + c->offsets[k * SIO_LIST_CHUNK], ch->vals, sizeof(int32_t) * (size_t)ch->n);
+    }
+}
+
+static void sio_parallel_for_chunk(int64_t n, int nthreads, void (*fn)(void*, int64_t, int64_t), void* ctx,
+                                   int64_t chunk);
+
+/* Copy the chunk buffers into out at the query offsets (offsets[nq + 1] = exclusive sums of
+   the counts the search wrote). */
+void sio_lists_copy(const void* h, const int64_t* offsets, int32_t* out, int nthreads) {
+    sio_copy_ctx c = {(const sio_lists*)h, offsets, out};
+    sio_parallel_for_chunk(((const sio_lists*)h)->n_chunks, nthreads, sio_copy_worker, &c, 1);
+}
+
+void sio_lists_free(void* h) {
+    sio_lists* L = (sio_lists*)h;
+    if (!L) return;
+    for (int64_t k = 0; k < L->n_chunks; ++k) free(L->chunks[k].vals);
+    free(L->chunks);
+    free(L);
+}
+
+static sio_lists* sio_lists_new(int64_t nq) {
+    sio_lists* L = (sio_lists*)calloc(1, sizeof(sio_lists));
+    if (!L) return NULL;
+    L->nq = nq;
+    L->n_chunks = (nq + SIO_LIST_CHUNK - 1) / SIO_LIST_CHUNK;
+    L->chunks = (sio_list_chunk*)calloc((size_t)(L->n_chunks ? L->n_chunks : 1), sizeof(sio_list_chunk));
+    if (!L->chunks) {
+        free(L);
+        return NULL;
+    }
+    return L;
 }
 
 /* ------------------------------------------------------------------------- */
@@ -422,6 +508,82 @@ void sio_search_batch_##SFX(const int64_t* seg, const S* starts, const S* ends, 
     c.qc = qc; c.qs = qs; c.qe = qe; c.order = order; c.offsets = offsets;              \
     c.out32 = out;                                                                      \
     sio_parallel_for(nq, nthreads, sio_search_worker_##SFX, &c);                        \
+}                                                                                       \
+                                                                                        \
+/* Single-pass batch search (see sio_lists above): counts[q] = hits of query q;  */     \
+/* returns the chunk lists (sio_lists_total / sio_lists_copy / sio_lists_free).  */     \
+typedef struct {                                                                        \
+    sio_batch_ctx_##SFX b; sio_lists* L; int failed;                                    \
+} sio_lists_ctx_##SFX;                                                                  \
+                                                                                        \
+static void sio_lists_worker_##SFX(void* p, int64_t cb, int64_t ce) {                   \
+    sio_lists_ctx_##SFX* x = (sio_lists_ctx_##SFX*)p;                                   \
+    const sio_batch_ctx_##SFX* c = &x->b;                                               \
+    for (int64_t k = cb; k < ce; ++k) {                                                 \
+        sio_list_chunk* ch = &x->L->chunks[k];                                          \
+        /* the chunk's buffer in locals: stores through vals cannot alias them */       \
+        int32_t* vals = ch->vals; int64_t w = ch->n, cap = ch->cap;                     \
+        const int64_t q1 = (k + 1) * SIO_LIST_CHUNK < x->L->nq ? (k + 1) * SIO_LIST_CHUNK \
+                                                               : x->L->nq;              \
+        for (int64_t q = k * SIO_LIST_CHUNK; q < q1; ++q) {                             \
+            int32_t g = c->qc ? c->qc[q] : 0;                                           \
+            int64_t lo = c->seg[g], n = c->seg[g + 1] - lo;                             \
+            const S* st = c->starts + lo; const S* en = c->ends + lo;                   \
+            const int64_t* br = c->branch + lo;                                         \
+            const int32_t* dd = c->data ? c->data + lo : NULL;                          \
+            const S qs = c->qs[q], qe = c->qe[q];                                       \
+            const int64_t w0 = w;                                                       \
+            int64_t idx = sio_upper_bound_##SFX(n, st, qe);                             \
+            if (idx != SIO_NONE) {                                                      \
+                int64_t i = idx;                                                        \
+                while (i != SIO_NONE && qs <= en[i]) --i;                               \
+                if (w + (idx - i) + 64 > cap) {                                         \
+                    ch->vals = vals; ch->n = w; ch->cap = cap;                          \
+                    if (!sio_list_reserve(ch, idx - i + 64)) { x->failed = 1; return; } \
+                    vals = ch->vals; cap = ch->cap;                                     \
+                }                                                                       \
+                if (c->order == SIO_ORDER_IDXS_CPP) {                                   \
+                    for (int64_t t = i + 1; t <= idx; ++t) vals[w++] = dd ? dd[t] : (int32_t)t; \
+                } else {                                                                \
+                    for (int64_t t = idx; t > i; --t) vals[w++] = dd ? dd[t] : (int32_t)t; \
+                }                                                                       \
+                if (i != SIO_NONE) {                                                    \
+                    i = br[i];                                                          \
+                    while (i != SIO_NONE) {                                             \
+                        if (qs <= en[i]) {                                              \
+                            if (w == cap) {                                             \
+                                ch->vals = vals; ch->n = w; ch->cap = cap;              \
+                                if (!sio_list_reserve(ch, 64)) { x->failed = 1; return; } \
+                                vals = ch->vals; cap = ch->cap;                         \
+                            }                                                           \
+                            vals[w++] = dd ? dd[i] : (int32_t)i;                        \
+                            --i;                                                        \
+                        } else {                                                        \
+                            i = br[i];                                                  \
+                        }                                                               \
+                    }                                                                   \
+                }                                                                       \
+            }                                                                           \
+            c->counts[q] = (uint32_t)(w - w0);                                          \
+        }                                                                               \
+        ch->vals = vals; ch->n = w; ch->cap = cap;                                      \
+    }                                                                                   \
+}                                                                                       \
+                                                                                        \
+void* sio_search_lists_##SFX(const int64_t* seg, const S* starts, const S* ends,        \
+                             const int64_t* branch, const int32_t* data, int64_t nq,    \
+                             const int32_t* qc, const S* qs, const S* qe, int order,    \
+                             uint32_t* counts, int nthreads) {                          \
+    sio_lists_ctx_##SFX x;                                                              \
+    memset(&x, 0, sizeof(x));                                                           \
+    x.b.seg = seg; x.b.starts = starts; x.b.ends = ends; x.b.branch = branch;           \
+    x.b.data = data; x.b.qc = qc; x.b.qs = qs; x.b.qe = qe; x.b.order = order;          \
+    x.b.counts = counts;                                                                \
+    x.L = sio_lists_new(nq);                                                            \
+    if (!x.L) return NULL;                                                              \
+    sio_parallel_for_chunk(x.L->n_chunks, nthreads, sio_lists_worker_##SFX, &x, 1);              \
+    if (x.failed) { sio_lists_free(x.L); return NULL; }                                 \
+    return x.L;                                                                         \
 }                                                                                       \
                                                                                         \
 /* Per-contig build over concatenated input segments (each segment is one map). */     \

@@ -1161,7 +1161,9 @@ extern "C" int getBatchedParamsGpu(const gSuperIntervals* si, int* tile_q, int* 
 //   * every call shares the array and it keeps the last call's contents: calls that overlap on
 //     the GPU (other streams, threads or handles) race on it, so the caller serializes them;
 //   * the first call on a device looks up the array's device address with that device current;
-//     make that first call before any stream capture.
+//     make that first call before any stream capture;
+//   * every call reads the result size back into host memory and waits for its stream, so it
+//     returns with the search finished.
 // =====================================================================================
 namespace {
 
@@ -1205,8 +1207,14 @@ int search_noalloc(gSuperIntervals* si, const sig::QueryBatch& q, int order, int
     SI_CK(cudaMemsetAsync(d_err, 0, sizeof(int), st));  // the error word starts at zero
     if (si->n == 0 || q.nq == 0) {
         SI_CK(cudaMemsetAsync(d_offsets, 0, sizeof(int64_t) * (q.nq + 1), st));
+        // an empty index still rejects contig ids outside [0, G), as searchDeviceGpu does
+        SI_CK(sig::launch_check_contigs(q.qc, q.nq, si->G, d_err, st));
+        int e = 0;
+        SI_CK(cudaMemcpyAsync(&e, d_err, sizeof(int), cudaMemcpyDeviceToHost, st));
         SI_CK(cudaStreamSynchronize(st));
         if (total) *total = 0;
+        if (e == sig::kDevBadContig) return fail(SI_ERR_INVALID, "a query names a contig outside [0, %d)", si->G);
+        if (e != 0) return fail(SI_ERR_CUDA, "device error word %d", e);
         return SI_OK;
     }
     SI_CK(sig::launch_count_plain<S>(view<S>(si), q, counts, d_err, st));
@@ -1238,6 +1246,7 @@ extern "C" int searchIdxsNoAllocGpu(gSuperIntervals* si, const void* d_qs, const
         return fail(SI_ERR_TOO_LARGE, "the allocation-free search takes at most %zu queries per call, got %zu",
                     kNoAllocMaxQueries, nq);
     if (!d_offsets || (nq && (!d_qs || !d_qe))) return fail(SI_ERR_INVALID, "null device buffer");
+    if (capacity > 0 && !d_values) return fail(SI_ERR_INVALID, "null value buffer with capacity %zu", capacity);
     SI_TRY(set_dev(si));
     cudaStream_t st = stream ? (cudaStream_t)stream : si->st;
     sig::QueryBatch q{d_qs, d_qe, d_qcontig, (int64_t)nq};

@@ -170,6 +170,20 @@ def config3(n=50_000_000, nq=50_000_000, contigs=None, long_queries=False) -> Wo
     )
 
 
+def config3_subset(names, scale=1.0, n_full=50_000_000, nq_full=50_000_000) -> Workload:
+    """Configuration 3 on a subset of its contigs with the subset's share of the intervals and
+    queries (contig length over the whole genome), so that intervals per bp and hits per query
+    stay those of the full configuration (~500 hits per query from the 1% of 1-5 Mb
+    intervals): a small case of the full-size regime for parity tests and profiles."""
+    names = list(names)
+    sub = [c for c in HUMAN_CONTIGS if c[0] in set(names)]
+    if len(sub) != len(set(names)):
+        raise ValueError(f"unknown contig in {names}")
+    share = sum(c[1] for c in sub) / sum(c[1] for c in HUMAN_CONTIGS)
+    n, nq = max(1000, int(n_full * scale * share)), max(1000, int(nq_full * scale * share))
+    return config3(n=n, nq=nq, contigs=sub)
+
+
 def _clustered_starts(rng, zrng, n, span, hotspots=10_000, zipf_s=1.1, jitter=5_000.0,
                       frac_hot=0.70):
     hot_pos = zrng.integers(0, span, hotspots, dtype=np.int64)

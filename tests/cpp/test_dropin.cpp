@@ -7,6 +7,11 @@
 
 #include "si_gpu/interval_map.hpp"
 
+// the reference declares these two noexcept (superintervals.hpp:651, 865)
+static_assert(noexcept(std::declval<const si::IntervalMap<int, int>&>().count(0, 0)), "count is noexcept");
+static_assert(noexcept(std::declval<const si::IntervalMap<int64_t, int>&>().has_overlaps(0, 0)),
+              "has_overlaps is noexcept");
+
 #define CHECK(c)                                                          \
     do {                                                                  \
         if (!(c)) {                                                       \

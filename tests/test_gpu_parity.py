@@ -117,6 +117,62 @@ def test_config3_scaled(api, oracle, path):
     _oracle_case(api, oracle, W.config3(n=1_000_000, nq=300_000), path, orders=(0, 1))
 
 
+def _host_threads():
+    import os
+    try:
+        return len(os.sched_getaffinity(0))
+    except Exception:
+        return os.cpu_count() or 1
+
+
+def test_config3_full_density_contig_subset(api, oracle):
+    """The headline configuration's density on two of its contigs: 50 M intervals and queries
+    over the 24 contigs, scaled to chr21 + chr22 by their share of the genome (1.58 M of each),
+    so ~500 hits per query from the 1% of 1-5 Mb intervals (nesting depth ~500).  This runs the
+    batched path the way the full workload does: rank counts, the automatic tile size at its
+    densest, long candidate lists holding nearly every hit, and the per-query miss handling of
+    long candidates.  The whole batch is compared with the oracle (superintervals.hpp:879-905
+    order, the fully descending order and payloads), with the default and the autotuned
+    tunables and the learned upper bound."""
+    import ctypes as C
+    from superintervals_gb300 import autotune, workloads as W
+    wl = W.config3_subset(["chr21", "chr22"])
+    nth = _host_threads()
+    idx = _index(api, wl.starts, wl.ends, wl.data, seg=wl.seg, path="batched")
+    idx.set_upper_bound(api.UB_LEARNED)
+    m = oracle.build(wl.starts, wl.ends, wl.data, seg=wl.seg)
+    rc = oracle.count_batch(m, wl.q_starts, wl.q_ends, wl.q_contig, nthreads=nth)
+    assert rc.sum() / wl.nq > 400                      # the headline's hits per query
+    assert np.array_equal(idx.count(wl.q_starts, wl.q_ends, wl.q_contig), rc)
+    ro, rv = oracle.search_batch(m, wl.q_starts, wl.q_ends, wl.q_contig, order=0, nthreads=nth, counts=rc)
+    off, out = idx.search(wl.q_starts, wl.q_ends, wl.q_contig, order=api.ORDER_IDXS_CPP)
+    assert np.array_equal(off, ro) and np.array_equal(out, rv)
+    del out
+    # the autotuned tunables, as the benchmark runs them (timed on the whole device batch)
+    lib = idx.lib
+    dev = []
+    for a in (wl.q_starts, wl.q_ends, wl.q_contig):
+        p = C.c_void_p()
+        api.check(lib.deviceMallocGpu(C.byref(p), a.nbytes))
+        api.check(lib.memcpyGpu(p, C.c_void_p(a.ctypes.data), a.nbytes, idx.stream))
+        dev.append(p)
+    choice = autotune.tune(idx, dev[0], dev[1], dev[2], wl.nq, sample=0, use_cache=False, keep_upper_bound=True)
+    for p in dev:
+        lib.deviceFreeGpu(p)
+    off, out = idx.search(wl.q_starts, wl.q_ends, wl.q_contig, order=api.ORDER_IDXS_CPP)
+    assert np.array_equal(off, ro) and np.array_equal(out, rv), choice
+    del out, rv
+    ro1, rv1 = oracle.search_batch(m, wl.q_starts, wl.q_ends, wl.q_contig, order=1, nthreads=nth, counts=rc)
+    off, out = idx.search(wl.q_starts, wl.q_ends, wl.q_contig, order=api.ORDER_DESC)
+    assert np.array_equal(off, ro1) and np.array_equal(out, rv1)
+    del out, rv1
+    _, rvv = oracle.search_batch(m, wl.q_starts, wl.q_ends, wl.q_contig, order=1, values=True, nthreads=nth,
+                                 counts=rc)
+    _, outv = idx.search(wl.q_starts, wl.q_ends, wl.q_contig, order=api.ORDER_DESC, values=True)
+    assert np.array_equal(outv, rvv)
+    idx.close()
+
+
 @pytest.mark.parametrize("path", PATHS)
 def test_config3_long_queries_scaled(api, oracle, path):
     from superintervals_gb300 import workloads as W
