@@ -302,8 +302,20 @@ def run_gpu(args, rank, world, dist):
     ms4 = (C.c_double * 4)()
     n4 = (C.c_int64 * 4)()
     _capi.check(lib.getPhaseTimesGpu(idx.h, ms4, n4))
-    _capi.check(lib.setProfilingGpu(idx.h, 0))
     res["phase_ms"] = [ms4[k] / max(1, n4[k]) for k in range(4)]
+    if path == _capi.PATH_BATCHED:
+        # the same steps with the long-interval list's section of part B filtered instead of
+        # copied (the emit's other mode), for comparison
+        _capi.check(lib.setProfilingGpu(idx.h, 0))
+        _capi.check(lib.setProfilingGpu(idx.h, 1))
+        _capi.check(lib.setBatchedOptionGpu(idx.h, _capi.OPT_EMIT_COPY, 0))
+        for _ in range(max(1, min(3, args.steps))):
+            _capi.check(lib.flushL2Gpu(st))
+            step()
+        _capi.check(lib.getPhaseTimesGpu(idx.h, ms4, n4))
+        res["emit_filter_only_ms"] = ms4[2] / max(1, n4[2])
+        _capi.check(lib.setBatchedOptionGpu(idx.h, _capi.OPT_EMIT_COPY, 1))
+    _capi.check(lib.setProfilingGpu(idx.h, 0))
 
     # the plain one-query-per-thread GPU path on the same inputs (the 1.0x baseline)
     if not args.no_plain and args.path != "plain":
@@ -414,43 +426,50 @@ def run_gpu_ub(args, rank, world, dist):
     host = np.empty(nq, dtype=np.int32)
     ref = None
     res = {"wl": wl, "nq": nq, "s_bytes": s_bytes, "build_s": build_s, "modes": {}}
-    for name, mode in UB_MODES:
-        t0 = time.perf_counter()
-        idx.set_upper_bound(mode)          # builds the provider's structure (model / tree)
-        prep_s = time.perf_counter() - t0
+    # each provider per query (plain path: one thread per query in the batch's order) and
+    # through the sorted batch (batched path: the ends radix-sorted, two searches per 256
+    # sorted ends, the rest resolved in a shared-memory window, answers scattered back)
+    for path_name, path in (("per_query", _capi.PATH_PLAIN), ("sorted_batch", _capi.PATH_BATCHED)):
+        idx.set_path(path)
+        for name, mode in UB_MODES:
+            t0 = time.perf_counter()
+            idx.set_upper_bound(mode)          # builds the provider's structure (model / tree)
+            prep_s = time.perf_counter() - t0
 
-        def step():
-            _capi.check(lib.upperBoundDeviceGpu(idx.h, d_qe, d_qc, nq, mode, d_out, st))
-        for _ in range(args.warmup):
-            _capi.check(lib.flushL2Gpu(st))
-            step()
-        _capi.check(lib.streamSynchronizeGpu(st))
-        if dist:
-            dist.barrier()
-        k0 = lib.getLaunchCountGpu()
-        total_ms = 0.0
-        with ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) as clk:
-            for _ in range(args.steps):
+            def step():
+                _capi.check(lib.upperBoundDeviceGpu(idx.h, d_qe, d_qc, nq, mode, d_out, st))
+            for _ in range(args.warmup):
                 _capi.check(lib.flushL2Gpu(st))
-                _capi.check(lib.eventRecordGpu(ev[0], st))
                 step()
-                _capi.check(lib.eventRecordGpu(ev[1], st))
-                _capi.check(lib.streamSynchronizeGpu(st))
-                ms = C.c_float()
-                _capi.check(lib.eventElapsedMsGpu(ev[0], ev[1], C.byref(ms)))
-                total_ms += ms.value
-        launches = lib.getLaunchCountGpu() - k0   # the L2 flush is a memset, not counted
-        total_ms = max_over_ranks(total_ms, dist)
-        _capi.check(lib.memcpyGpu(C.c_void_p(host.ctypes.data), d_out, host.nbytes, st))
-        _capi.check(lib.streamSynchronizeGpu(st))
-        if ref is None:
-            ref = host.copy()
-            same = True
-        else:
-            same = bool(np.array_equal(host, ref))
-        res["modes"][name] = {"ms_per_step": total_ms / args.steps, "prepare_s": prep_s,
-                              "identical_to_binary": same, "launches": launches,
-                              "clocks": clk.summary()}
+            _capi.check(lib.streamSynchronizeGpu(st))
+            if dist:
+                dist.barrier()
+            k0 = lib.getLaunchCountGpu()
+            total_ms = 0.0
+            with ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) as clk:
+                for _ in range(args.steps):
+                    _capi.check(lib.flushL2Gpu(st))
+                    _capi.check(lib.eventRecordGpu(ev[0], st))
+                    step()
+                    _capi.check(lib.eventRecordGpu(ev[1], st))
+                    _capi.check(lib.streamSynchronizeGpu(st))
+                    ms = C.c_float()
+                    _capi.check(lib.eventElapsedMsGpu(ev[0], ev[1], C.byref(ms)))
+                    total_ms += ms.value
+            launches = lib.getLaunchCountGpu() - k0   # the L2 flush is a memset, not counted
+            total_ms = max_over_ranks(total_ms, dist)
+            _capi.check(lib.memcpyGpu(C.c_void_p(host.ctypes.data), d_out, host.nbytes, st))
+            _capi.check(lib.streamSynchronizeGpu(st))
+            if ref is None:
+                ref = host.copy()
+                same = True
+            else:
+                same = bool(np.array_equal(host, ref))
+            key = name if path_name == "per_query" else f"{name}+sorted"
+            res["modes"][key] = {"ms_per_step": total_ms / args.steps, "prepare_s": prep_s,
+                                 "identical_to_binary": same, "launches": launches,
+                                 "clocks": clk.summary(), "path": path_name}
+    idx.set_path(_capi.PATH_AUTO)
     # the oracle's upper bound on a sample (sanity check of the binary result itself)
     from oracle.oracle import Oracle
     o = Oracle()
@@ -464,6 +483,7 @@ def run_gpu_ub(args, rank, world, dist):
     if not args.no_e2e:
         mode = dict(UB_MODES)[args.ub]
         idx.set_upper_bound(mode)
+        idx.set_path(_capi.PATH_BATCHED)
         hp, ho = C.c_void_p(), C.c_void_p()
         _capi.check(lib.hostMallocPinnedGpu(C.byref(hp), qe.nbytes))
         _capi.check(lib.hostMallocPinnedGpu(C.byref(ho), 4 * nq))
@@ -510,27 +530,32 @@ def cpu_run_ub(o, m, wl, seconds, nthreads):
 def ub_line(args, res, world):
     wl, nq, s = res["wl"], res["nq"], res["s_bytes"]
     modes = res["modes"]
-    main = modes[args.ub]
+    main = modes[args.ub + "+sorted"]
     ms = main["ms_per_step"]
     peak, peak_kind = measured_peak()
-    # algorithmic bytes per query: the query end, the int32 result and one 32-byte sector
-    # of the starts array (the least a verified search reads)
-    algo = nq * (s + 4 + 32)
+    # algorithmic bytes: every query end read and its int32 result written, the starts array
+    # read once (the sorted batch reads each block's window of starts once)
+    algo = nq * (s + 4) + wl.n * s
     line = {"metric": METRIC_UB, "value": world * nq / (ms / 1e3), "unit": "queries/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "int64" if s == 8 else "int32",
             "data": "synthetic (seeded)",
-            "config": dict(workload_desc(args.config, wl), op="upper_bound", upper_bound=args.ub),
+            "config": dict(workload_desc(args.config, wl), op="upper_bound", upper_bound=args.ub,
+                           path="sorted batch (batched path)"),
             "build_s": res["build_s"], "clocks": main["clocks"],
             "providers": {k: {"queries_per_s": nq / (v["ms_per_step"] / 1e3), "ms_per_step": v["ms_per_step"],
-                              "prepare_s": v["prepare_s"], "identical_to_binary": v["identical_to_binary"]}
+                              "prepare_s": v["prepare_s"], "identical_to_binary": v["identical_to_binary"],
+                              "path": v["path"]}
                           for k, v in modes.items()},
             "speedup_vs_binary": modes["binary"]["ms_per_step"] / ms,
+            "speedup_vs_binary_note": "binary = the reference's halving search, one query per thread in "
+                                      "the batch's order; value = the chosen provider on the sorted batch",
+            "learned_vs_binary_per_query": modes["binary"]["ms_per_step"] / modes["learned"]["ms_per_step"],
             "oracle_sample_identical": res["oracle_sample_ok"],
             "roofline": {"bound": "hbm", "achieved": algo / (ms / 1e3) / 1e9, "peak": peak, "unit": "GB/s",
-                         "frac": algo / (ms / 1e3) / 1e9 / peak, "traffic": None, "kernel": "k_ub_plain",
-                         "peak_kind": peak_kind, "algorithmic_bytes": algo,
-                         "note": "dependent random probes: latency-bound, not bandwidth-bound"},
+                         "frac": algo / (ms / 1e3) / 1e9 / peak, "traffic": None,
+                         "kernel": "sorted batch (radix sort + k_qprep + k_ub_scatter)",
+                         "peak_kind": peak_kind, "algorithmic_bytes": algo},
             "gpu_launches": main["launches"]}
     line["config"]["inputs"] = "index > L2 (starts array alone 0.8 GB); L2 flushed between steps"
     if "e2e_s" in res:
@@ -1162,6 +1187,7 @@ def main():
                         "traffic_frac": (traffic / (emit_ms / 1000.0) / 1e9 / peak) if traffic else None,
                         "peak_kind": peak_kind, "algorithmic_bytes": algo,
                         "phase_ms": {"count": ph[0], "scan": ph[1], "emit": ph[2], "prepare": ph[3]},
+                        "emit_ms_filter_only": res.get("emit_filter_only_ms"),
                         "whole_step_frac": (algo / (ms / 1000.0) / 1e9) / peak}
     line["gpu_launches"] = res["launches"]
     if "plain_ms" in res:

@@ -162,6 +162,16 @@ int setBatchedParamsGpu(gSuperIntervals* si, int tile_queries, int tile_candidat
                         int64_t long_query_len, int64_t split_len);
 int getBatchedParamsGpu(const gSuperIntervals* si, int* tile_queries, int* tile_candidates,
                         int64_t* long_query_len, int64_t* split_len);
+/* Further tunables of the batched path (no reference counterpart); results never depend on
+ * them.  SI_OPT_EMIT_COPY: 1 (default) writes the section of a tile's long candidates that
+ * comes from the long-interval list (intervals at least 65536 long) as copied runs between
+ * its few misses, 0 filters every candidate.  SI_OPT_EYTZ_DEPTH: levels of the Eytzinger
+ * tree (1-13, 0 automatic), resampled at once when it is the current provider.
+ * getBatchedOptionGpu reports the depth in use. */
+#define SI_OPT_EMIT_COPY 1
+#define SI_OPT_EYTZ_DEPTH 2
+int setBatchedOptionGpu(gSuperIntervals* si, int option, int64_t value);
+int getBatchedOptionGpu(const gSuperIntervals* si, int option, int64_t* value);
 /* Autotuner of the batched path: times full searches on the first `sample`
  * queries of a device-resident batch (sample = 0 or >= nq: the whole batch; a
  * prefix of an unsorted batch is sparser along the genome than the batch, so it

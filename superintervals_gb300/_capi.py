@@ -27,6 +27,9 @@ ORDER_DESC = 1
 
 TUNE_KEEP_UPPER_BOUND = 1
 
+OPT_EMIT_COPY = 1
+OPT_EYTZ_DEPTH = 2
+
 PATH_AUTO = 0
 PATH_PLAIN = 1
 PATH_BATCHED = 2
@@ -92,6 +95,8 @@ SIGNATURES = {
     "setOutputBudgetGpu": (_I, [_H, _SZ]),
     "setBatchedParamsGpu": (_I, [_H, _I, _I, C.c_int64, C.c_int64]),
     "getBatchedParamsGpu": (_I, [_H, _P, _P, _P, _P]),
+    "setBatchedOptionGpu": (_I, [_H, _I, C.c_int64]),
+    "getBatchedOptionGpu": (_I, [_H, _I, _P]),
     "autotuneBatchedGpu": (_I, [_H, _P, _P, _P, _SZ, _SZ, _I, C.c_char_p, _SZ]),
     "setProfilingGpu": (_I, [_H, _I]),
     "getPhaseTimesGpu": (_I, [_H, _P, _P]),

@@ -1,7 +1,8 @@
 """Cached autotuning of the batched path.
 
 `tune()` runs the library's autotuner (`autotuneBatchedGpu`: coordinate descent over the
-upper-bound provider, tile size, candidate capacity and length split, timed on a sample of
+upper-bound provider, tile size, candidate capacity, length split, the emit's copy mode and the
+Eytzinger tree's depth, timed on a sample of
 the caller's own device-resident queries) once per (GPU model, index size, batch size,
 coordinate width, contig count) and stores the choice in a JSON file; later calls with the
 same key apply the stored choice without timing anything.
@@ -43,6 +44,10 @@ def apply(index, choice: dict):
     tile = -1 if int(choice.get("tile_auto", 0)) else int(choice["tile_queries"])
     _capi.check(lib.setBatchedParamsGpu(index.h, tile, int(choice["tile_candidates"]),
                                         int(choice["long_query_len"]), int(choice["split_len"])))
+    if "emit_copy" in choice:
+        _capi.check(lib.setBatchedOptionGpu(index.h, _capi.OPT_EMIT_COPY, int(choice["emit_copy"])))
+    if "eytz_depth" in choice:
+        _capi.check(lib.setBatchedOptionGpu(index.h, _capi.OPT_EYTZ_DEPTH, int(choice["eytz_depth"])))
     index.set_upper_bound(int(choice["upper_bound"]))
 
 

@@ -178,6 +178,7 @@ struct TileArgs {
     int64_t out_base;
     int order;
     bool values;
+    bool emit_copy;          // copy the long-interval list's section of part B (else filter it)
     int32_t* out;
     int* d_err;
     // per-tile candidate lists stored by the count pass and reloaded by the emit pass
@@ -395,7 +396,8 @@ __device__ __forceinline__ bool is_long_iv(S start, S end, int64_t X) {
     return end >= start && (uint64_t)end - (uint64_t)start >= (uint64_t)X;
 }
 
-constexpr int kLnu = 128;        // long candidates ending before the tile's max qs
+constexpr int kLnu = 128;        // long-list candidates ending before the tile's max qs
+constexpr int kCacheHeader = 32; // bytes before a tile's cached lists
 constexpr int kMaxBlocks = 8192 / 32 + 1;
 
 // First position p in [a, b] with start[p] >= qs - X (starts ascending; b means none).
@@ -567,6 +569,47 @@ __device__ void long_query(const TileArgs<S>& a, S qs, int64_t u, int64_t lo, in
     }
 }
 
+// One warp copies src[0, len) (shared memory, any word offset) to dst[0, len) (global memory,
+// any 4-byte offset): 4-byte stores up to dst's first 16-byte boundary, then one 16-byte store
+// per lane and round (512 bytes per warp store), then the tail.  The four words of a lane's
+// 16-byte store are read in a lane-rotated order (lane l reads word (k + l / 8) mod 4 of its
+// group in step k), so that each shared-memory read touches 32 distinct banks, and rotated back
+// in registers.
+__device__ __forceinline__ void warp_copy_s2g(int32_t* __restrict__ dst, const int32_t* __restrict__ src, int len,
+                                              int lane) {
+    if (len <= 0) return;
+    const int head = min(len, (int)(((16u - ((uint32_t)(uintptr_t)dst & 15u)) & 15u) >> 2));
+    if (lane < head) dst[lane] = src[lane];
+    dst += head;
+    src += head;
+    len -= head;
+    const int n4 = len >> 2;
+    const int rot = lane >> 3;
+    const int o0 = rot & 3, o1 = (rot + 1) & 3, o2 = (rot + 2) & 3, o3 = (rot + 3) & 3;
+    int4* __restrict__ d4 = reinterpret_cast<int4*>(dst);
+    for (int c = lane; c < n4; c += 32) {
+        const int32_t* g = src + 4 * c;
+        int32_t v0 = g[o0], v1 = g[o1], v2 = g[o2], v3 = g[o3];  // v_k = word (k + rot) mod 4
+        if (rot & 2) {  // back to word order: swap the halves, then rotate right by one
+            const int32_t t0 = v0, t1 = v1;
+            v0 = v2;
+            v1 = v3;
+            v2 = t0;
+            v3 = t1;
+        }
+        if (rot & 1) {
+            const int32_t t = v3;
+            v3 = v2;
+            v2 = v1;
+            v1 = v0;
+            v0 = t;
+        }
+        d4[c] = make_int4(v0, v1, v2, v3);
+    }
+    const int base = n4 << 2, tail = len & 3;
+    if (lane < tail) dst[base + lane] = src[base + lane];
+}
+
 template <typename S, bool EMIT>
 __global__ void __launch_bounds__(kThreads, 4) k_tiles(TileArgs<S> a) {
     extern __shared__ __align__(16) unsigned char smem[];
@@ -589,15 +632,15 @@ __global__ void __launch_bounds__(kThreads, 4) k_tiles(TileArgs<S> a) {
     int32_t* lpos = lst;
     S* lend = reinterpret_cast<S*>(cnt);
     S* cstart = (sizeof(S) == 4) ? reinterpret_cast<S*>(msk) : reinterpret_cast<S*>(msk + cap);
-    __shared__ int s_tile, s_n, s_sum, s_nlnu, s_next;
+    __shared__ int s_tile, s_n, s_sum, s_nlnu, s_nlm, s_next;
     __shared__ int64_t s_cut[2];
     __shared__ int s_wsum[kWarpsPerCta];
     __shared__ S s_red[kWarpsPerCta], s_red2[kWarpsPerCta];
     __shared__ int32_t s_red3[kWarpsPerCta];
     __shared__ uint32_t s_bmask[kMaxBlocks];
     __shared__ int32_t s_boff[kMaxBlocks];
-    __shared__ int32_t s_lnu_pos[kLnu];
-    __shared__ S s_lnu_end[kLnu];
+    __shared__ int32_t s_lnu_idx[kLnu];  // long candidates ending before the run's max qs: their
+    __shared__ S s_lnu_end[kLnu];        // indices in the long list (ascending) and their ends
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int64_t X = a.split_len;
@@ -658,7 +701,9 @@ __global__ void __launch_bounds__(kThreads, 4) k_tiles(TileArgs<S> a) {
             const int64_t lo = a.seg[g];
             bool per_query = is_long && a.PL.ends == nullptr;
             const bool long_run = is_long && !per_query;
-            int nc = 0, nl = 0, nlnu = 0;
+            // nc candidates; nl of them long, the first nlm of which come from the tile's own
+            // gather (positions >= p_cut), the rest from the long-interval list; nlnu lnu entries
+            int nc = 0, nl = 0, nlnu = 0, nlm = 0;
             // count pass over an index without inverted intervals: the prepare pass counted every
             // query but those with start > end (from ranks)
             const bool rank_run = !EMIT && a.end_sorted != nullptr && !code_is_inverted(cw, a.G);
@@ -666,13 +711,13 @@ __global__ void __launch_bounds__(kThreads, 4) k_tiles(TileArgs<S> a) {
                 // a tile that is one run can reuse the candidate lists the count pass stored
                 const bool whole = (r0 == 0 && r1 == nt);
                 unsigned char* rec = (whole && a.cache) ? a.cache + (size_t)t * a.cache_stride : nullptr;
-                int32_t* g_cpos = reinterpret_cast<int32_t*>(rec + 16);
+                int32_t* g_cpos = reinterpret_cast<int32_t*>(rec + kCacheHeader);
                 S* g_cend = reinterpret_cast<S*>(g_cpos + cap);
                 S* g_cstart = g_cend + cap;
                 int32_t* g_lpos = reinterpret_cast<int32_t*>(g_cstart + cap);
                 S* g_lend = reinterpret_cast<S*>(g_lpos + cap);
-                int32_t* g_lnu_pos = reinterpret_cast<int32_t*>(g_lend + cap);
-                S* g_lnu_end = reinterpret_cast<S*>(g_lnu_pos + kLnu);
+                int32_t* g_lnu_idx = reinterpret_cast<int32_t*>(g_lend + cap);
+                S* g_lnu_end = reinterpret_cast<S*>(g_lnu_idx + kLnu);
                 bool cached = false;
                 if (EMIT && rec) {
                     if (tid == 0) {
@@ -680,12 +725,14 @@ __global__ void __launch_bounds__(kThreads, 4) k_tiles(TileArgs<S> a) {
                         s_n = hdr[3] == 1 ? hdr[0] : -1;
                         s_sum = hdr[1];
                         s_nlnu = hdr[2];
+                        s_nlm = hdr[4];
                     }
                     __syncthreads();
                     if (s_n >= 0) {
                         nc = s_n;
                         nl = s_sum;
                         nlnu = s_nlnu;
+                        nlm = s_nlm;
                         for (int k = tid; k < nc; k += kThreads) {
                             cpos[k] = g_cpos[k];
                             cend[k] = g_cend[k];
@@ -696,7 +743,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_tiles(TileArgs<S> a) {
                             lend[k] = g_lend[k];
                         }
                         for (int k = tid; k < nlnu && k < kLnu; k += kThreads) {
-                            s_lnu_pos[k] = g_lnu_pos[k];
+                            s_lnu_idx[k] = g_lnu_idx[k];
                             s_lnu_end[k] = g_lnu_end[k];
                         }
                         __syncthreads();
@@ -772,8 +819,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_tiles(TileArgs<S> a) {
                     }
                     per_query = nc < 0;
                     if (!per_query && nc > 0) {
-                        // long candidates (end - start >= X) into (lpos, lend), in order; the ones
-                        // ending before Q (possible misses for some query) also into the lnu list
+                        // long candidates (end - start >= X) into (lpos, lend), in order
                         const int nb = (nc + 31) >> 5;
                         for (int b = warp; b < nb; b += kWarpsPerCta) {
                             const int tt = (b << 5) + lane;
@@ -782,13 +828,6 @@ __global__ void __launch_bounds__(kThreads, 4) k_tiles(TileArgs<S> a) {
                                 const S st = a.starts[cpos[tt]];
                                 cstart[tt] = st;
                                 isl = is_long_iv<S>(st, cend[tt], X);
-                                if (isl && cend[tt] < Q) {
-                                    const int slot = atomicAdd(&s_nlnu, 1);
-                                    if (slot < kLnu) {
-                                        s_lnu_pos[slot] = cpos[tt];
-                                        s_lnu_end[slot] = cend[tt];
-                                    }
-                                }
                             }
                             const unsigned m = __ballot_sync(kFull, isl);
                             if (lane == 0) {
@@ -809,7 +848,34 @@ __global__ void __launch_bounds__(kThreads, 4) k_tiles(TileArgs<S> a) {
                             }
                         }
                         __syncthreads();
+                        // nlm: long candidates from the tile's own gather (positions >= p_cut).  The
+                        // lnu list: the others (from the long-interval list, at least 65536 long)
+                        // that end before Q, i.e. possible misses for some query, in long-list order
+                        // as their long-list indices (at most kLnu kept; a larger count makes every
+                        // query filter them)
+                        if (warp == 0) {
+                            int w = 0, nm = 0;
+                            for (int b0 = 0; b0 < nl; b0 += 32) {
+                                const int k = b0 + lane;
+                                const bool own = k < nl && (int64_t)lpos[k] >= pcut;
+                                const bool f = k < nl && !own && lend[k] < Q;
+                                const unsigned m = __ballot_sync(kFull, f);
+                                const int slot = w + __popc(m & lanemask_lt());
+                                if (f && slot < kLnu) {
+                                    s_lnu_idx[slot] = k;
+                                    s_lnu_end[slot] = lend[k];
+                                }
+                                w += __popc(m);
+                                nm += __popc(__ballot_sync(kFull, own));
+                            }
+                            if (lane == 0) {
+                                s_nlnu = w;
+                                s_nlm = nm;
+                            }
+                        }
+                        __syncthreads();
                         nlnu = s_nlnu;
+                        nlm = s_nlm;
                     }
                     if (!EMIT && rec) {
                         // store the lists for the emit pass (header last field: 1 = usable)
@@ -823,7 +889,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_tiles(TileArgs<S> a) {
                             g_lend[k] = lend[k];
                         }
                         for (int k = tid; k < nlnu && k < kLnu; k += kThreads) {
-                            g_lnu_pos[k] = s_lnu_pos[k];
+                            g_lnu_idx[k] = s_lnu_idx[k];
                             g_lnu_end[k] = s_lnu_end[k];
                         }
                         if (tid == 0) {
@@ -832,6 +898,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_tiles(TileArgs<S> a) {
                             hdr[1] = nl;
                             hdr[2] = nlnu;
                             hdr[3] = per_query ? 0 : 1;
+                            hdr[4] = nlm;
                         }
                     }
                 }
@@ -926,7 +993,9 @@ __global__ void __launch_bounds__(kThreads, 4) k_tiles(TileArgs<S> a) {
                             if (cpos[t] == u - (t - t0) && cend[t] >= qs) ++head;
                             else open = false;
                         }
-                        // part B: long candidates below the split are hits unless they end before qs
+                        // part B: long candidates below the split are hits unless they end before qs:
+                        // the tile's own ones are checked one by one, those from the long-interval
+                        // list are all hits but the lnu entries that end before qs
                         if (tsplit < nc && nl > 0) {
                             const int32_t psplit = cpos[tsplit];
                             int l0 = 0, l1 = nl;
@@ -935,13 +1004,15 @@ __global__ void __launch_bounds__(kThreads, 4) k_tiles(TileArgs<S> a) {
                                 if (lpos[mid] > psplit) l0 = mid + 1;
                                 else l1 = mid;
                             }
+                            const int b2 = max(l0, nlm);
+                            for (int k = l0; k < b2; ++k) c += lend[k] >= qs ? 1u : 0u;
                             if (nlnu <= kLnu) {
-                                int miss = 0;
+                                int miss = 0;  // lnu entries at or after b2
                                 for (int k = 0; k < nlnu; ++k)
-                                    miss += (s_lnu_pos[k] <= psplit && s_lnu_end[k] < qs) ? 1 : 0;
-                                c += (uint32_t)(nl - l0 - miss);
+                                    miss += (s_lnu_idx[k] >= b2 && s_lnu_end[k] < qs) ? 1 : 0;
+                                c += (uint32_t)(nl - b2 - miss);
                             } else {
-                                for (int k = l0; k < nl; ++k) c += lend[k] >= qs ? 1u : 0u;
+                                for (int k = b2; k < nl; ++k) c += lend[k] >= qs ? 1u : 0u;
                             }
                         }
                     }
@@ -954,7 +1025,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_tiles(TileArgs<S> a) {
                 for (int i = r0 + tid; i < r1; i += kThreads) {
                     const S qs = q_s[i];
                     const int32_t u = q_u[i];
-                    int ta = nc, tsplit = nc, lb = nl, flags = 0;
+                    int ta = nc, tsplit = nc, lb = nl;
                     if (a.end_sorted) q_h[i] = 0;  // no candidate: no head (set below otherwise)
                     if (u >= lo && nc > 0) {
                         int b0 = 0, b1 = nc;  // first candidate at or below u
@@ -1000,17 +1071,11 @@ __global__ void __launch_bounds__(kThreads, 4) k_tiles(TileArgs<S> a) {
                                 else l1 = mid;
                             }
                             lb = l0;
-                            if (nlnu > kLnu) {
-                                flags = 1;
-                            } else {
-                                for (int k = 0; k < nlnu; ++k)
-                                    if (s_lnu_pos[k] <= pb && s_lnu_end[k] < qs) flags = 1;
-                            }
                         }
                     }
                     q_ta[i] = ta;
                     q_tsplit[i] = tsplit;
-                    q_lb[i] = flags ? -1 - lb : lb;  // negative: some long candidate misses
+                    q_lb[i] = lb;
                 }
                 __syncthreads();
                 // the lists now only feed the writes: turn positions into the values written
@@ -1065,64 +1130,76 @@ __global__ void __launch_bounds__(kThreads, 4) k_tiles(TileArgs<S> a) {
                         room -= c;
                     }
                 }
-                // part B: the long candidates from lb on
-                const int lbf = q_lb[i];
-                const bool miss = lbf < 0;
-                const int lb = miss ? -1 - lbf : lbf;
-                if (!bad && lb < nl) {
-                    if (!miss) {
-                        const int len = nl - lb;
-                        if (len > room) {
-                            bad = true;
-                        } else {
-                            const int32_t* src = lpos + lb;
-                            int k = lane;
-                            for (; k + 32 < len; k += 64) {
-                                const int32_t v0 = src[k], v1 = src[k + 32];
-                                d[k] = v0;
-                                d[k + 32] = v1;
-                            }
-                            if (k < len) d[k] = src[k];
+                // part B: the long candidates from lb on.  Those of the tile's own gather ([lb, b2))
+                // are filtered one by one.  Those from the long-interval list ([b2, nl)) are all
+                // hits but the few lnu entries (ending before the run's largest qs) that end
+                // before this query's start: with the copy mode on, that section is copied as runs
+                // between those entries with 16-byte stores, else it is filtered too
+                const int lb = q_lb[i];
+                const int b2 = max(lb, nlm);
+                int fend = a.emit_copy && nlnu <= kLnu ? b2 : nl;  // filtered: [lb, fend)
+                for (int kk = lb; !bad && kk < fend; kk += 128) {
+                    // 128 candidates per round as four independent 32-wide slices, so their
+                    // shared-memory reads and ballots overlap instead of chaining
+                    bool hit[4];
+                    int32_t pv[4];
+                    unsigned m[4];
+#pragma unroll
+                    for (int s2 = 0; s2 < 4; ++s2) {
+                        const int tt = kk + 32 * s2 + lane;
+                        const bool in = tt < fend;
+                        hit[s2] = in && lend[tt] >= qs;
+                        pv[s2] = in ? lpos[tt] : 0;
+                    }
+#pragma unroll
+                    for (int s2 = 0; s2 < 4; ++s2) m[s2] = __ballot_sync(kFull, hit[s2]);
+                    const int c0 = __popc(m[0]), c1 = c0 + __popc(m[1]), c2 = c1 + __popc(m[2]);
+                    const int c = c2 + __popc(m[3]);
+                    if (c > room) {
+                        bad = true;
+                        break;
+                    }
+                    if (hit[0]) d[__popc(m[0] & lt)] = pv[0];
+                    if (hit[1]) d[c0 + __popc(m[1] & lt)] = pv[1];
+                    if (hit[2]) d[c1 + __popc(m[2] & lt)] = pv[2];
+                    if (hit[3]) d[c2 + __popc(m[3] & lt)] = pv[3];
+                    d += c;
+                    room -= c;
+                }
+                if (!bad && fend < nl) {
+                    // the long-interval list's section: misses are the lnu entries at or after b2
+                    // that end before qs, in long-list order
+                    unsigned mm[kLnu / 32];
+                    int nmiss = 0;
+#pragma unroll
+                    for (int j = 0; j < kLnu / 32; ++j) {
+                        mm[j] = 0u;
+                        if (32 * j < nlnu) {  // warp-uniform
+                            const int k = 32 * j + lane;
+                            const bool ms = k < nlnu && s_lnu_idx[k] >= b2 && s_lnu_end[k] < qs;
+                            mm[j] = __ballot_sync(kFull, ms);
+                            nmiss += __popc(mm[j]);
                         }
+                    }
+                    const int len = nl - b2 - nmiss;
+                    if (len > room) {
+                        bad = true;
                     } else {
-                        // 128 candidates per round as four independent 32-wide slices, so their
-                        // shared-memory reads and ballots overlap instead of chaining; only the
-                        // last round checks the list end
-                        for (int kk = lb; kk < nl; kk += 128) {
-                            bool hit[4];
-                            int32_t pv[4];
-                            unsigned m[4];
-                            if (kk + 128 <= nl) {
+                        int at = b2;
 #pragma unroll
-                                for (int s = 0; s < 4; ++s) {
-                                    const int tt = kk + 32 * s + lane;
-                                    hit[s] = lend[tt] >= qs;
-                                    pv[s] = lpos[tt];
-                                }
-                            } else {
-#pragma unroll
-                                for (int s = 0; s < 4; ++s) {
-                                    const int tt = kk + 32 * s + lane;
-                                    const bool in = tt < nl;
-                                    hit[s] = in && lend[tt] >= qs;
-                                    pv[s] = in ? lpos[tt] : 0;
-                                }
+                        for (int j = 0; j < kLnu / 32; ++j) {
+                            unsigned mj = mm[j];
+                            while (mj) {
+                                const int mi = s_lnu_idx[32 * j + __ffs(mj) - 1];
+                                mj &= mj - 1;
+                                warp_copy_s2g(d, lpos + at, mi - at, lane);
+                                d += mi - at;
+                                at = mi + 1;
                             }
-#pragma unroll
-                            for (int s = 0; s < 4; ++s) m[s] = __ballot_sync(kFull, hit[s]);
-                            const int c0 = __popc(m[0]), c1 = c0 + __popc(m[1]), c2 = c1 + __popc(m[2]);
-                            const int c = c2 + __popc(m[3]);
-                            if (c > room) {
-                                bad = true;
-                                break;
-                            }
-                            if (hit[0]) d[__popc(m[0] & lt)] = pv[0];
-                            if (hit[1]) d[c0 + __popc(m[1] & lt)] = pv[1];
-                            if (hit[2]) d[c1 + __popc(m[2] & lt)] = pv[2];
-                            if (hit[3]) d[c2 + __popc(m[3] & lt)] = pv[3];
-                            d += c;
-                            room -= c;
                         }
+                        warp_copy_s2g(d, lpos + at, nl - at, lane);
+                        d += nl - at;
+                        room -= len;
                     }
                 }
                 if (bad && lane == 0) atomicCAS(a.d_err, kDevOk, kDevOverflow);
@@ -1521,16 +1598,19 @@ __global__ void __launch_bounds__(kThreads) k_cov_ranks(const S* __restrict__ sq
     cov[id] = (S)(smin_sum - smax_sum);
 }
 
-// upper bounds in the original query order (plain path with an accelerator, tests).  With
-// one contig and the Eytzinger provider, each block first stages the tree in shared memory.
+// upper bounds in the original query order (plain path with an accelerator, tests).  With the
+// Eytzinger provider each block first stages the top `top_n` slots (whole levels) of every
+// contig's tree in shared memory; the descent continues in global memory below them.
 template <typename S>
 __global__ void k_ub_plain(const S* __restrict__ qe, const int32_t* __restrict__ qc, int64_t nq,
-                           MapView<S> m, UbView<S> U, int32_t* __restrict__ out, int* d_err) {
+                           MapView<S> m, UbView<S> U, int32_t* __restrict__ out, int* d_err, int top_n) {
     extern __shared__ __align__(16) unsigned char smem[];
-    S* tree = reinterpret_cast<S*>(smem);
-    const bool staged = U.mode == 1 && m.G == 1 && U.eytz_n > 1;
-    if (staged) {
-        for (int i = threadIdx.x; i < U.eytz_n; i += blockDim.x) tree[i] = U.eytz_keys[i];
+    S* top = reinterpret_cast<S*>(smem);
+    if (U.mode == 1 && top_n > 0) {
+        for (int64_t i = threadIdx.x; i < (int64_t)m.G * top_n; i += blockDim.x) {
+            const int64_t g = i / top_n, k = i - g * top_n;
+            top[i] = U.eytz_keys[g * U.eytz_n + k];
+        }
         __syncthreads();
     }
     const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -1542,8 +1622,23 @@ __global__ void k_ub_plain(const S* __restrict__ qe, const int32_t* __restrict__
         return;
     }
     const int64_t lo = m.seg[g], n = m.seg[g + 1] - lo;
-    const S* tr = (U.mode == 1) ? (staged ? tree : U.eytz_keys + (int64_t)g * U.eytz_n) : nullptr;
-    out[q] = (int32_t)ub_search(U, g, m.starts + lo, n, qe[q], tr);
+    const S* tr = (U.mode == 1) ? U.eytz_keys + (int64_t)g * U.eytz_n : nullptr;
+    out[q] = (int32_t)ub_search(U, g, m.starts + lo, n, qe[q], tr, top + (int64_t)g * top_n, (int64_t)top_n);
+}
+
+// Upper bounds of sorted queries back to the original order: contig-local position or -1.
+__global__ void k_ub_scatter(const int32_t* __restrict__ sq_u, const uint32_t* __restrict__ sq_c,
+                             const int32_t* __restrict__ sq_id, int64_t nq, const int64_t* __restrict__ seg, int G,
+                             int32_t* __restrict__ out) {
+    const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= nq) return;
+    const uint32_t c = sq_c[j];
+    const int32_t id = sq_id[j];
+    if (c >= 3u * (uint32_t)G) {  // a contig outside [0, G): reported by the prepare kernel
+        out[id] = -1;
+        return;
+    }
+    out[id] = sq_u[j] - (int32_t)seg[code_contig(c, G)];
 }
 
 // ---- learned upper-bound model: GPU least squares ---------------------------------------
@@ -1595,79 +1690,70 @@ __global__ void k_leaf_keys(const S* __restrict__ starts, const int64_t* __restr
     leaf_key[L] = n > 0 ? starts[lo + leaf_pos[L]] : Lim<S>::lo;
 }
 
+// One warp per leaf: mean key, least-squares slope of position on key, then the leaf's max
+// errors under that line (the same prediction formula as the query, ub_search).
 template <typename S>
-__global__ void k_leaf_fit(const S* __restrict__ starts, const int64_t* __restrict__ seg,
-                           const int32_t* __restrict__ leaf_contig, const int32_t* __restrict__ leaf_base,
-                           const int32_t* __restrict__ bnd, const double* __restrict__ mean_x,
-                           LeafModel* __restrict__ leaves, int total) {
-    __shared__ double red[32];
-    __shared__ int ired[2][32];
-    for (int L = blockIdx.x; L < total; L += gridDim.x) {
-        const int g = leaf_contig[L];
-        const int64_t lo = seg[g];
-        const int l = L - leaf_base[g];
-        const int nl = leaf_base[g + 1] - leaf_base[g];
-        const int64_t a = bnd[L];
-        const int64_t b = (l + 1 < nl) ? (int64_t)bnd[L + 1] : (seg[g + 1] - lo);
-        const int64_t cnt = b - a;
-        LeafModel M;
-        if (cnt <= 0) {
-            if (threadIdx.x == 0) {
-                M.x0 = 0;
-                M.slope = 0;
-                M.y0 = (double)a;
-                M.err_lo = 1;
-                M.err_hi = 1;
-                leaves[L] = M;
-            }
-            __syncthreads();
-            continue;
-        }
-        double sx = 0;
-        for (int64_t k = a + threadIdx.x; k < b; k += blockDim.x) sx += (double)starts[lo + k] - mean_x[g];
-        sx = block_sum(sx, red);
-        const double x0 = sx / (double)cnt;
-        const double y0 = 0.5 * (double)(a + b - 1);
-        double sxy = 0, sxx = 0;
-        for (int64_t k = a + threadIdx.x; k < b; k += blockDim.x) {
-            const double dx = (double)starts[lo + k] - mean_x[g] - x0, dy = (double)k - y0;
-            sxy += dx * dy;
-            sxx += dx * dx;
-        }
-        sxy = block_sum(sxy, red);
-        sxx = block_sum(sxx, red);
-        const double slope = (sxx > 0.0 && sxy > 0.0) ? sxy / sxx : 0.0;
-        int elo = 0, ehi = 0;
-        for (int64_t k = a + threadIdx.x; k < b; k += blockDim.x) {
-            const double pred = y0 + slope * ((double)starts[lo + k] - mean_x[g] - x0);
-            const double e = (double)k - pred;
-            if (e > 0) ehi = max(ehi, (int)ceil(e));
-            else elo = max(elo, (int)ceil(-e));
-        }
-#pragma unroll
-        for (int d = 16; d > 0; d >>= 1) {
-            elo = max(elo, __shfl_xor_sync(kFull, elo, d));
-            ehi = max(ehi, __shfl_xor_sync(kFull, ehi, d));
-        }
-        __syncthreads();
-        if ((threadIdx.x & 31) == 0) {
-            ired[0][threadIdx.x >> 5] = elo;
-            ired[1][threadIdx.x >> 5] = ehi;
-        }
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            for (int w = 1; w < (int)(blockDim.x >> 5); ++w) {
-                elo = max(elo, ired[0][w]);
-                ehi = max(ehi, ired[1][w]);
-            }
-            M.x0 = x0;
-            M.slope = slope;
-            M.y0 = y0;
-            M.err_lo = elo;
-            M.err_hi = ehi;
+__global__ void __launch_bounds__(kThreads) k_leaf_fit(const S* __restrict__ starts, const int64_t* __restrict__ seg,
+                                                       const int32_t* __restrict__ leaf_contig,
+                                                       const int32_t* __restrict__ leaf_base,
+                                                       const int32_t* __restrict__ bnd, const double* __restrict__ mean_x,
+                                                       LeafModel* __restrict__ leaves, int total) {
+    const int lane = threadIdx.x & 31;
+    const int L = (int)(((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    if (L >= total) return;  // warp-uniform
+    const int g = leaf_contig[L];
+    const int64_t lo = seg[g];
+    const int l = L - leaf_base[g];
+    const int nl = leaf_base[g + 1] - leaf_base[g];
+    const int64_t a = bnd[L];
+    const int64_t b = (l + 1 < nl) ? (int64_t)bnd[L + 1] : (seg[g + 1] - lo);
+    const int64_t cnt = b - a;
+    LeafModel M;
+    if (cnt <= 0) {
+        if (lane == 0) {
+            M.x0 = 0;
+            M.slope = 0;
+            M.y0 = (double)a;
+            M.err_lo = 1;
+            M.err_hi = 1;
             leaves[L] = M;
         }
-        __syncthreads();
+        return;
+    }
+    const double mx = mean_x[g];
+    double sx = 0;
+    for (int64_t k = a + lane; k < b; k += 32) sx += (double)starts[lo + k] - mx;
+    sx = warp_sum(sx);
+    const double x0 = sx / (double)cnt;
+    const double y0 = 0.5 * (double)(a + b - 1);
+    double sxy = 0, sxx = 0;
+    for (int64_t k = a + lane; k < b; k += 32) {
+        const double dx = (double)starts[lo + k] - mx - x0, dy = (double)k - y0;
+        sxy += dx * dy;
+        sxx += dx * dx;
+    }
+    sxy = warp_sum(sxy);
+    sxx = warp_sum(sxx);
+    const double slope = (sxx > 0.0 && sxy > 0.0) ? sxy / sxx : 0.0;
+    int elo = 0, ehi = 0;
+    for (int64_t k = a + lane; k < b; k += 32) {
+        const double pred = y0 + slope * ((double)starts[lo + k] - mx - x0);
+        const double e = (double)k - pred;
+        if (e > 0) ehi = max(ehi, (int)ceil(e));
+        else elo = max(elo, (int)ceil(-e));
+    }
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) {
+        elo = max(elo, __shfl_xor_sync(kFull, elo, d));
+        ehi = max(ehi, __shfl_xor_sync(kFull, ehi, d));
+    }
+    if (lane == 0) {
+        M.x0 = x0;
+        M.slope = slope;
+        M.y0 = y0;
+        M.err_lo = elo;
+        M.err_hi = ehi;
+        leaves[L] = M;
     }
 }
 
@@ -1783,7 +1869,7 @@ int build_learned(BatchedWorkspace& ws, MapView<S> m, cudaStream_t st) {
                                                      total, ws.ub.leaf_key.as<S>());
     note_launch();
     SI_CU(cudaGetLastError());
-    k_leaf_fit<S><<<(unsigned)std::min(total, 152 * 32), kThreads, 0, st>>>(
+    k_leaf_fit<S><<<nblk((int64_t)total * 32), kThreads, 0, st>>>(
         m.starts, m.seg, lc.as<int32_t>(), ws.ub.leaf_base.as<int32_t>(), ws.ub.leaf_pos.as<int32_t>(),
         ws.ub.key_mean.as<double>(), ws.ub.leaves.as<LeafModel>(), total);
     note_launch();
@@ -1834,7 +1920,7 @@ int batched_prepare(BatchedWorkspace& ws, MapView<S> m, Levels<S>, int, const in
 
 template <typename S>
 int batched_prepare_queries(BatchedWorkspace& ws, MapView<S> m, const QueryBatch& q, int* d_err, int ub_mode,
-                            cudaStream_t st, uint32_t* counts) {
+                            cudaStream_t st, uint32_t* counts, bool tile_cuts) {
     const int64_t nq = q.nq;
     ws.prepared_nq = -1;
     if (nq <= 0) return SI_OK;
@@ -1912,7 +1998,7 @@ int batched_prepare_queries(BatchedWorkspace& ws, MapView<S> m, const QueryBatch
     bool in_alt = false;
     int passes = 0;
     SI_CU(radix_sort(kp, ka, ws.pay.as<uint32_t>(), ws.palt.as<uint32_t>(), Kp, nq, ws.sort_tmp.p, tb, &in_alt,
-                     &passes, st, ws.capturing ? 0x7u : 0u));
+                     &passes, st, ws.capturing ? 0x7u : 0u, d_err));
     const uint32_t* spay = in_alt ? ws.palt.as<uint32_t>() : ws.pay.as<uint32_t>();
     const uint32_t* swc = in_alt ? ka[Kp - 1] : kp[Kp - 1];
     UbView<S> U = make_ub<S>(ws, ub_mode);
@@ -1921,11 +2007,12 @@ int batched_prepare_queries(BatchedWorkspace& ws, MapView<S> m, const QueryBatch
                                               static_cast<const S*>(q.qe), packed ? ws.qpair.as<S>() : nullptr,
                                               nq, m, U, ws.sq_s.as<S>(), ws.sq_u.as<int32_t>(),
                                               ws.sq_c.as<uint32_t>(), ws.sq_id.as<int32_t>(), d_err, ws.long_split,
-                                              ws.long_pos, ws.long_seg, ws.long_pos ? ws.blk_cut.as<int64_t>() : nullptr,
+                                              ws.long_pos, ws.long_seg,
+                                              (tile_cuts && ws.long_pos) ? ws.blk_cut.as<int64_t>() : nullptr,
                                               static_cast<const S*>(ws.end_sorted), counts);
     note_launch();
     SI_CU(cudaGetLastError());
-    ws.launches += 2 + 3 * passes + 1;
+    ws.launches += 2 + 2 + passes + 1;  // keys, min/max, histogram, digit offsets, passes, prepare
     ws.prepared_qs = q.qs;
     ws.prepared_nq = nq;
     ws.prepared_mode = ub_mode;
@@ -1975,6 +2062,7 @@ static int run_tiles(BatchedWorkspace& ws, MapView<S> m, Levels<S> L, int H, int
     a.out_base = out_base;
     a.order = order;
     a.values = values;
+    a.emit_copy = prm.emit_copy;
     a.out = out;
     a.d_err = d_err;
     a.cache = (use_cache && ws.cache_ok) ? ws.tile_cache.as<unsigned char>() : nullptr;
@@ -2022,7 +2110,7 @@ int batched_count(BatchedWorkspace& ws, MapView<S> m, Levels<S> L, int H, const 
     }
     // room for every tile's candidate lists, so that the emit pass need not gather again;
     // without room (device budget) the emit pass simply gathers again
-    ws.cache_stride = (int64_t)round_up(16 + (int64_t)ws.prm.cap * (8 + 3 * (int64_t)sizeof(S)) +
+    ws.cache_stride = (int64_t)round_up(kCacheHeader + (int64_t)ws.prm.cap * (8 + 3 * (int64_t)sizeof(S)) +
                                             (int64_t)kLnu * (4 + (int64_t)sizeof(S)), 256);
     const int64_t n_tiles = ceil_div(nq, ws.prm.tile_q);
     ws.cache_ok = ws.tile_cache.reserve((size_t)(n_tiles * ws.cache_stride)) == SI_OK;
@@ -2067,13 +2155,34 @@ int batched_emit(BatchedWorkspace& ws, MapView<S> m, Levels<S> L, int H, const Q
 
 template <typename S>
 int upper_bounds(BatchedWorkspace& ws, MapView<S> m, const QueryBatch& q, int ub_mode, int32_t* out, int* d_err,
-                 cudaStream_t st) {
+                 cudaStream_t st, bool sorted) {
     if (q.nq <= 0) return SI_OK;
+    if (sorted) {
+        QueryBatch qq = q;
+        qq.qs = q.qe;  // queries [qe, qe]: one class per contig, the sort key is the end
+        SI_OKR(batched_prepare_queries<S>(ws, m, qq, d_err, ub_mode, st, nullptr, false));
+        k_ub_scatter<<<nblk(q.nq), kThreads, 0, st>>>(ws.sq_u.as<int32_t>(), ws.sq_c.as<uint32_t>(),
+                                                      ws.sq_id.as<int32_t>(), q.nq, m.seg, m.G, out);
+        note_launch();
+        SI_CU(cudaGetLastError());
+        ws.launches += 1;
+        // the sorted records hold (qe, qe) queries: no search may take them as its own
+        ws.prepared_nq = -1;
+        ws.prepared_qs = nullptr;
+        return SI_OK;
+    }
     UbView<S> U = make_ub<S>(ws, ub_mode);
-    const size_t sm = (U.mode == 1 && m.G == 1 && U.eytz_n > 1) ? sizeof(S) * (size_t)U.eytz_n : 0;
-    if (sm > 48 * 1024)
-        SI_CU(cudaFuncSetAttribute(k_ub_plain<S>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-    k_ub_plain<S><<<nblk(q.nq), kThreads, sm, st>>>(static_cast<const S*>(q.qe), q.qc, q.nq, m, U, out, d_err);
+    // the tree's top levels of every contig that fit 48 KiB of shared memory (2^d slots each,
+    // d <= the tree's depth)
+    int top_n = 0;
+    if (U.mode == 1 && U.eytz_n > 1) {
+        top_n = U.eytz_n;
+        while (top_n > 1 && (size_t)top_n * sizeof(S) * (size_t)m.G > 48 * 1024) top_n >>= 1;
+        if (top_n <= 1) top_n = 0;
+    }
+    const size_t sm = sizeof(S) * (size_t)top_n * (size_t)m.G;
+    k_ub_plain<S><<<nblk(q.nq), kThreads, sm, st>>>(static_cast<const S*>(q.qe), q.qc, q.nq, m, U, out, d_err,
+                                                    top_n);
     note_launch();
     SI_CU(cudaGetLastError());
     ws.launches += 1;
@@ -2100,14 +2209,14 @@ int batched_coverage(BatchedWorkspace& ws, MapView<S> m, const QueryBatch& q, co
     template int batched_prepare<S>(BatchedWorkspace&, MapView<S>, Levels<S>, int, const int64_t*, int,            \
                                     cudaStream_t);                                                              \
     template int batched_prepare_queries<S>(BatchedWorkspace&, MapView<S>, const QueryBatch&, int*, int,          \
-                                            cudaStream_t, uint32_t*);                                                      \
+                                            cudaStream_t, uint32_t*, bool);                                                \
     template int batched_count<S>(BatchedWorkspace&, MapView<S>, Levels<S>, int, const QueryBatch&, uint32_t*,   \
                                   int*, cudaStream_t);                                                          \
     template int batched_emit<S>(BatchedWorkspace&, MapView<S>, Levels<S>, int, const QueryBatch&, int64_t,      \
                                  const int64_t*, int64_t, int, bool, int32_t*, int*, int, cudaStream_t,         \
                                  int64_t);                                                                      \
     template int upper_bounds<S>(BatchedWorkspace&, MapView<S>, const QueryBatch&, int, int32_t*, int*,          \
-                                 cudaStream_t);                                                                 \
+                                 cudaStream_t, bool);                                                           \
     template int batched_coverage<S>(BatchedWorkspace&, MapView<S>, const QueryBatch&, const uint64_t*,         \
                                      const uint64_t*, uint64_t*, S*, int*, int, cudaStream_t);
 SIG_BINST(int32_t)

@@ -29,6 +29,9 @@ struct BatchedParams {
     int64_t long_len = 16384;    // queries longer than this take the per-query walk
     int64_t split_len = 2048;    // candidates at least this long form the tile's long list
     int eytz_depth = 0;          // 0: automatic
+    // emit: copy the section of a tile's long candidates that comes from the long-interval list
+    // (all hits but a few) as runs with 16-byte stores instead of filtering each candidate
+    bool emit_copy = true;
     // pick tile_q per batch (emit without a count-pass cache) from the batch's intervals per
     // query and hits per query, so that a tile's candidates fit its shared memory
     bool auto_tile = true;
@@ -115,9 +118,10 @@ int batched_prepare(BatchedWorkspace& ws, MapView<S> m, Levels<S> L, int H, cons
 // Sorts the queries by (class, contig, end) and finds each one's upper bound.  With counts and
 // an index that keeps its sorted ends (no interval has start > end), also writes the count of
 // every short query (the count pass then handles the long ones only).
+// tile_cuts: also record each 256-query block's long-list cut for the tiles (search paths).
 template <typename S>
 int batched_prepare_queries(BatchedWorkspace& ws, MapView<S> m, const QueryBatch& q, int* d_err,
-                            int ub_mode, cudaStream_t st, uint32_t* counts = nullptr);
+                            int ub_mode, cudaStream_t st, uint32_t* counts = nullptr, bool tile_cuts = true);
 template <typename S>
 int batched_count(BatchedWorkspace& ws, MapView<S> m, Levels<S> L, int H, const QueryBatch& q,
                   uint32_t* counts, int* d_err, cudaStream_t st);
@@ -136,10 +140,13 @@ template <typename S>
 int batched_coverage(BatchedWorkspace& ws, MapView<S> m, const QueryBatch& q, const uint64_t* ps_start,
                      const uint64_t* ps_end, uint64_t* count, S* cov, int* d_err, int ub_mode, cudaStream_t st);
 
-// Upper bound of every query (original order) with the handle's accelerator; used by
-// the plain path when a learned / Eytzinger mode is selected, and by tests.
+// Upper bound of every query end (original order) with the handle's accelerator.  Per query
+// (one thread each, in the batch's order), or, with sorted, through the batched path's
+// preparation: the ends are radix-sorted, each block of 256 sorted ends searches only its
+// smallest and largest end and resolves the rest in a shared-memory window of starts, and the
+// answers are scattered back to the original order.
 template <typename S>
 int upper_bounds(BatchedWorkspace& ws, MapView<S> m, const QueryBatch& q, int ub_mode, int32_t* out,
-                 int* d_err, cudaStream_t st);
+                 int* d_err, cudaStream_t st, bool sorted = false);
 
 }  // namespace sig

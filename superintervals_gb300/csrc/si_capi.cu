@@ -314,7 +314,9 @@ int build_impl(gSuperIntervals* si) {
         si->built = true;
         return SI_OK;
     }
-    DevBuf s_in, e_in, d_in, flag;
+    DevBuf s_in, e_in, d_in, flag, berr;
+    SI_TRY(berr.reserve(sizeof(int)));  // bounded waits of the one-sweep sorts and scans
+    SI_CK(cudaMemsetAsync(berr.p, 0, sizeof(int), st));
     SI_TRY(s_in.reserve(sizeof(S) * n));
     SI_TRY(e_in.reserve(sizeof(S) * n));
     SI_TRY(d_in.reserve(sizeof(int32_t) * n));
@@ -352,7 +354,7 @@ int build_impl(gSuperIntervals* si) {
                                        pay.as<uint32_t>(), st));
         bool in_alt = false;
         SI_CK(sig::radix_sort(kp, ka, pay.as<uint32_t>(), palt.as<uint32_t>(), K, n, tmp.p, tb,
-                              &in_alt, &si->sort_passes, st));
+                              &in_alt, &si->sort_passes, st, 0, berr.as<int>()));
         uint32_t* const* res_k = in_alt ? ka : kp;
         const uint32_t* res_p = in_alt ? palt.as<uint32_t>() : pay.as<uint32_t>();
         SI_CK(sig::launch_decode<S>(res_k, res_p, d_in.as<int32_t>(), n, n_pad, si->starts.as<S>(),
@@ -376,7 +378,7 @@ int build_impl(gSuperIntervals* si) {
         SI_TRY(tmp.reserve(sig::scan_temp_bytes(n)));
         SI_CK(sig::launch_long_flags<S>(si->starts.as<S>(), ends, n, sig::kLongIntervalSplit, flags.as<uint32_t>(),
                                         st));
-        SI_CK(sig::exclusive_scan_u32_to_i64(flags.as<uint32_t>(), offs.as<int64_t>(), n, tmp.p, st));
+        SI_CK(sig::exclusive_scan_u32_to_i64(flags.as<uint32_t>(), offs.as<int64_t>(), n, tmp.p, st, berr.as<int>()));
         int64_t n_long = 0;
         SI_CK(cudaMemcpyAsync(&n_long, offs.as<int64_t>() + n, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
         SI_CK(cudaStreamSynchronize(st));
@@ -430,7 +432,7 @@ int build_impl(gSuperIntervals* si) {
         bool in_alt = false;
         int passes = 0;
         SI_CK(sig::radix_sort(kp, ka, pay.as<uint32_t>(), palt.as<uint32_t>(), K, n, tmp.p, tb, &in_alt, &passes,
-                              st));
+                              st, 0, berr.as<int>()));
         SI_TRY(si->end_sorted.reserve(sizeof(S) * n_pad));
         SI_CK(sig::launch_end_decode<S>(in_alt ? ka : kp, n, n_pad, si->end_sorted.as<S>(), st));
         SI_CK(cudaStreamSynchronize(st));  // the temporaries are released on scope exit
@@ -440,6 +442,11 @@ int build_impl(gSuperIntervals* si) {
                                    si->ub_mode, st));
     SI_CK(cudaStreamSynchronize(st));
     SI_CK(cudaGetLastError());
+    {
+        int be = 0;
+        SI_CK(cudaMemcpy(&be, berr.p, sizeof(int), cudaMemcpyDeviceToHost));
+        if (be) return fail(SI_ERR_CUDA, "build: a bounded wait in a sort or scan kernel gave up (%d)", be);
+    }
     si->built = true;
     return SI_OK;
 }
@@ -458,6 +465,7 @@ int read_dev_err(gSuperIntervals* si, cudaStream_t st = nullptr) {
     SI_CK(cudaStreamSynchronize(st));
     if (e == sig::kDevBadContig) return fail(SI_ERR_INVALID, "a query names a contig outside [0, %d)", si->G);
     if (e == sig::kDevOverflow) return fail(SI_ERR_CUDA, "internal: emit overran its offsets");
+    if (e == sig::kDevTimeout) return fail(SI_ERR_CUDA, "a bounded wait in a sort or scan kernel gave up");
     if (e != 0) return fail(SI_ERR_CUDA, "device error word %d", e);
     return SI_OK;
 }
@@ -524,7 +532,7 @@ int search_device(gSuperIntervals* si, const sig::QueryBatch& q, int order, bool
     SI_TRY(run_count<S>(si, q, si->w_counts.as<uint32_t>(), st));
     {
         PhaseTimer pt(si, 1, st);
-        SI_CK(sig::exclusive_scan_u32_to_i64(si->w_counts.as<uint32_t>(), d_offsets, q.nq, si->w_tmp.p, st));
+        SI_CK(sig::exclusive_scan_u32_to_i64(si->w_counts.as<uint32_t>(), d_offsets, q.nq, si->w_tmp.p, st, si->w_err.as<int>()));
     }
     int64_t P = 0;
     SI_CK(cudaMemcpyAsync(&P, d_offsets + q.nq, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
@@ -586,7 +594,7 @@ int search_host(gSuperIntervals* si, const S* qs, const S* qe, const int32_t* qc
     int64_t* d_off = si->w_offsets.as<int64_t>();
     {
         PhaseTimer pt(si, 1, st);
-        SI_CK(sig::exclusive_scan_u32_to_i64(si->w_counts.as<uint32_t>(), d_off, (int64_t)nq, si->w_tmp.p, st));
+        SI_CK(sig::exclusive_scan_u32_to_i64(si->w_counts.as<uint32_t>(), d_off, (int64_t)nq, si->w_tmp.p, st, si->w_err.as<int>()));
     }
     SI_CK(cudaMemcpyAsync(h_off, d_off, sizeof(int64_t) * (nq + 1), cudaMemcpyDeviceToHost, st));
     SI_CK(cudaStreamSynchronize(st));
@@ -1105,9 +1113,13 @@ extern "C" int upperBoundDeviceGpu(gSuperIntervals* si, const void* d_qe, const 
         return SI_OK;
     }
     sig::QueryBatch q{d_qe, d_qe, d_qc, (int64_t)nq};
+    // the batched query path sorts the ends first (same answers): see setQueryPathGpu
+    const bool sorted = use_batched(si, (int64_t)nq);
     int r = si->bits == 64
-                ? sig::upper_bounds<int64_t>(si->bws, view<int64_t>(si), q, mode, d_out, si->w_err.as<int>(), st)
-                : sig::upper_bounds<int32_t>(si->bws, view<int32_t>(si), q, mode, d_out, si->w_err.as<int>(), st);
+                ? sig::upper_bounds<int64_t>(si->bws, view<int64_t>(si), q, mode, d_out, si->w_err.as<int>(), st,
+                                             sorted)
+                : sig::upper_bounds<int32_t>(si->bws, view<int32_t>(si), q, mode, d_out, si->w_err.as<int>(), st,
+                                             sorted);
     if (r != SI_OK) return fail(r, "upper-bound kernel failed");
     return SI_OK;
 }
@@ -1140,6 +1152,30 @@ extern "C" int getBatchedParamsGpu(const gSuperIntervals* si, int* tile_q, int* 
     if (cap) *cap = si->bws.prm.cap;
     if (long_len) *long_len = si->bws.prm.long_len;
     if (split_len) *split_len = si->bws.prm.split_len;
+    return SI_OK;
+}
+
+extern "C" int setBatchedOptionGpu(gSuperIntervals* si, int option, int64_t value) {
+    if (!si) return fail(SI_ERR_INVALID, "null handle");
+    if (option == SI_OPT_EMIT_COPY) {
+        si->bws.prm.emit_copy = value != 0;
+        return SI_OK;
+    }
+    if (option == SI_OPT_EYTZ_DEPTH) {
+        if (value < 0 || value > 13) return fail(SI_ERR_INVALID, "Eytzinger depth %lld outside [0, 13]", (long long)value);
+        si->bws.prm.eytz_depth = (int)value;
+        // the tree is sampled at build time: rebuild it when it is the current provider
+        if (si->built && si->ub_mode == SI_UB_EYTZINGER) return setUpperBoundModeGpu(si, SI_UB_EYTZINGER);
+        return SI_OK;
+    }
+    return fail(SI_ERR_INVALID, "unknown option %d", option);
+}
+
+extern "C" int getBatchedOptionGpu(const gSuperIntervals* si, int option, int64_t* value) {
+    if (!si || !value) return fail(SI_ERR_INVALID, "null argument");
+    if (option == SI_OPT_EMIT_COPY) *value = si->bws.prm.emit_copy ? 1 : 0;
+    else if (option == SI_OPT_EYTZ_DEPTH) *value = si->bws.ub.eytz_depth > 0 ? si->bws.ub.eytz_depth : si->bws.prm.eytz_depth;
+    else return fail(SI_ERR_INVALID, "unknown option %d", option);
     return SI_OK;
 }
 
@@ -1332,12 +1368,18 @@ extern "C" int autotuneBatchedGpu(gSuperIntervals* si, const void* d_qs, const v
         return status;
     }
     int trials = 1;
+    // set parameters and provider; the provider's structure is rebuilt when the provider or the
+    // Eytzinger depth changes
+    auto apply = [&](const sig::BatchedParams& p, int ub) -> bool {
+        const bool rebuild = ub != si->ub_mode || (ub == SI_UB_EYTZINGER && p.eytz_depth != si->bws.prm.eytz_depth);
+        si->bws.prm = p;
+        return !rebuild || setUpperBoundModeGpu(si, ub) == SI_OK;
+    };
     auto try_params = [&](const sig::BatchedParams& p, int ub) {
         const sig::BatchedParams keep = si->bws.prm;
         const int keep_ub = si->ub_mode;
-        si->bws.prm = p;
-        if (ub != si->ub_mode && setUpperBoundModeGpu(si, ub) != SI_OK) {
-            si->bws.prm = keep;
+        if (!apply(p, ub)) {
+            apply(keep, keep_ub);
             return;
         }
         int s = SI_OK;
@@ -1350,8 +1392,7 @@ extern "C" int autotuneBatchedGpu(gSuperIntervals* si, const void* d_qs, const v
             best = p;
             best_ub = ub;
         } else {
-            si->bws.prm = keep;
-            if (si->ub_mode != keep_ub) setUpperBoundModeGpu(si, keep_ub);
+            apply(keep, keep_ub);
         }
     };
     if (!(flags & SI_TUNE_KEEP_UPPER_BOUND))
@@ -1376,16 +1417,27 @@ extern "C" int autotuneBatchedGpu(gSuperIntervals* si, const void* d_qs, const v
             p.split_len = x;
             try_params(p, best_ub);
         }
-    si->bws.prm = best;
-    if (si->ub_mode != best_ub) SI_TRY(setUpperBoundModeGpu(si, best_ub));
+    {  // how the emit writes the long-interval list's section of part B
+        sig::BatchedParams p = best;
+        p.emit_copy = !best.emit_copy;
+        try_params(p, best_ub);
+    }
+    if (best_ub == SI_UB_EYTZINGER)  // depth of the Eytzinger tree (the shared-memory top levels)
+        for (int dpt : {7, 10, 13})
+            if (dpt != si->bws.ub.eytz_depth) {
+                sig::BatchedParams p = best;
+                p.eytz_depth = dpt;
+                try_params(p, best_ub);
+            }
+    if (!apply(best, best_ub)) return fail(SI_ERR_CUDA, "autotune: restoring the chosen provider failed");
     si->path = saved_path;
     if (report && report_len) {
         snprintf(report, report_len,
                  "{\"upper_bound\": %d, \"tile_queries\": %d, \"tile_auto\": %d, \"tile_candidates\": %d, "
-                 "\"split_len\": %lld, \"long_query_len\": %lld, \"sample_queries\": %zu, \"sample_ms\": %.4f, "
-                 "\"trials\": %d}",
+                 "\"split_len\": %lld, \"long_query_len\": %lld, \"emit_copy\": %d, \"eytz_depth\": %d, "
+                 "\"sample_queries\": %zu, \"sample_ms\": %.4f, \"trials\": %d}",
                  best_ub, best.tile_q, best.auto_tile ? 1 : 0, best.cap, (long long)best.split_len,
-                 (long long)best.long_len, ns, best_ms, trials);
+                 (long long)best.long_len, best.emit_copy ? 1 : 0, best.eytz_depth, ns, best_ms, trials);
     }
     return SI_OK;
 }
@@ -1409,7 +1461,7 @@ int capture_plain(gSuperIntervals* si, const sig::QueryBatch& q, int order, int6
     cudaError_t e = cudaMemsetAsync(si->w_err.p, 0, sizeof(int), st);
     if (e == cudaSuccess) e = sig::launch_count_plain<S>(view<S>(si), q, si->w_counts.as<uint32_t>(), si->w_err.as<int>(), st);
     if (e == cudaSuccess)
-        e = sig::exclusive_scan_u32_to_i64(si->w_counts.as<uint32_t>(), d_offsets, q.nq, si->w_tmp.p, st);
+        e = sig::exclusive_scan_u32_to_i64(si->w_counts.as<uint32_t>(), d_offsets, q.nq, si->w_tmp.p, st, si->w_err.as<int>());
     if (e == cudaSuccess)
         e = sig::launch_emit_plain<S>(view<S>(si), q, d_offsets, 0, order, false, d_values, si->w_err.as<int>(), st,
                                       (int64_t)capacity);
@@ -1459,7 +1511,7 @@ int capture_batched(gSuperIntervals* si, const sig::QueryBatch& q, int order, in
     int r = run_count<S>(si, q, si->w_counts.as<uint32_t>(), st);
     cudaError_t e = cudaSuccess;
     if (r == SI_OK)
-        e = sig::exclusive_scan_u32_to_i64(si->w_counts.as<uint32_t>(), d_offsets, nq, si->w_tmp.p, st);
+        e = sig::exclusive_scan_u32_to_i64(si->w_counts.as<uint32_t>(), d_offsets, nq, si->w_tmp.p, st, si->w_err.as<int>());
     if (r == SI_OK && e == cudaSuccess)
         r = run_emit<S>(si, q, 0, d_offsets, 0, order, false, d_values, st, (int64_t)tot);
     ws.capturing = false;
@@ -1556,7 +1608,7 @@ int hit_lists(gSuperIntervals* si, const sig::QueryBatch& q, int order, cudaStre
     SI_TRY(si->w_tmp.reserve(sig::scan_temp_bytes(q.nq)));
     SI_TRY(run_count<S>(si, q, si->w_counts.as<uint32_t>(), st));
     SI_CK(sig::exclusive_scan_u32_to_i64(si->w_counts.as<uint32_t>(), si->so_hoff.as<int64_t>(), q.nq, si->w_tmp.p,
-                                         st));
+                                         st, si->w_err.as<int>()));
     int64_t P = 0;
     SI_CK(cudaMemcpyAsync(&P, si->so_hoff.as<int64_t>() + q.nq, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
     SI_CK(cudaStreamSynchronize(st));
@@ -1635,7 +1687,7 @@ int setop_device(gSuperIntervals* si, const sig::QueryBatch& q, int op, int orde
         SI_CK(sig::launch_isect<S>(view<S>(si), q, hoff, hits, cnt, nullptr, nullptr, nullptr, nullptr, si->w_err.as<int>(), st));
     else
         SI_CK(sig::launch_diff<S>(view<S>(si), q, hoff, hits, sequential, cnt, nullptr, nullptr, nullptr, si->w_err.as<int>(), st));
-    SI_CK(sig::exclusive_scan_u32_to_i64(cnt, d_off, q.nq, si->w_tmp.p, st));
+    SI_CK(sig::exclusive_scan_u32_to_i64(cnt, d_off, q.nq, si->w_tmp.p, st, si->w_err.as<int>()));
     int64_t T = 0;
     SI_CK(cudaMemcpyAsync(&T, d_off + q.nq, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
     SI_TRY(read_dev_err(si, st));  // synchronizes

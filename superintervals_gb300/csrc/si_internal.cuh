@@ -49,14 +49,17 @@ enum DeviceError : int {
     kDevOk = 0,
     kDevBadContig = 1,     // a query named a contig outside [0, G)
     kDevOverflow = 2,      // an output offset ran past the output capacity
+    kDevTimeout = 3,       // a bounded wait on another block's published result gave up
 };
 
 // ---------------------------------------------------------------- scan
 // Exclusive prefix sums over n values; `out` receives n+1 values (the last one
-// is the total).  `temp` must hold scan_temp_bytes(n).
+// is the total).  `temp` must hold scan_temp_bytes(n).  With d_err (a device error word) the
+// u32 -> i64 scan is one kernel with decoupled look-back across tiles; a wait that gives up
+// records kDevTimeout there.  Without it, tile totals are scanned first (reduce-then-scan).
 size_t scan_temp_bytes(int64_t n);
 cudaError_t exclusive_scan_u32_to_i64(const uint32_t* in, int64_t* out, int64_t n, void* temp,
-                                      cudaStream_t st);
+                                      cudaStream_t st, int* d_err = nullptr);
 cudaError_t exclusive_scan_u32_to_u32(const uint32_t* in, uint32_t* out, int64_t n, void* temp,
                                       cudaStream_t st);
 // exclusive prefix sums mod 2^64 of signed coordinates (sign-extended), n + 1 entries
@@ -110,9 +113,13 @@ cudaError_t launch_contig_names(const uint32_t* first_rec, const int64_t* r_noff
 // no host round trip, so that the sort can be captured in a CUDA graph.
 constexpr int kMaxKeyWords = 5;
 size_t radix_temp_bytes(int64_t n, int K);
+// With d_err (a device error word) each pass is one kernel with decoupled look-back across
+// tiles (one-sweep); a wait that gives up records kDevTimeout there.  Without it, each pass is
+// a tile histogram, a scan and a scatter.
 cudaError_t radix_sort(uint32_t* const* keys, uint32_t* const* alt_keys, uint32_t* payload,
                        uint32_t* alt_payload, int K, int64_t n, void* temp, size_t temp_bytes,
-                       bool* result_in_alt, int* passes_run, cudaStream_t st, uint32_t pass_mask = 0);
+                       bool* result_in_alt, int* passes_run, cudaStream_t st, uint32_t pass_mask = 0,
+                       int* d_err = nullptr);
 
 // ---------------------------------------------------------------- build
 template <typename S>

@@ -1,9 +1,18 @@
-// si_scan.cu -- device-wide exclusive prefix sum (reduce-then-scan).
+// si_scan.cu -- device-wide exclusive prefix sum.
 //
 // Used for the per-query result offsets (count -> exclusive scan -> emit, the
 // CSR form of the per-query result lists of src/superintervals/intervalmap.pyx:402-494)
-// and for the digit offsets of the radix sort.  HBM-bound: one read for the
-// tile totals, one read + one write for the scan itself.
+// and for the digit offsets of the three-kernel radix sort.  HBM-bound.
+//
+// Two forms:
+//  * single pass (u32 counts -> i64 offsets, when the caller passes a device error word):
+//    a block takes the next 4096-value tile from an atomic counter, publishes its total, and
+//    its first warp looks back over the earlier tiles' published totals 32 tiles at a time
+//    (decoupled look-back: a tile's inclusive prefix, once published, ends the walk), then
+//    publishes its own inclusive prefix and writes its offsets: one read and one write;
+//  * reduce-then-scan: tile totals, their scan, then the tiles: two reads and one write.
+#include <algorithm>
+
 #include "si_internal.cuh"
 
 namespace sig {
@@ -86,6 +95,98 @@ __global__ void __launch_bounds__(kThreads) k_tile_scan(const Tin* __restrict__ 
     if (threadIdx.x == 0 && tile_end >= n) out[n] = total;
 }
 
+// Look-back status of a tile: 2 flag bits over a 62-bit sum.
+constexpr unsigned long long kTileAgg = 1ull << 62;   // the tile's own total
+constexpr unsigned long long kTilePre = 2ull << 62;   // the total of this and all earlier tiles
+constexpr unsigned long long kTileVal = (1ull << 62) - 1ull;
+constexpr int kScanSpinLimit = 1 << 22;               // polls of one window before giving up
+
+__device__ __forceinline__ void st_tile(unsigned long long* p, unsigned long long v) {
+    asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+__device__ __forceinline__ unsigned long long ld_tile(const unsigned long long* p) {
+    unsigned long long v;
+    asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+
+// Single-pass exclusive scan of u32 counts into i64 offsets (out has n + 1 slots).  status holds
+// one word per tile and tile_ctr one counter, all zero at launch.  A look-back window that stays
+// unpublished for kScanSpinLimit polls records kDevTimeout in *d_err and the walk goes on, so
+// the kernel always ends.
+__global__ void __launch_bounds__(kThreads) k_scan_lookback(const uint32_t* __restrict__ in, int64_t n,
+                                                            int64_t* __restrict__ out,
+                                                            unsigned long long* __restrict__ status,
+                                                            unsigned int* __restrict__ tile_ctr,
+                                                            int* __restrict__ d_err) {
+    __shared__ int64_t wtot[kWarps];
+    __shared__ int64_t s_prefix;
+    __shared__ unsigned int s_t;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (threadIdx.x == 0) s_t = atomicAdd(tile_ctr, 1u);  // tiles in start order: earlier tiles run
+    __syncthreads();
+    const int64_t t = s_t;
+    const int64_t base = t * kTile + (int64_t)w * (kItems * kWarp) + lane;
+    int64_t v[kItems];
+    int64_t carry = 0;
+#pragma unroll
+    for (int r = 0; r < kItems; ++r) {
+        const int64_t i = base + r * kWarp;
+        const int64_t x = (i < n) ? (int64_t)in[i] : 0;
+        const int64_t inc = warp_inclusive_sum(x, lane);
+        v[r] = carry + inc - x;
+        carry += __shfl_sync(kFull, inc, 31);
+    }
+    if (lane == 0) wtot[w] = carry;
+    __syncthreads();
+    int64_t total = 0;
+#pragma unroll
+    for (int k = 0; k < kWarps; ++k) total += wtot[k];
+    if (w == 0) {
+        if (lane == 0) st_tile(status + t, (t == 0 ? kTilePre : kTileAgg) | (unsigned long long)total);
+        int64_t excl = 0;
+        if (t > 0) {
+            // earlier tiles, 32 at a time: lane l holds tile top - l; the nearest published
+            // inclusive prefix ends the walk, the totals of the tiles after it are added
+            int64_t top = t - 1;
+            int spins = 0;
+            while (true) {
+                const int64_t p = top - lane;
+                const unsigned long long s = p >= 0 ? ld_tile(status + p) : kTilePre;
+                const unsigned long long f = s & ~kTileVal;
+                if (__any_sync(kFull, f == 0ull)) {
+                    if (++spins > kScanSpinLimit) {
+                        if (lane == 0) atomicCAS(d_err, kDevOk, kDevTimeout);
+                        break;
+                    }
+                    __nanosleep(32);
+                    continue;
+                }
+                spins = 0;
+                const unsigned pm = __ballot_sync(kFull, f == kTilePre);
+                const int first = pm ? __ffs(pm) - 1 : 32;
+                int64_t x = lane <= first ? (int64_t)(s & kTileVal) : 0;
+#pragma unroll
+                for (int d = 16; d > 0; d >>= 1) x += __shfl_xor_sync(kFull, x, d);
+                excl += x;
+                if (pm) break;
+                top -= 32;
+            }
+            if (lane == 0) st_tile(status + t, kTilePre | (unsigned long long)(excl + total));
+        }
+        if (lane == 0) s_prefix = excl;
+    }
+    __syncthreads();
+    int64_t off = s_prefix;
+    for (int k = 0; k < w; ++k) off += wtot[k];
+#pragma unroll
+    for (int r = 0; r < kItems; ++r) {
+        const int64_t i = base + r * kWarp;
+        if (i < n) out[i] = v[r] + off;
+    }
+    if (threadIdx.x == 0 && (t + 1) * kTile >= n) out[n] = s_prefix + total;
+}
+
 template <typename Tin, typename Tout>
 cudaError_t scan_impl(const Tin* in, Tout* out, int64_t n, char* temp, cudaStream_t st) {
     if (n <= 0) {
@@ -120,7 +221,21 @@ size_t scan_temp_impl(int64_t n) {
         bytes += sizeof(Tout) * (size_t)(round_up(tiles, 64) + round_up(tiles + 1, 64));
         m = tiles;
     }
-    return bytes + 256;
+    // the single-pass form: one status word per tile and the tile counter
+    const size_t one = sizeof(unsigned long long) * (size_t)round_up(ceil_div(n > 0 ? n : 1, kTile), 64) + 256;
+    return std::max(bytes, one) + 256;
+}
+
+cudaError_t scan_lookback(const uint32_t* in, int64_t* out, int64_t n, char* temp, int* d_err, cudaStream_t st) {
+    const int64_t tiles = ceil_div(n, kTile);
+    unsigned long long* status = reinterpret_cast<unsigned long long*>(temp);
+    const size_t sb = sizeof(unsigned long long) * (size_t)round_up(tiles, 64);
+    unsigned int* ctr = reinterpret_cast<unsigned int*>(temp + sb);
+    cudaError_t e = cudaMemsetAsync(temp, 0, sb + 256, st);
+    if (e != cudaSuccess) return e;
+    k_scan_lookback<<<(unsigned)tiles, kThreads, 0, st>>>(in, n, out, status, ctr, d_err);
+    note_launch();
+    return cudaGetLastError();
 }
 
 }  // namespace
@@ -130,7 +245,8 @@ size_t scan_temp_bytes(int64_t n) {
 }
 
 cudaError_t exclusive_scan_u32_to_i64(const uint32_t* in, int64_t* out, int64_t n, void* temp,
-                                      cudaStream_t st) {
+                                      cudaStream_t st, int* d_err) {
+    if (d_err && n > 0) return scan_lookback(in, out, n, static_cast<char*>(temp), d_err, st);
     return scan_impl<uint32_t, int64_t>(in, out, n, static_cast<char*>(temp), st);
 }
 

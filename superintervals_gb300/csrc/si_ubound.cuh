@@ -62,14 +62,17 @@ __device__ __forceinline__ int64_t eytz_sample_pos(int64_t r, int64_t n, int64_t
 }
 
 // Upper bound inside one contig: starts points at the contig's first key, n keys.
-// `tree` (may be shared memory) holds the contig's Eytzinger keys, 1-based.
+// `tree` holds the contig's Eytzinger keys, 1-based; its slots below `top_n` may also be
+// read from `top` (the tree's top levels staged in shared memory).
 template <typename S>
 __device__ __forceinline__ int64_t ub_search(const UbView<S>& U, int g, const S* __restrict__ starts,
-                                             int64_t n, S v, const S* tree) {
+                                             int64_t n, S v, const S* tree, const S* top = nullptr,
+                                             int64_t top_n = 0) {
     if (n <= 0) return -1;
     if (U.mode == 1 && U.eytz_n > 1) {
         const int64_t K = U.eytz_n - 1;
         int64_t i = 1;
+        while (i < top_n) i = 2 * i + (top[i] <= v ? 1 : 0);
         while (i <= K) i = 2 * i + (tree[i] <= v ? 1 : 0);
         i >>= __ffsll(~i);
         // rank of the first sample > v (K when every sample is <= v)

@@ -265,15 +265,17 @@ def _device_ub(api, idx, qe, qc, mode):
     return out
 
 
+@pytest.mark.parametrize("path", PATHS)
 @pytest.mark.parametrize("mode", UB_MODES)
-def test_upper_bound_providers_exact(api, mode):
+def test_upper_bound_providers_exact(api, mode, path):
     """Every provider returns the reference's upper_bound (hpp:501-516) for every query,
-    including values before the first start, after the last one and on duplicates."""
+    including values before the first start, after the last one and on duplicates: per query
+    (plain path) and through the sorted batch (batched path)."""
     from superintervals_gb300 import workloads as W
     for wl in (W.config4(n=400_000, nq=100_000), W.config3(n=300_000, nq=100_000),
                W.random_nested(41, 5000, 5000, dtype=np.int64)):
         idx = _index(api, wl.starts, wl.ends, wl.data, seg=wl.seg if len(wl.seg) > 2 else None,
-                     path="batched")
+                     path=path)
         idx.set_upper_bound(_ub_const(api, mode))
         s, _, _, _ = idx.arrays()
         qe = np.concatenate([wl.q_ends, s[:1000], s[:1000] - 1, [s.min() - 5, s.max() + 5]]).astype(idx.dtype)

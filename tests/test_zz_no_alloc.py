@@ -114,14 +114,16 @@ def test_no_alloc_search_matches_allocating_entry_point(lib, bits):
     few = np.ascontiguousarray(wl.q_starts[:4], dt), np.ascontiguousarray(wl.q_ends[:4], dt)
     d_bs, d_be = _dev(lib, check, few[0], stream=st), _dev(lib, check, few[1], stream=st)
     d_bc = _dev(lib, check, bad_c, stream=st)
-    d_bo, d_bv = _dev(lib, check, nbytes=8 * 5), _dev(lib, check, nbytes=4 * 4096)
-    st_ = lib.searchIdxsNoAllocGpu(idx.h, d_bs, d_be, d_bc, 4, 0, d_bo, d_bv, 4096, C.byref(t3), st)
+    want_off, want_out = o.search_batch(m, few[0], few[1], np.zeros(4, np.int32), order=0)
+    cap = max(int(want_off[-1]), 1)
+    d_bo, d_bv = _dev(lib, check, nbytes=8 * 5), _dev(lib, check, nbytes=4 * cap)
+    st_ = lib.searchIdxsNoAllocGpu(idx.h, d_bs, d_be, d_bc, 4, 0, d_bo, d_bv, cap, C.byref(t3), st)
     assert st_ == _capi.SI_ERR_INVALID
     bad_c[2] = 0
     check(lib.memcpyGpu(d_bc, C.c_void_p(bad_c.ctypes.data), bad_c.nbytes, st))
-    check(lib.searchIdxsNoAllocGpu(idx.h, d_bs, d_be, d_bc, 4, 0, d_bo, d_bv, 4096, C.byref(t3), st))
-    want_off, _ = o.search_batch(m, few[0], few[1], bad_c, order=0)
+    check(lib.searchIdxsNoAllocGpu(idx.h, d_bs, d_be, d_bc, 4, 0, d_bo, d_bv, cap, C.byref(t3), st))
     assert int(t3.value) == int(want_off[-1])
+    assert np.array_equal(_host(lib, check, d_bv, int(want_off[-1]), np.int32, st), want_out)
     for p in (d_qs, d_qe, d_qc, d_off, d_bs, d_be, d_bc, d_bo, d_bv):
         if p is not None:
             lib.deviceFreeGpu(p)
