@@ -380,6 +380,33 @@ def run_gpu(args, rank, world, dist):
         for p in (hq_s, hq_e, hq_c, h_off, h_out):
             if p:
                 lib.hostFreePinnedGpu(p)
+    # latency of single-query calls (the drop-in's per-query methods are one-query batches
+    # through the host-buffer C-ABI): count and search_idxs of one query, median of 200 calls
+    if rank == 0:
+        one_s, one_e = wl.q_starts[:1].copy(), wl.q_ends[:1].copy()
+        one_c = None if wl.q_contig is None else wl.q_contig[:1].copy()
+        cnt1 = np.zeros(1, np.uint32)
+        off1 = np.zeros(2, np.int64)
+        val1 = np.zeros(1 << 16, np.int32)
+        f_cnt = lib.countOverlapsBatchGpu_i64 if s_bytes == 8 else lib.countOverlapsBatchGpu
+        lat = {"count": [], "search_idxs": []}
+        saved = path
+        idx.set_path(_capi.PATH_AUTO)     # one query takes the plain path
+        for _ in range(220):
+            t0 = time.perf_counter()
+            _capi.check(f_cnt(idx.h, C.c_void_p(one_s.ctypes.data), C.c_void_p(one_e.ctypes.data),
+                              None if one_c is None else C.c_void_p(one_c.ctypes.data), 1,
+                              C.c_void_p(cnt1.ctypes.data)))
+            t1 = time.perf_counter()
+            _capi.check(lib.searchBatchIntoGpu(idx.h, C.c_void_p(one_s.ctypes.data), C.c_void_p(one_e.ctypes.data),
+                                               None if one_c is None else C.c_void_p(one_c.ctypes.data), 1, 0, 0,
+                                               C.c_void_p(off1.ctypes.data), C.c_void_p(val1.ctypes.data),
+                                               val1.size, C.byref(total)))
+            t2 = time.perf_counter()
+            lat["count"].append(t1 - t0)
+            lat["search_idxs"].append(t2 - t1)
+        idx.set_path(saved)
+        res["single_query_us"] = {k: 1e6 * statistics.median(v[20:]) for k, v in lat.items()}
     for p in (d_qs, d_qe, d_qc, d_off, d_out):
         if p:
             lib.deviceFreeGpu(p)
@@ -1190,6 +1217,10 @@ def main():
                         "emit_ms_filter_only": res.get("emit_filter_only_ms"),
                         "whole_step_frac": (algo / (ms / 1000.0) / 1e9) / peak}
     line["gpu_launches"] = res["launches"]
+    if "single_query_us" in res:
+        line["single_query_latency_us"] = dict(res["single_query_us"],
+                                               note="one-query calls through the host-buffer C-ABI "
+                                                    "(the drop-in's per-query methods), median of 200")
     if "plain_ms" in res:
         line["plain_gpu"] = {"ms_per_step": res["plain_ms"], "queries_per_s": nq / (res["plain_ms"] / 1e3),
                              "speedup_vs_plain": res["plain_ms"] / ms}

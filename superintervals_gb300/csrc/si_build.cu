@@ -236,6 +236,182 @@ __global__ void __launch_bounds__(kThreads) k_branch(const S* __restrict__ ends,
     branch[i] = (int32_t)res;
 }
 
+// ---- branch pass with decoupled look-back across tiles ------------------------------------
+// A block takes the next tile of kBrTile positions from an atomic counter and finds each
+// position's nearest earlier position with end >= its end: inside its 32-position chunk with
+// warp shuffles, then among the tile's earlier chunks (chunk maxima in shared memory).  The tile
+// publishes its maximum end (flag 1) as soon as it is known; warp 0 then walks back over the
+// earlier tiles' published maxima, 32 tiles per step, until a tile that has published its
+// inclusive prefix maximum (flag 2) and publishes its own.  A position still unresolved (its end
+// exceeds every earlier end of the tile) looks back the same way for the nearest earlier tile
+// whose maximum reaches it -- or stops at a prefix maximum below its end, or at its contig's
+// first tile -- and descends that tile's 32 chunk maxima (pyramid level 1) and the chosen
+// chunk's 32 ends.  Waits on unpublished tiles are bounded; giving up records kDevTimeout.
+constexpr int kBrTile = 1024;
+constexpr int kBrSpinLimit = 1 << 22;
+
+__device__ __forceinline__ void st_flag_release(int* p, int v) {
+    asm volatile("st.release.gpu.global.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ int ld_flag_acquire(const int* p) {
+    int v;
+    asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+template <typename S>
+__global__ void __launch_bounds__(kThreads) k_branch_lookback(const S* __restrict__ ends, int64_t n, int64_t n_pad,
+                                                              const S* __restrict__ lvl1,
+                                                              const int64_t* __restrict__ seg, int G,
+                                                              int32_t* __restrict__ branch, S* __restrict__ t_max,
+                                                              S* __restrict__ t_pre, int* __restrict__ t_flag,
+                                                              unsigned int* __restrict__ tile_ctr,
+                                                              int* __restrict__ d_err) {
+    __shared__ S se[kBrTile];
+    __shared__ S cmax[kBrTile / 32];
+    __shared__ int16_t s_un[kBrTile];
+    __shared__ int s_nun;
+    __shared__ unsigned int s_t;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    if (tid == 0) {
+        s_t = atomicAdd(tile_ctr, 1u);  // tiles in start order: earlier tiles run
+        s_nun = 0;
+    }
+    __syncthreads();
+    const int64_t t = s_t;
+    const int64_t base = t * kBrTile;
+    for (int k = tid; k < kBrTile; k += kThreads) {
+        const int64_t p = base + k;
+        se[k] = p < n_pad ? ends[p] : Lim<S>::lo;
+    }
+    __syncthreads();
+    for (int c = warp; c < kBrTile / 32; c += kThreads / 32) {
+        S v = se[c * 32 + lane];
+#pragma unroll
+        for (int d = 16; d > 0; d >>= 1) {
+            const S o = __shfl_xor_sync(kFull, v, d);
+            v = o > v ? o : v;
+        }
+        if (lane == 0) cmax[c] = v;
+    }
+    __syncthreads();
+    if (tid == 0) {
+        S m = cmax[0];
+        for (int c = 1; c < kBrTile / 32; ++c) m = cmax[c] > m ? cmax[c] : m;
+        t_max[t] = m;
+        if (t == 0) t_pre[0] = m;
+        st_flag_release(t_flag + t, t == 0 ? 2 : 1);
+    }
+    // inside the tile: the chunk by shuffles, then the tile's earlier chunks
+    for (int c = warp; c < kBrTile / 32; c += kThreads / 32) {
+        const int k = c * 32 + lane;
+        const int64_t i = base + k;
+        const S e = se[k];
+        int best = -1;
+#pragma unroll
+        for (int j = 0; j < 31; ++j) {
+            const S v = __shfl_sync(kFull, e, j);
+            if (j < lane && v >= e) best = j;
+        }
+        int64_t res = best >= 0 ? base + c * 32 + best : -1;
+        if (best < 0 && i < n) {
+            int cc = c - 1;
+            while (cc >= 0 && cmax[cc] < e) --cc;
+            if (cc >= 0) {
+                int j = 31;
+                while (se[cc * 32 + j] < e) --j;  // the chunk's maximum is >= e
+                res = base + cc * 32 + j;
+            } else {
+                s_un[atomicAdd(&s_nun, 1)] = (int16_t)k;
+            }
+        }
+        if (i < n && (best >= 0 || res >= 0)) {
+            if (G > 1 && res < seg[seg_of(seg, G, i)]) res = -1;
+            branch[i] = (int32_t)res;
+        }
+    }
+    __syncthreads();
+    // warp 0: this tile's inclusive prefix maximum, from the earlier tiles' published values
+    if (warp == 0 && t > 0) {
+        S pre = Lim<S>::lo;
+        int64_t top = t - 1;
+        int spins = 0;
+        while (true) {
+            const int64_t p = top - lane;
+            const int f = p >= 0 ? ld_flag_acquire(t_flag + p) : 2;
+            if (__any_sync(kFull, f == 0)) {
+                if (++spins > kBrSpinLimit) {
+                    if (lane == 0) atomicCAS(d_err, kDevOk, kDevTimeout);
+                    break;
+                }
+                __nanosleep(32);
+                continue;
+            }
+            spins = 0;
+            const unsigned pm = __ballot_sync(kFull, f == 2);
+            const int first = pm ? __ffs(pm) - 1 : 32;
+            S v = Lim<S>::lo;
+            if (p >= 0 && lane <= first) v = (lane == first) ? t_pre[p] : t_max[p];
+#pragma unroll
+            for (int d = 16; d > 0; d >>= 1) {
+                const S o = __shfl_xor_sync(kFull, v, d);
+                v = o > v ? o : v;
+            }
+            pre = v > pre ? v : pre;
+            if (pm) break;
+            top -= 32;
+        }
+        if (lane == 0) {
+            S m = t_max[t];
+            t_pre[t] = m > pre ? m : pre;
+            st_flag_release(t_flag + t, 2);
+        }
+    }
+    // positions whose end exceeds every earlier end of the tile: one warp each
+    const int nun = s_nun;
+    for (int u = warp; u < nun; u += kThreads / 32) {
+        const int k = s_un[u];
+        const int64_t i = base + k;
+        const S e = se[k];
+        const int64_t cs = G > 1 ? seg[seg_of(seg, G, i)] : 0;  // the contig's first position
+        int64_t res = -1;
+        int64_t top = t - 1;
+        int spins = 0;
+        while (top >= 0) {
+            const int64_t p = top - lane;
+            const bool live = p >= 0 && (p + 1) * kBrTile > cs;  // the tile holds positions >= cs
+            const int f = live ? ld_flag_acquire(t_flag + p) : 2;
+            if (__any_sync(kFull, f == 0)) {
+                if (++spins > kBrSpinLimit) {
+                    if (lane == 0) atomicCAS(d_err, kDevOk, kDevTimeout);
+                    break;
+                }
+                __nanosleep(32);
+                continue;
+            }
+            spins = 0;
+            const bool reach = live && t_max[p] >= e;
+            const bool stop = !live || (f == 2 && t_pre[p] < e);  // nothing at or before p reaches
+            const unsigned hm = __ballot_sync(kFull, reach), sm = __ballot_sync(kFull, stop);
+            const int fh = hm ? __ffs(hm) - 1 : 32, fs = sm ? __ffs(sm) - 1 : 32;
+            if (fh < fs) {
+                // the nearest tile reaching e: its last chunk, then the chunk's last position
+                const int64_t pt = top - fh;
+                const S cm = lvl1[pt * 32 + lane];
+                const unsigned cmask = __ballot_sync(kFull, cm >= e);
+                const int64_t ch = pt * 32 + (31 - __clz(cmask));
+                const S v = ends[ch * 32 + lane];
+                const unsigned vmask = __ballot_sync(kFull, v >= e);
+                res = ch * 32 + (31 - __clz(vmask));
+                break;
+            }
+            if (sm) break;
+            top -= 32;
+        }
+        if (lane == 0 && i < n) branch[i] = (int32_t)(res >= cs ? res : -1);
+    }
+}
+
 inline unsigned blocks_for(int64_t n, int t = kThreads) {
     return (unsigned)std::max<int64_t>(1, ceil_div(n, t));
 }
@@ -414,11 +590,32 @@ cudaError_t launch_end_decode(const uint32_t* const* kw, int64_t n, int64_t n_pa
     return cudaGetLastError();
 }
 
+size_t branch_temp_bytes(int64_t n_pad) {
+    const int64_t tiles = ceil_div(std::max<int64_t>(n_pad, 1), kBrTile);
+    return (size_t)round_up(tiles, 64) * (2 * sizeof(int64_t) + sizeof(int)) + 1024;
+}
+
 template <typename S>
 cudaError_t launch_branch(const S* ends, int64_t n, int64_t n_pad, Levels<S> L, int H,
-                          const int64_t* seg, int G, int32_t* branch, cudaStream_t st) {
+                          const int64_t* seg, int G, int32_t* branch, cudaStream_t st, void* temp,
+                          int* d_err) {
     if (n <= 0) return cudaSuccess;
-    k_branch<S><<<blocks_for(n_pad), kThreads, 0, st>>>(ends, n, n_pad, L, H, seg, G, branch);
+    if (!temp || !d_err || H < 1) {
+        k_branch<S><<<blocks_for(n_pad), kThreads, 0, st>>>(ends, n, n_pad, L, H, seg, G, branch);
+        note_launch();
+        return cudaGetLastError();
+    }
+    const int64_t tiles = ceil_div(n_pad, kBrTile);
+    const int64_t tp = round_up(tiles, 64);
+    char* p = static_cast<char*>(temp);
+    S* t_max = reinterpret_cast<S*>(p);
+    S* t_pre = t_max + tp;
+    int* t_flag = reinterpret_cast<int*>(p + 2 * sizeof(int64_t) * tp);
+    unsigned int* ctr = reinterpret_cast<unsigned int*>(t_flag + tp);
+    cudaError_t e = cudaMemsetAsync(t_flag, 0, sizeof(int) * tp + 256, st);
+    if (e != cudaSuccess) return e;
+    k_branch_lookback<S><<<(unsigned)tiles, kThreads, 0, st>>>(ends, n, n_pad, L.p[0], seg, G, branch, t_max, t_pre,
+                                                               t_flag, ctr, d_err);
     note_launch();
     return cudaGetLastError();
 }
@@ -439,7 +636,7 @@ cudaError_t launch_branch(const S* ends, int64_t n, int64_t n_pad, Levels<S> L, 
                                                 int64_t, const int64_t*, int, int32_t*, S*, int64_t*,        \
                                                 cudaStream_t);                                               \
     template cudaError_t launch_branch<S>(const S*, int64_t, int64_t, Levels<S>, int,           \
-                                          const int64_t*, int, int32_t*, cudaStream_t);        \
+                                          const int64_t*, int, int32_t*, cudaStream_t, void*, int*); \
     template int end_key_words<S>(int);                                                          \
     template cudaError_t launch_end_keys<S>(const S*, int64_t, const int64_t*, int, uint32_t* const*, \
                                             cudaStream_t);                                       \

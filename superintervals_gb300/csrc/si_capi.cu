@@ -366,8 +366,13 @@ int build_impl(gSuperIntervals* si) {
     S* lp[sig::kMaxLevels];
     for (int h = 0; h < sig::kMaxLevels; ++h) lp[h] = si->lvl[h].as<S>();
     SI_CK(sig::launch_pyramid<S>(ends, si->lvl_sizes, si->H, lp, st));
-    SI_CK(sig::launch_branch<S>(ends, n, n_pad, levels<S>(si), si->H, si->seg.as<int64_t>(), G,
-                                si->branch.as<int32_t>(), st));
+    {
+        DevBuf btmp;
+        SI_TRY(btmp.reserve(sig::branch_temp_bytes(n_pad)));
+        SI_CK(sig::launch_branch<S>(ends, n, n_pad, levels<S>(si), si->H, si->seg.as<int64_t>(), G,
+                                    si->branch.as<int32_t>(), st, btmp.p, berr.as<int>()));
+        SI_CK(cudaStreamSynchronize(st));  // the temporary is released on scope exit
+    }
     // long-interval list of the batched path: intervals at least kLongIntervalSplit long, in
     // position order, with their own max pyramid (a tile reaches them without visiting the
     // positions in between)

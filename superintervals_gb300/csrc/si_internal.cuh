@@ -185,9 +185,13 @@ cudaError_t launch_long_scatter(const S* starts, const S* ends, int64_t n, int64
                                 S* lend, int64_t* long_seg, cudaStream_t st);
 // flag = 1 when a[i] != b[i] for some i < n
 cudaError_t launch_differs_i32(const int32_t* a, const int32_t* b, int64_t n, int* flag, cudaStream_t st);
+// branch array: with temp (branch_temp_bytes(n_pad)) and an error word, one kernel with
+// decoupled look-back across tiles; otherwise the pyramid climb
+size_t branch_temp_bytes(int64_t n_pad);
 template <typename S>
 cudaError_t launch_branch(const S* ends, int64_t n, int64_t n_pad, Levels<S> L, int H,
-                          const int64_t* seg, int G, int32_t* branch, cudaStream_t st);
+                          const int64_t* seg, int G, int32_t* branch, cudaStream_t st, void* temp = nullptr,
+                          int* d_err = nullptr);
 // each contig's ends in ascending order: sort keys (end_key_words<S>(G) words, for
 // radix_sort), then the sorted keys decoded into out[0, n_pad) (padding: the largest value)
 template <typename S>

@@ -104,6 +104,7 @@ def test_bench_search_line_gpu():
     for k in ("roofline", "cpu_baseline", "e2e", "clocks", "plain_gpu"):
         assert k in line, k
     assert 0 < line["roofline"]["frac"] < 2
+    assert line["parity_sample_ok"] is True      # the timed result's first queries against the oracle
 
 
 @pytest.mark.gpu
@@ -112,7 +113,11 @@ def test_bench_upper_bound_line_gpu():
                     "--cpu-seconds", "0.5"])
     assert line["oracle_sample_identical"]
     assert all(v["identical_to_binary"] for v in line["providers"].values())
-    assert line["gpu_launches"] == 3 and "e2e" in line and "cpu_baseline" in line
+    # the headline is the sorted batch: keys, min/max, histogram, digit offsets, three sort passes,
+    # prepare and the scatter back per step; per query it is one kernel per step
+    assert line["gpu_launches"] == 3 * 9 and "e2e" in line and "cpu_baseline" in line
+    assert line["providers"]["binary"]["path"] == "per_query"
+    assert line["providers"]["learned+sorted"]["path"] == "sorted_batch"
 
 
 @pytest.mark.gpu
