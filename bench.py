@@ -304,17 +304,22 @@ def run_gpu(args, rank, world, dist):
     _capi.check(lib.getPhaseTimesGpu(idx.h, ms4, n4))
     res["phase_ms"] = [ms4[k] / max(1, n4[k]) for k in range(4)]
     if path == _capi.PATH_BATCHED:
-        # the same steps with the long-interval list's section of part B filtered instead of
-        # copied (the emit's other mode), for comparison
-        _capi.check(lib.setProfilingGpu(idx.h, 0))
-        _capi.check(lib.setProfilingGpu(idx.h, 1))
-        _capi.check(lib.setBatchedOptionGpu(idx.h, _capi.OPT_EMIT_COPY, 0))
-        for _ in range(max(1, min(3, args.steps))):
-            _capi.check(lib.flushL2Gpu(st))
-            step()
-        _capi.check(lib.getPhaseTimesGpu(idx.h, ms4, n4))
-        res["emit_filter_only_ms"] = ms4[2] / max(1, n4[2])
-        _capi.check(lib.setBatchedOptionGpu(idx.h, _capi.OPT_EMIT_COPY, 1))
+        # the emit in each of its two modes for the long-interval list's section of part B
+        # (copied around its misses / filtered), the tuned mode restored afterwards
+        cur = C.c_int64(1)
+        _capi.check(lib.getBatchedOptionGpu(idx.h, _capi.OPT_EMIT_COPY, C.byref(cur)))
+        res["emit_mode_ms"] = {}
+        for mode, name in ((1, "copy"), (0, "filter")):
+            _capi.check(lib.setProfilingGpu(idx.h, 0))
+            _capi.check(lib.setProfilingGpu(idx.h, 1))
+            _capi.check(lib.setBatchedOptionGpu(idx.h, _capi.OPT_EMIT_COPY, mode))
+            for _ in range(max(1, min(3, args.steps))):
+                _capi.check(lib.flushL2Gpu(st))
+                step()
+            _capi.check(lib.getPhaseTimesGpu(idx.h, ms4, n4))
+            res["emit_mode_ms"][name] = ms4[2] / max(1, n4[2])
+        _capi.check(lib.setBatchedOptionGpu(idx.h, _capi.OPT_EMIT_COPY, cur.value))
+        res["emit_copy_tuned"] = int(cur.value)
     _capi.check(lib.setProfilingGpu(idx.h, 0))
 
     # the plain one-query-per-thread GPU path on the same inputs (the 1.0x baseline)
@@ -1214,7 +1219,7 @@ def main():
                         "traffic_frac": (traffic / (emit_ms / 1000.0) / 1e9 / peak) if traffic else None,
                         "peak_kind": peak_kind, "algorithmic_bytes": algo,
                         "phase_ms": {"count": ph[0], "scan": ph[1], "emit": ph[2], "prepare": ph[3]},
-                        "emit_ms_filter_only": res.get("emit_filter_only_ms"),
+                        "emit_ms_by_mode": res.get("emit_mode_ms"),
                         "whole_step_frac": (algo / (ms / 1000.0) / 1e9) / peak}
     line["gpu_launches"] = res["launches"]
     if "single_query_us" in res:

@@ -569,45 +569,32 @@ __device__ void long_query(const TileArgs<S>& a, S qs, int64_t u, int64_t lo, in
     }
 }
 
-// One warp copies src[0, len) (shared memory, any word offset) to dst[0, len) (global memory,
-// any 4-byte offset): 4-byte stores up to dst's first 16-byte boundary, then one 16-byte store
-// per lane and round (512 bytes per warp store), then the tail.  The four words of a lane's
-// 16-byte store are read in a lane-rotated order (lane l reads word (k + l / 8) mod 4 of its
-// group in step k), so that each shared-memory read touches 32 distinct banks, and rotated back
-// in registers.
-__device__ __forceinline__ void warp_copy_s2g(int32_t* __restrict__ dst, const int32_t* __restrict__ src, int len,
-                                              int lane) {
-    if (len <= 0) return;
-    const int head = min(len, (int)(((16u - ((uint32_t)(uintptr_t)dst & 15u)) & 15u) >> 2));
-    if (lane < head) dst[lane] = src[lane];
-    dst += head;
-    src += head;
-    len -= head;
-    const int n4 = len >> 2;
-    const int rot = lane >> 3;
-    const int o0 = rot & 3, o1 = (rot + 1) & 3, o2 = (rot + 2) & 3, o3 = (rot + 3) & 3;
-    int4* __restrict__ d4 = reinterpret_cast<int4*>(dst);
-    for (int c = lane; c < n4; c += 32) {
-        const int32_t* g = src + 4 * c;
-        int32_t v0 = g[o0], v1 = g[o1], v2 = g[o2], v3 = g[o3];  // v_k = word (k + rot) mod 4
-        if (rot & 2) {  // back to word order: swap the halves, then rotate right by one
-            const int32_t t0 = v0, t1 = v1;
-            v0 = v2;
-            v1 = v3;
-            v2 = t0;
-            v3 = t1;
-        }
-        if (rot & 1) {
-            const int32_t t = v3;
-            v3 = v2;
-            v2 = v1;
-            v1 = v0;
-            v0 = t;
-        }
-        d4[c] = make_int4(v0, v1, v2, v3);
+// One warp copies src[0, len) (shared memory) to dst[0, len) (global memory): 4-byte stores,
+// 128 values per round in four independent 32-wide slices.
+__device__ __forceinline__ void warp_copy4(int32_t* __restrict__ dst, const int32_t* __restrict__ src, int len,
+                                           int lane) {
+    int k = lane;
+    for (; k + 96 < len; k += 128) {
+        const int32_t v0 = src[k], v1 = src[k + 32], v2 = src[k + 64], v3 = src[k + 96];
+        dst[k] = v0;
+        dst[k + 32] = v1;
+        dst[k + 64] = v2;
+        dst[k + 96] = v3;
     }
-    const int base = n4 << 2, tail = len & 3;
-    if (lane < tail) dst[base + lane] = src[base + lane];
+    for (; k < len; k += 32) dst[k] = src[k];
+}
+
+// Misses per query that the image copy of the long-interval list's section takes (more: the
+// section is copied as runs between them).
+constexpr int kMaxMiss = 16;
+
+// Position in the long-interval list's section of output value o of a query whose outputs skip
+// the section's misses: o plus the number of misses at or before o in output order (mp holds
+// the misses' output positions, ascending, n of them).
+__device__ __forceinline__ int skip_src(const int* __restrict__ mp, int n, int o) {
+    int c = 0;
+    for (int k = 0; k < n; ++k) c += mp[k] <= o ? 1 : 0;
+    return o + c;
 }
 
 template <typename S, bool EMIT>
@@ -632,6 +619,8 @@ __global__ void __launch_bounds__(kThreads, 4) k_tiles(TileArgs<S> a) {
     int32_t* lpos = lst;
     S* lend = reinterpret_cast<S*>(cnt);
     S* cstart = (sizeof(S) == 4) ? reinterpret_cast<S*>(msk) : reinterpret_cast<S*>(msk + cap);
+    int32_t* img = reinterpret_cast<int32_t*>(cstart);             // emit step 2: the section images
+    const int img_cap = cap * (int)sizeof(S) / 4;
     __shared__ int s_tile, s_n, s_sum, s_nlnu, s_nlm, s_next;
     __shared__ int64_t s_cut[2];
     __shared__ int s_wsum[kWarpsPerCta];
@@ -639,6 +628,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_tiles(TileArgs<S> a) {
     __shared__ int32_t s_red3[kWarpsPerCta];
     __shared__ uint32_t s_bmask[kMaxBlocks];
     __shared__ int32_t s_boff[kMaxBlocks];
+    __shared__ int s_mp[kWarpsPerCta][kMaxMiss + 1];  // per warp: its query's miss positions
     __shared__ int32_t s_lnu_idx[kLnu];  // long candidates ending before the run's max qs: their
     __shared__ S s_lnu_end[kLnu];        // indices in the long list (ascending) and their ends
 
@@ -704,6 +694,8 @@ __global__ void __launch_bounds__(kThreads, 4) k_tiles(TileArgs<S> a) {
             // nc candidates; nl of them long, the first nlm of which come from the tile's own
             // gather (positions >= p_cut), the rest from the long-interval list; nlnu lnu entries
             int nc = 0, nl = 0, nlnu = 0, nlm = 0;
+            int img_len = 0;      // values per image of the long-interval list's section
+            bool img_ok = false;  // the images are built for this run
             // count pass over an index without inverted intervals: the prepare pass counted every
             // query but those with start > end (from ranks)
             const bool rank_run = !EMIT && a.end_sorted != nullptr && !code_is_inverted(cw, a.G);
@@ -1089,6 +1081,20 @@ __global__ void __launch_bounds__(kThreads, 4) k_tiles(TileArgs<S> a) {
                     lpos[k] = a.values ? a.data[p] : p - (int32_t)lo;
                 }
                 __syncthreads();
+                // four images of the long-interval list's section (values from index nlm on), image
+                // r shifted by r values, in the space of the candidates' starts (not read by step
+                // 2): any four consecutive values of the section are one aligned 16-byte read
+                img_len = ((nl - nlm) + 3 + 3) & ~3;
+                img_ok = a.emit_copy && nl > nlm && 4 * img_len <= img_cap &&
+                         (reinterpret_cast<uintptr_t>(img) & 15u) == 0;  // tile sizes keep it aligned
+                if (img_ok) {
+                    const int nb2 = nl - nlm;
+                    for (int k = tid; k < 4 * img_len; k += kThreads) {
+                        const int r = k / img_len, jj = k - r * img_len;
+                        img[k] = jj + r < nb2 ? lpos[nlm + jj + r] : 0;
+                    }
+                    __syncthreads();
+                }
             }
             for (int i = r0 + warp; EMIT && !per_query && !long_run && i < r1; i += kWarpsPerCta) {
                 // emit, step 2: one query per WARP writes its hits, coalesced
@@ -1133,8 +1139,9 @@ __global__ void __launch_bounds__(kThreads, 4) k_tiles(TileArgs<S> a) {
                 // part B: the long candidates from lb on.  Those of the tile's own gather ([lb, b2))
                 // are filtered one by one.  Those from the long-interval list ([b2, nl)) are all
                 // hits but the few lnu entries (ending before the run's largest qs) that end
-                // before this query's start: with the copy mode on, that section is copied as runs
-                // between those entries with 16-byte stores, else it is filtered too
+                // before this query's start: with the copy mode on, that section is copied around
+                // those entries (16-byte reads from shifted images and 16-byte stores), else it is
+                // filtered too
                 const int lb = q_lb[i];
                 const int b2 = max(lb, nlm);
                 int fend = a.emit_copy && nlnu <= kLnu ? b2 : nl;  // filtered: [lb, fend)
@@ -1184,7 +1191,65 @@ __global__ void __launch_bounds__(kThreads, 4) k_tiles(TileArgs<S> a) {
                     const int len = nl - b2 - nmiss;
                     if (len > room) {
                         bad = true;
+                    } else if (img_ok && nmiss <= kMaxMiss) {
+                        // output o (0 <= o < len) is section value sb + skip_src(o): the misses'
+                        // output positions go to the warp's list, then 16-byte chunks of the
+                        // output (aligned in global memory) are read from the image whose
+                        // shift makes them one aligned 16-byte read
+                        int* mp = s_mp[warp];
+                        {
+                            int before = 0;
+#pragma unroll
+                            for (int j = 0; j < kLnu / 32; ++j) {
+                                if ((mm[j] >> lane) & 1u) {
+                                    const int rank = before + __popc(mm[j] & lt);
+                                    mp[rank] = (s_lnu_idx[32 * j + lane] - b2) - rank;
+                                }
+                                before += __popc(mm[j]);
+                            }
+                            if (lane == 0) mp[nmiss] = INT32_MAX;
+                            __syncwarp();
+                        }
+                        const int sb = b2 - nlm;
+                        const int32_t* sec = lpos + nlm;
+                        const int hd = min(len, (int)(((16u - ((uint32_t)(uintptr_t)d & 15u)) & 15u) >> 2));
+                        if (lane < hd) d[lane] = sec[sb + skip_src(mp, nmiss, lane)];
+                        const int n4 = (len - hd) >> 2;
+                        int4* __restrict__ d4 = reinterpret_cast<int4*>(d + hd);
+                        int kn = 0;  // first miss at or after the round's first output
+                        for (int c0 = 0; c0 < n4; c0 += 32) {
+                            const int R = hd + 4 * c0;
+                            while (mp[kn] < R) ++kn;  // the list ends with INT32_MAX
+                            const int o = R + 4 * lane;
+                            int co = kn, c3 = kn;  // misses at or before o, at or before o + 3
+                            if (mp[kn] < R + 128) {
+                                for (int k = kn; k < nmiss && mp[k] <= o + 3; ++k) {
+                                    co += mp[k] <= o ? 1 : 0;
+                                    ++c3;
+                                }
+                            }
+                            if (c0 + lane < n4) {
+                                const int sv = sb + o + co;
+                                int4 v;
+                                if (co == c3) {
+                                    const int r = sv & 3;
+                                    v = *reinterpret_cast<const int4*>(img + r * img_len + (sv - r));
+                                } else {  // a miss inside the chunk
+                                    v.x = sec[sb + skip_src(mp, nmiss, o)];
+                                    v.y = sec[sb + skip_src(mp, nmiss, o + 1)];
+                                    v.z = sec[sb + skip_src(mp, nmiss, o + 2)];
+                                    v.w = sec[sb + skip_src(mp, nmiss, o + 3)];
+                                }
+                                d4[c0 + lane] = v;
+                            }
+                        }
+                        const int tl = hd + 4 * n4;
+                        if (tl + lane < len) d[tl + lane] = sec[sb + skip_src(mp, nmiss, tl + lane)];
+                        __syncwarp();  // mp is rewritten by the warp's next query
+                        d += len;
+                        room -= len;
                     } else {
+                        // runs between the misses
                         int at = b2;
 #pragma unroll
                         for (int j = 0; j < kLnu / 32; ++j) {
@@ -1192,12 +1257,12 @@ __global__ void __launch_bounds__(kThreads, 4) k_tiles(TileArgs<S> a) {
                             while (mj) {
                                 const int mi = s_lnu_idx[32 * j + __ffs(mj) - 1];
                                 mj &= mj - 1;
-                                warp_copy_s2g(d, lpos + at, mi - at, lane);
+                                warp_copy4(d, lpos + at, mi - at, lane);
                                 d += mi - at;
                                 at = mi + 1;
                             }
                         }
-                        warp_copy_s2g(d, lpos + at, nl - at, lane);
+                        warp_copy4(d, lpos + at, nl - at, lane);
                         d += nl - at;
                         room -= len;
                     }
