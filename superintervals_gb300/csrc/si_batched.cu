@@ -450,6 +450,36 @@ __device__ __forceinline__ int64_t warp_first_geq(const T* __restrict__ arr, int
     return m ? a + __ffs(m) - 1 : b;
 }
 
+// Upper bound of v inside one contig (last k with starts[k] <= v, else -1) by one warp: 32-ary
+// steps over the contig's starts.  With the learned provider, the leaf (32-ary steps over the
+// leaves' first keys) and the leaf model's error window narrow the range first; the answer is
+// checked against its neighbours and the whole leaf is searched when the window missed (exact
+// either way, as ub_search).  Warp-uniform.
+template <typename S>
+__device__ int64_t warp_ub(const UbView<S>& U, int g, const S* __restrict__ starts, int64_t n, S v, int lane) {
+    if (n <= 0 || v < starts[0]) return -1;
+    if (v == Lim<S>::hi) return n - 1;
+    const S v1 = (S)(v + 1);  // first index whose start is >= v1, minus one
+    if (U.mode == 2 && U.leaves) {
+        const int base = U.leaf_base[g];
+        const int nl = U.leaf_base[g + 1] - base;
+        const int l0 = (int)warp_first_geq<S, S>(U.leaf_key + base, 0, nl, v1, lane) - 1;  // >= 0
+        const int64_t pa = U.leaf_pos[base + l0];
+        const int64_t pb = (l0 + 1 < nl ? (int64_t)U.leaf_pos[base + l0 + 1] : n) - 1;
+        const LeafModel M = U.leaves[base + l0];
+        const double pred = M.y0 + M.slope * ((double)v - U.key_mean[g] - M.x0);
+        const double plo = pred - (double)M.err_lo - 1.0, phi = pred + (double)M.err_hi + 1.0;
+        const int64_t a = plo <= (double)pa ? pa : (plo >= (double)pb ? pb : (int64_t)plo);
+        int64_t b = phi >= (double)pb ? pb : (phi <= (double)pa ? pa : (int64_t)phi + 1);
+        if (b > pb) b = pb;
+        const int64_t r = warp_first_geq<S, S>(starts, a, b + 1, v1, lane) - 1;
+        const bool ok = r >= pa && starts[r] <= v && (r + 1 >= n || starts[r + 1] > v);
+        if (ok) return r;
+        return warp_first_geq<S, S>(starts, pa, pb + 1, v1, lane) - 1;
+    }
+    return warp_first_geq<S, S>(starts, 0, n, v1, lane) - 1;
+}
+
 // First index in [a, b) of an ascending position list whose position is >= key (b when none).
 __device__ __forceinline__ int64_t warp_first_pos_geq(const int32_t* __restrict__ pos, int64_t a, int64_t b,
                                                       int64_t key, int lane) {
@@ -584,19 +614,6 @@ __device__ __forceinline__ void warp_copy4(int32_t* __restrict__ dst, const int3
     for (; k < len; k += 32) dst[k] = src[k];
 }
 
-// Misses per query that the image copy of the long-interval list's section takes (more: the
-// section is copied as runs between them).
-constexpr int kMaxMiss = 16;
-
-// Position in the long-interval list's section of output value o of a query whose outputs skip
-// the section's misses: o plus the number of misses at or before o in output order (mp holds
-// the misses' output positions, ascending, n of them).
-__device__ __forceinline__ int skip_src(const int* __restrict__ mp, int n, int o) {
-    int c = 0;
-    for (int k = 0; k < n; ++k) c += mp[k] <= o ? 1 : 0;
-    return o + c;
-}
-
 template <typename S, bool EMIT>
 __global__ void __launch_bounds__(kThreads, 4) k_tiles(TileArgs<S> a) {
     extern __shared__ __align__(16) unsigned char smem[];
@@ -619,8 +636,6 @@ __global__ void __launch_bounds__(kThreads, 4) k_tiles(TileArgs<S> a) {
     int32_t* lpos = lst;
     S* lend = reinterpret_cast<S*>(cnt);
     S* cstart = (sizeof(S) == 4) ? reinterpret_cast<S*>(msk) : reinterpret_cast<S*>(msk + cap);
-    int32_t* img = reinterpret_cast<int32_t*>(cstart);             // emit step 2: the section images
-    const int img_cap = cap * (int)sizeof(S) / 4;
     __shared__ int s_tile, s_n, s_sum, s_nlnu, s_nlm, s_next;
     __shared__ int64_t s_cut[2];
     __shared__ int s_wsum[kWarpsPerCta];
@@ -628,7 +643,6 @@ __global__ void __launch_bounds__(kThreads, 4) k_tiles(TileArgs<S> a) {
     __shared__ int32_t s_red3[kWarpsPerCta];
     __shared__ uint32_t s_bmask[kMaxBlocks];
     __shared__ int32_t s_boff[kMaxBlocks];
-    __shared__ int s_mp[kWarpsPerCta][kMaxMiss + 1];  // per warp: its query's miss positions
     __shared__ int32_t s_lnu_idx[kLnu];  // long candidates ending before the run's max qs: their
     __shared__ S s_lnu_end[kLnu];        // indices in the long list (ascending) and their ends
 
@@ -694,8 +708,6 @@ __global__ void __launch_bounds__(kThreads, 4) k_tiles(TileArgs<S> a) {
             // nc candidates; nl of them long, the first nlm of which come from the tile's own
             // gather (positions >= p_cut), the rest from the long-interval list; nlnu lnu entries
             int nc = 0, nl = 0, nlnu = 0, nlm = 0;
-            int img_len = 0;      // values per image of the long-interval list's section
-            bool img_ok = false;  // the images are built for this run
             // count pass over an index without inverted intervals: the prepare pass counted every
             // query but those with start > end (from ranks)
             const bool rank_run = !EMIT && a.end_sorted != nullptr && !code_is_inverted(cw, a.G);
@@ -1081,20 +1093,6 @@ __global__ void __launch_bounds__(kThreads, 4) k_tiles(TileArgs<S> a) {
                     lpos[k] = a.values ? a.data[p] : p - (int32_t)lo;
                 }
                 __syncthreads();
-                // four images of the long-interval list's section (values from index nlm on), image
-                // r shifted by r values, in the space of the candidates' starts (not read by step
-                // 2): any four consecutive values of the section are one aligned 16-byte read
-                img_len = ((nl - nlm) + 3 + 3) & ~3;
-                img_ok = a.emit_copy && nl > nlm && 4 * img_len <= img_cap &&
-                         (reinterpret_cast<uintptr_t>(img) & 15u) == 0;  // tile sizes keep it aligned
-                if (img_ok) {
-                    const int nb2 = nl - nlm;
-                    for (int k = tid; k < 4 * img_len; k += kThreads) {
-                        const int r = k / img_len, jj = k - r * img_len;
-                        img[k] = jj + r < nb2 ? lpos[nlm + jj + r] : 0;
-                    }
-                    __syncthreads();
-                }
             }
             for (int i = r0 + warp; EMIT && !per_query && !long_run && i < r1; i += kWarpsPerCta) {
                 // emit, step 2: one query per WARP writes its hits, coalesced
@@ -1139,24 +1137,33 @@ __global__ void __launch_bounds__(kThreads, 4) k_tiles(TileArgs<S> a) {
                 // part B: the long candidates from lb on.  Those of the tile's own gather ([lb, b2))
                 // are filtered one by one.  Those from the long-interval list ([b2, nl)) are all
                 // hits but the few lnu entries (ending before the run's largest qs) that end
-                // before this query's start: with the copy mode on, that section is copied around
-                // those entries (16-byte reads from shifted images and 16-byte stores), else it is
-                // filtered too
+                // before this query's start: with the copy mode on, that section is copied as runs
+                // between those entries, else it is filtered too
                 const int lb = q_lb[i];
                 const int b2 = max(lb, nlm);
                 int fend = a.emit_copy && nlnu <= kLnu ? b2 : nl;  // filtered: [lb, fend)
                 for (int kk = lb; !bad && kk < fend; kk += 128) {
                     // 128 candidates per round as four independent 32-wide slices, so their
-                    // shared-memory reads and ballots overlap instead of chaining
+                    // shared-memory reads and ballots overlap instead of chaining; only the last
+                    // round checks the range end
                     bool hit[4];
                     int32_t pv[4];
                     unsigned m[4];
+                    if (kk + 128 <= fend) {
 #pragma unroll
-                    for (int s2 = 0; s2 < 4; ++s2) {
-                        const int tt = kk + 32 * s2 + lane;
-                        const bool in = tt < fend;
-                        hit[s2] = in && lend[tt] >= qs;
-                        pv[s2] = in ? lpos[tt] : 0;
+                        for (int s2 = 0; s2 < 4; ++s2) {
+                            const int tt = kk + 32 * s2 + lane;
+                            hit[s2] = lend[tt] >= qs;
+                            pv[s2] = lpos[tt];
+                        }
+                    } else {
+#pragma unroll
+                        for (int s2 = 0; s2 < 4; ++s2) {
+                            const int tt = kk + 32 * s2 + lane;
+                            const bool in = tt < fend;
+                            hit[s2] = in && lend[tt] >= qs;
+                            pv[s2] = in ? lpos[tt] : 0;
+                        }
                     }
 #pragma unroll
                     for (int s2 = 0; s2 < 4; ++s2) m[s2] = __ballot_sync(kFull, hit[s2]);
@@ -1191,65 +1198,8 @@ __global__ void __launch_bounds__(kThreads, 4) k_tiles(TileArgs<S> a) {
                     const int len = nl - b2 - nmiss;
                     if (len > room) {
                         bad = true;
-                    } else if (img_ok && nmiss <= kMaxMiss) {
-                        // output o (0 <= o < len) is section value sb + skip_src(o): the misses'
-                        // output positions go to the warp's list, then 16-byte chunks of the
-                        // output (aligned in global memory) are read from the image whose
-                        // shift makes them one aligned 16-byte read
-                        int* mp = s_mp[warp];
-                        {
-                            int before = 0;
-#pragma unroll
-                            for (int j = 0; j < kLnu / 32; ++j) {
-                                if ((mm[j] >> lane) & 1u) {
-                                    const int rank = before + __popc(mm[j] & lt);
-                                    mp[rank] = (s_lnu_idx[32 * j + lane] - b2) - rank;
-                                }
-                                before += __popc(mm[j]);
-                            }
-                            if (lane == 0) mp[nmiss] = INT32_MAX;
-                            __syncwarp();
-                        }
-                        const int sb = b2 - nlm;
-                        const int32_t* sec = lpos + nlm;
-                        const int hd = min(len, (int)(((16u - ((uint32_t)(uintptr_t)d & 15u)) & 15u) >> 2));
-                        if (lane < hd) d[lane] = sec[sb + skip_src(mp, nmiss, lane)];
-                        const int n4 = (len - hd) >> 2;
-                        int4* __restrict__ d4 = reinterpret_cast<int4*>(d + hd);
-                        int kn = 0;  // first miss at or after the round's first output
-                        for (int c0 = 0; c0 < n4; c0 += 32) {
-                            const int R = hd + 4 * c0;
-                            while (mp[kn] < R) ++kn;  // the list ends with INT32_MAX
-                            const int o = R + 4 * lane;
-                            int co = kn, c3 = kn;  // misses at or before o, at or before o + 3
-                            if (mp[kn] < R + 128) {
-                                for (int k = kn; k < nmiss && mp[k] <= o + 3; ++k) {
-                                    co += mp[k] <= o ? 1 : 0;
-                                    ++c3;
-                                }
-                            }
-                            if (c0 + lane < n4) {
-                                const int sv = sb + o + co;
-                                int4 v;
-                                if (co == c3) {
-                                    const int r = sv & 3;
-                                    v = *reinterpret_cast<const int4*>(img + r * img_len + (sv - r));
-                                } else {  // a miss inside the chunk
-                                    v.x = sec[sb + skip_src(mp, nmiss, o)];
-                                    v.y = sec[sb + skip_src(mp, nmiss, o + 1)];
-                                    v.z = sec[sb + skip_src(mp, nmiss, o + 2)];
-                                    v.w = sec[sb + skip_src(mp, nmiss, o + 3)];
-                                }
-                                d4[c0 + lane] = v;
-                            }
-                        }
-                        const int tl = hd + 4 * n4;
-                        if (tl + lane < len) d[tl + lane] = sec[sb + skip_src(mp, nmiss, tl + lane)];
-                        __syncwarp();  // mp is rewritten by the warp's next query
-                        d += len;
-                        room -= len;
                     } else {
-                        // runs between the misses
+                        // runs between the misses, 4-byte warp stores
                         int at = b2;
 #pragma unroll
                         for (int j = 0; j < kLnu / 32; ++j) {
@@ -1472,14 +1422,16 @@ __global__ void __launch_bounds__(kThreads, 6) k_qprep(const uint32_t* __restric
                 blk_cut[2 * blockIdx.x + 1] = ch;
             }
         }
-        if (tid < 2 && n > 0) {
-            S x = tid == 0 ? s_mn[0] : s_mx[0];  // thread 0: smallest end, thread 1: largest
+        if ((warp == 4 || warp == 5) && n > 0) {
+            // warp 4: upper bound of the block's smallest end, warp 5: of its largest
+            S x = warp == 4 ? s_mn[0] : s_mx[0];
             for (int w = 1; w < kWarpsPerCta; ++w)
-                x = tid == 0 ? (s_mn[w] < x ? s_mn[w] : x) : (s_mx[w] > x ? s_mx[w] : x);
-            const S* tr = (U.mode == 1) ? U.eytz_keys + (int64_t)g * U.eytz_n : nullptr;
-            const int64_t r = ub_search(U, g, m.starts + lo, n, x, tr);
-            if (tid == 0) s_a = r;
-            else s_b = r;
+                x = warp == 4 ? (s_mn[w] < x ? s_mn[w] : x) : (s_mx[w] > x ? s_mx[w] : x);
+            const int64_t r = warp_ub(U, g, m.starts + lo, n, x, lane);
+            if (lane == 0) {
+                if (warp == 4) s_a = r;
+                else s_b = r;
+            }
         }
         __syncthreads();
         if (n > 0) {

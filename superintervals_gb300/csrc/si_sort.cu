@@ -186,6 +186,7 @@ constexpr uint32_t kStAgg = 1u << 30;     // the tile's own count of the digit
 constexpr uint32_t kStPre = 2u << 30;     // the count of the digit in this and all earlier tiles
 constexpr uint32_t kStVal = (1u << 30) - 1u;
 constexpr int kSpinLimit = 1 << 22;       // polls of one status word before giving up
+constexpr int kLookWindow = 8;            // earlier tiles read per look-back step
 
 __device__ __forceinline__ void st_status(uint32_t* p, uint32_t v) {
     asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
@@ -263,26 +264,47 @@ __global__ void __launch_bounds__(kThreads) k_onesweep(KeyPtrs kin, KeyOutPtrs k
         if (lane >= dd) inc += y;
     }
     if (lane == 31) wsum[w] = inc;
-    // decoupled look-back: the digit's count in all earlier tiles
+    // decoupled look-back: the digit's count in all earlier tiles, kLookWindow tiles per step
+    // (independent reads, so that a chain of tiles that have published only their own counts
+    // costs one memory round trip per window instead of one per tile)
     uint32_t pre = 0;
     if (t > 0) {
         int64_t p = t - 1;
         int spins = 0;
         while (true) {
-            const uint32_t v = ld_status(status + p * kRadix + tid);
-            const uint32_t f = v & ~kStVal;
-            if (f == 0u) {
+            uint32_t v[kLookWindow];
+#pragma unroll
+            for (int k = 0; k < kLookWindow; ++k)
+                v[k] = p - k >= 0 ? ld_status(status + (p - k) * kRadix + tid) : kStPre;  // before tile 0: none
+            int used = kLookWindow;  // window entries consumed
+            bool done = false, wait = false;
+#pragma unroll
+            for (int k = 0; k < kLookWindow; ++k) {
+                if (!done && !wait) {
+                    const uint32_t f = v[k] & ~kStVal;
+                    if (f == 0u) {
+                        wait = true;  // tile p - k has published nothing yet
+                        used = k;
+                    } else {
+                        pre += v[k] & kStVal;
+                        if (f == kStPre) {
+                            done = true;
+                            used = k + 1;
+                        }
+                    }
+                }
+            }
+            if (done) break;
+            p -= used;
+            if (wait) {
                 if (++spins > kSpinLimit) {
                     atomicCAS(d_err, kDevOk, kDevTimeout);
                     break;
                 }
                 __nanosleep(32);
-                continue;
+            } else {
+                spins = 0;
             }
-            spins = 0;
-            pre += v & kStVal;
-            if (f == kStPre || p == 0) break;
-            --p;
         }
         st_status(my, kStPre | ((pre + cnt) & kStVal));
     }
