@@ -201,7 +201,7 @@ __device__ __forceinline__ uint32_t ld_status(const uint32_t* p) {
 // tile_ctr one counter, both zero at launch.  A look-back that polls one word kSpinLimit
 // times (which needs an earlier tile that never publishes) records kDevTimeout in *d_err and
 // goes on, so the kernel always ends.
-__global__ void __launch_bounds__(kThreads) k_onesweep(KeyPtrs kin, KeyOutPtrs kout, int K,
+__global__ void __launch_bounds__(kThreads, 3) k_onesweep(KeyPtrs kin, KeyOutPtrs kout, int K,
                                                        const uint32_t* __restrict__ pin,
                                                        uint32_t* __restrict__ pout, int dw, int sh,
                                                        int64_t n, const uint32_t* __restrict__ goff,
@@ -224,19 +224,23 @@ __global__ void __launch_bounds__(kThreads) k_onesweep(KeyPtrs kin, KeyOutPtrs k
     const int64_t t = s_t;
     const int64_t base = t * kTile + (int64_t)w * (kItems * kWarp) + lane;
     const uint32_t* dword = kin.w[dw];
-    uint32_t dg[kItems];
     uint32_t lp[kItems];
+    uint32_t key[kItems];  // the digit word of every item, loaded before any ranking step waits
 #pragma unroll
     for (int r = 0; r < kItems; ++r) {
         const int64_t i = base + r * kWarp;
-        const uint32_t d = (i < n) ? ((dword[i] >> sh) & 255u) : (uint32_t)kRadix;
+        key[r] = (i < n) ? dword[i] : 0u;
+    }
+#pragma unroll
+    for (int r = 0; r < kItems; ++r) {
+        const int64_t i = base + r * kWarp;
+        const uint32_t d = (i < n) ? ((key[r] >> sh) & 255u) : (uint32_t)kRadix;
         const uint32_t peers = __match_any_sync(kFull, d);
         const uint32_t rank = __popc(peers & lanemask_lt());
         const uint32_t b = wcnt[w][d];
         __syncwarp();
         if (rank == 0) wcnt[w][d] = b + __popc(peers);
         __syncwarp();
-        dg[r] = d;
         lp[r] = b + rank;
     }
     __syncthreads();
@@ -316,11 +320,13 @@ __global__ void __launch_bounds__(kThreads) k_onesweep(KeyPtrs kin, KeyOutPtrs k
     go[tid] = (int32_t)(goff[tid] + pre) - (int32_t)excl;
     __syncthreads();
 
+    const int64_t n_here = n - base;  // items of this thread with r * kWarp < n_here are valid
 #pragma unroll
     for (int r = 0; r < kItems; ++r) {
-        if (dg[r] < (uint32_t)kRadix) {
-            lp[r] = tdo[dg[r]] + wcnt[w][dg[r]] + lp[r];
-            sd[lp[r]] = (uint8_t)dg[r];
+        if (r * kWarp < n_here) {
+            const uint32_t dr = (key[r] >> sh) & 255u;
+            lp[r] = tdo[dr] + wcnt[w][dr] + lp[r];
+            sd[lp[r]] = (uint8_t)dr;
         }
     }
     const int tile_n = (int)((n - t * kTile) < kTile ? (n - t * kTile) : kTile);
@@ -328,9 +334,20 @@ __global__ void __launch_bounds__(kThreads) k_onesweep(KeyPtrs kin, KeyOutPtrs k
         const uint32_t* src = (a < K) ? kin.w[a] : pin;
         uint32_t* dst = (a < K) ? kout.w[a] : pout;
         __syncthreads();
+        if (a == dw) {  // the digit word is already in registers
 #pragma unroll
-        for (int r = 0; r < kItems; ++r) {
-            if (dg[r] < (uint32_t)kRadix) stage[lp[r]] = src[base + r * kWarp];
+            for (int r = 0; r < kItems; ++r)
+                if (r * kWarp < n_here) stage[lp[r]] = key[r];
+        } else {
+            uint32_t v[kItems];
+#pragma unroll
+            for (int r = 0; r < kItems; ++r) {
+                const int64_t i = base + r * kWarp;
+                v[r] = (i < n) ? src[i] : 0u;
+            }
+#pragma unroll
+            for (int r = 0; r < kItems; ++r)
+                if (r * kWarp < n_here) stage[lp[r]] = v[r];
         }
         __syncthreads();
         for (int j = tid; j < tile_n; j += kThreads) {
