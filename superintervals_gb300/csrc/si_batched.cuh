@@ -30,8 +30,9 @@ struct BatchedParams {
     int64_t split_len = 2048;    // candidates at least this long form the tile's long list
     int eytz_depth = 0;          // 0: automatic
     // emit: copy the section of a tile's long candidates that comes from the long-interval list
-    // (all hits but a few) as runs with 16-byte stores instead of filtering each candidate
-    bool emit_copy = true;
+    // (all hits but a few) as runs between its misses instead of checking each candidate (the
+    // check measured faster on configuration 3; the autotuner tries both)
+    bool emit_copy = false;
     // pick tile_q per batch (emit without a count-pass cache) from the batch's intervals per
     // query and hits per query, so that a tile's candidates fit its shared memory
     bool auto_tile = true;
@@ -63,6 +64,7 @@ struct BatchedWorkspace {
     DBuf kw[3], kalt[3], pay, palt, sort_tmp;
     DBuf qpair;                  // (start, end) per query, interleaved: one sector per gather
     DBuf blk_cut;                // per 256 sorted queries: (p_cut, long-list end) or -1, for the tiles
+    DBuf bwin;                   // per 256 sorted queries: the prepare kernel's search windows
     DBuf qminmax;                // smallest and largest query end (key packing)
     // sorted query records
     DBuf sq_s, sq_u, sq_c, sq_id;
