@@ -1313,84 +1313,6 @@ __global__ void k_qkeys(const S* __restrict__ qs, const S* __restrict__ qe, cons
 }
 
 constexpr int kPrepWindow = 2048;  // starts staged per block by the cooperative search
-constexpr int64_t kNoWindow = INT64_MIN;  // a block whose windows the prepare kernel finds itself
-
-// Search windows of every block of 256 sorted queries, from the block's first and last packed
-// key alone (one thread per block, all blocks at once, so that no block of the prepare kernel
-// waits on dependent searches).  A packed key holds the class code over the query end's offset
-// from the batch's smallest end, shifted right by `shift`, so a block of one short or long class
-// has its ends inside [e_lo, e_hi] (the key range widened to whole key steps).  Per block, 6
-// values: the upper bounds of e_lo and e_hi (every query's upper bound lies between them); the
-// first sorted end >= e_lo - long_len and >= e_hi (a short query's start is > e_lo - long_len and
-// <= its end, so its rank among the sorted ends lies between); the first position whose start is
-// within long_split of e_lo - long_len and the first long-list index at or after it (a superset
-// of the tile's own candidate range).  Blocks of mixed or other classes get kNoWindow.
-template <typename S>
-__global__ void k_block_windows(const uint32_t* __restrict__ swc, int64_t nq, int ebits, int shift,
-                                const int* __restrict__ d_pack, const unsigned long long* __restrict__ mm,
-                                MapView<S> m, UbView<S> U, int64_t long_len, int64_t long_split,
-                                const int32_t* __restrict__ long_pos, const int64_t* __restrict__ long_seg,
-                                const S* __restrict__ end_sorted, int64_t* __restrict__ bw) {
-    const int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (b * kThreads >= nq) return;
-    if (d_pack) {  // worked out on the device
-        shift = d_pack[0];
-        ebits = d_pack[1];
-    }
-    int64_t* o = bw + 6 * b;
-    const int64_t j0 = b * kThreads, j1 = (j0 + kThreads < nq ? j0 + kThreads : nq) - 1;
-    const uint32_t k0 = swc[j0], k1 = swc[j1];
-    const uint32_t c0 = k0 >> ebits, c1 = k1 >> ebits;
-    const int G = m.G;
-    if (c0 != c1 || c0 >= 2u * (uint32_t)G) {
-        o[0] = kNoWindow;
-        return;
-    }
-    const int g = code_contig(c0, G);
-    const int64_t lo = m.seg[g], n = m.seg[g + 1] - lo;
-    if (n <= 0) {
-        o[0] = kNoWindow;
-        return;
-    }
-    const uint32_t emask = ebits >= 32 ? ~0u : ((1u << ebits) - 1u);
-    unsigned long long elo = mm[0] + ((unsigned long long)(k0 & emask) << shift);
-    unsigned long long ehi = mm[0] + ((unsigned long long)(k1 & emask) << shift) + ((1ull << shift) - 1ull);
-    if (ehi > mm[1]) ehi = mm[1];
-    if (elo > ehi) elo = ehi;
-    const S e_lo = (S)(int64_t)(elo ^ 0x8000000000000000ull), e_hi = (S)(int64_t)(ehi ^ 0x8000000000000000ull);
-    const S* tr = (U.mode == 1) ? U.eytz_keys + (int64_t)g * U.eytz_n : nullptr;
-    const S* st = m.starts + lo;
-    o[0] = ub_search(U, g, st, n, e_lo, tr);
-    o[1] = ub_search(U, g, st, n, e_hi, tr);
-    // smallest start a query of the block may have (long queries: any)
-    const S qs_lo = (c0 < (uint32_t)G && (uint64_t)e_lo - (uint64_t)Lim<S>::lo > (uint64_t)long_len)
-                        ? (S)((uint64_t)e_lo - (uint64_t)long_len)
-                        : Lim<S>::lo;
-    auto first_geq = [](const S* arr, int64_t a, int64_t z, S key) {
-        while (a < z) {
-            const int64_t mid = (a + z) >> 1;
-            if (arr[mid] < key) a = mid + 1;
-            else z = mid;
-        }
-        return a;
-    };
-    o[2] = end_sorted ? first_geq(end_sorted, lo, lo + n, qs_lo) : 0;
-    o[3] = end_sorted ? first_geq(end_sorted, lo, lo + n, e_hi) : 0;
-    int64_t pc = -1, ch = -1;
-    if (long_pos && c0 < (uint32_t)G) {
-        pc = first_geq(m.starts, lo, lo + n, near_threshold<S>(qs_lo, long_split));
-        int64_t a = long_seg[g], z = long_seg[g + 1];
-        while (a < z) {
-            const int64_t mid = (a + z) >> 1;
-            if ((int64_t)long_pos[mid] < pc) a = mid + 1;
-            else z = mid;
-        }
-        ch = a;
-    }
-    o[4] = pc;
-    o[5] = ch;
-}
-
 
 // Prepare the sorted batch: gather each query's record and find its upper bound.  A block
 // holds 256 consecutive sorted queries; when they share one class/contig code (the usual
@@ -1410,7 +1332,7 @@ __global__ void __launch_bounds__(kThreads, 6) k_qprep(const uint32_t* __restric
                                                     const int32_t* __restrict__ long_pos,
                                                     const int64_t* __restrict__ long_seg,
                                                     int64_t* __restrict__ blk_cut, const S* __restrict__ end_sorted,
-                                                    uint32_t* __restrict__ counts, const int64_t* __restrict__ bw) {
+                                                    uint32_t* __restrict__ counts) {
     __shared__ S win[kPrepWindow];
     __shared__ S s_mn[kWarpsPerCta], s_mx[kWarpsPerCta], s_mq[kWarpsPerCta], s_xq[kWarpsPerCta];
     __shared__ int64_t s_a, s_b, s_ra, s_rb;
@@ -1452,23 +1374,7 @@ __global__ void __launch_bounds__(kThreads, 6) k_qprep(const uint32_t* __restric
     // has start > end
     const bool rank_count = counts != nullptr && end_sorted != nullptr;
     const bool rank_block = rank_count && uniform && cfirst < 2u * (uint32_t)m.G && n > 0;
-    const bool windowed = uniform && bw != nullptr && bw[6 * blockIdx.x] != kNoWindow;
-    if (windowed) {
-        // the windows found by k_block_windows
-        if (tid == 0) {
-            const int64_t* o = bw + 6 * blockIdx.x;
-            s_a = o[0];
-            s_b = o[1];
-            s_ra = o[2];
-            s_rb = o[3];
-            if (blk_cut) {
-                blk_cut[2 * blockIdx.x] = o[4];
-                blk_cut[2 * blockIdx.x + 1] = o[5];
-            }
-        }
-        __syncthreads();
-    }
-    if (uniform && !windowed) {
+    if (uniform) {
         S mn = valid ? v : Lim<S>::hi, mx = valid ? v : Lim<S>::lo, mq = valid ? vs : Lim<S>::hi;
         S xq = valid ? vs : Lim<S>::lo;
 #pragma unroll
@@ -1528,8 +1434,6 @@ __global__ void __launch_bounds__(kThreads, 6) k_qprep(const uint32_t* __restric
             }
         }
         __syncthreads();
-    }
-    if (uniform) {
         if (n > 0) {
             const int64_t a0 = s_a < 0 ? 0 : s_a, b0 = s_b;
             if (b0 < a0) {
@@ -2116,25 +2020,13 @@ int batched_prepare_queries(BatchedWorkspace& ws, MapView<S> m, const QueryBatch
     const uint32_t* swc = in_alt ? ka[Kp - 1] : kp[Kp - 1];
     UbView<S> U = make_ub<S>(ws, ub_mode);
     SI_OKR(ws.blk_cut.reserve(2 * sizeof(int64_t) * (size_t)nblk(nq)));
-    const int64_t* bw = nullptr;
-    if (packed) {
-        // every block's search windows at once, from its first and last key
-        SI_OKR(ws.bwin.reserve(6 * sizeof(int64_t) * (size_t)nblk(nq)));
-        k_block_windows<S><<<nblk(nblk(nq)), kThreads, 0, st>>>(
-            swc, nq, ebits, shift, d_pack, ws.qminmax.as<unsigned long long>(), m, U, ws.prm.long_len, ws.long_split,
-            ws.long_pos, ws.long_seg, static_cast<const S*>(ws.end_sorted), ws.bwin.as<int64_t>());
-        note_launch();
-        SI_CU(cudaGetLastError());
-        bw = ws.bwin.as<int64_t>();
-        ws.launches += 1;
-    }
     k_qprep<S><<<nblk(nq), kThreads, 0, st>>>(spay, swc, packed ? ebits : 0, d_pack, static_cast<const S*>(q.qs),
                                               static_cast<const S*>(q.qe), packed ? ws.qpair.as<S>() : nullptr,
                                               nq, m, U, ws.sq_s.as<S>(), ws.sq_u.as<int32_t>(),
                                               ws.sq_c.as<uint32_t>(), ws.sq_id.as<int32_t>(), d_err, ws.long_split,
                                               ws.long_pos, ws.long_seg,
                                               (tile_cuts && ws.long_pos) ? ws.blk_cut.as<int64_t>() : nullptr,
-                                              static_cast<const S*>(ws.end_sorted), counts, bw);
+                                              static_cast<const S*>(ws.end_sorted), counts);
     note_launch();
     SI_CU(cudaGetLastError());
     ws.launches += 2 + 2 + passes + 1;  // keys, min/max, histogram, digit offsets, passes, prepare

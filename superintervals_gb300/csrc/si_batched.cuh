@@ -64,7 +64,6 @@ struct BatchedWorkspace {
     DBuf kw[3], kalt[3], pay, palt, sort_tmp;
     DBuf qpair;                  // (start, end) per query, interleaved: one sector per gather
     DBuf blk_cut;                // per 256 sorted queries: (p_cut, long-list end) or -1, for the tiles
-    DBuf bwin;                   // per 256 sorted queries: the prepare kernel's search windows
     DBuf qminmax;                // smallest and largest query end (key packing)
     // sorted query records
     DBuf sq_s, sq_u, sq_c, sq_id;
