@@ -363,6 +363,9 @@ def run_gpu(args, rank, world, dist):
             e2e_step()
         e2e_s = (time.perf_counter() - t0) / k
         res["e2e_s"] = max_over_ranks(e2e_s, dist)
+        free_b, tot_b = C.c_size_t(0), C.c_size_t(0)
+        _capi.check(lib.deviceMemInfoGpu(local_device(), C.byref(free_b), C.byref(tot_b)))
+        res["e2e_chunks"] = -(-4 * P // max(tot_b.value // 16, 4 << 30))   # the library's default chunk budget
         res["h2d_bytes"] = wl.q_starts.nbytes + wl.q_ends.nbytes + (wl.q_contig.nbytes if hq_c else 0)
         res["d2h_bytes"] = 8 * (nq + 1) + 4 * P
         # the host link this box gives, copied the way the e2e call copies its result: 4 GiB
@@ -1233,7 +1236,7 @@ def main():
         line["e2e"] = {"value": world * nq / res["e2e_s"], "unit": "queries/s",
                        "h2d_bytes_per_step": res["h2d_bytes"], "d2h_bytes_per_step": res["d2h_bytes"],
                        "pairs_per_s": world * P / res["e2e_s"], "d2h_link_GBps": res.get("d2h_link_GBps"),
-                       "ms_per_step": 1e3 * res["e2e_s"]}
+                       "ms_per_step": 1e3 * res["e2e_s"], "result_chunks": res.get("e2e_chunks")}
     if not args.no_cpu:
         nth = host_threads()
         keep = len(res["gpu_prefix"][0]) - 1 if "gpu_prefix" in res else 0

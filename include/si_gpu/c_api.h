@@ -185,9 +185,11 @@ int getBatchedOptionGpu(const gSuperIntervals* si, int option, int64_t* value);
 int autotuneBatchedGpu(gSuperIntervals* si, const void* d_qs, const void* d_qe,
                        const int32_t* d_qcontig, size_t nq, size_t sample, int flags, char* report,
                        size_t report_len);
-/* Device bytes one host-buffer search call may use for a result chunk (4 GiB by
- * default); larger results are emitted in query chunks against it, two chunk
- * buffers alternating so that emit and device-to-host copy overlap. */
+/* Device bytes one host-buffer search call may use for a result chunk (by default
+ * 1/16 of the device's memory, at least 4 GiB); larger results are emitted in
+ * query chunks against it, two chunk buffers alternating so that emit and
+ * device-to-host copy overlap.  Each chunk's emit visits every tile of the batch,
+ * so fewer, larger chunks cost less GPU time. */
 int setOutputBudgetGpu(gSuperIntervals* si, size_t bytes);
 /* Per-phase device time of the query pipeline, measured with CUDA events on
  * the stream the phase runs on while profiling is on (it synchronizes after

@@ -772,6 +772,14 @@ int createSuperIntervalsGpu(gSuperIntervals** out, int coord_bits, int device) {
     auto* si = new gSuperIntervals();
     si->bits = coord_bits;
     si->device = device;
+    {
+        // result chunks of host-buffer searches: 1/16 of the device's memory (at least 4 GiB), so
+        // that a result of tens of GB takes a few emit passes over the batch's tiles, not dozens
+        size_t free_b = 0, total_b = 0;
+        if (cudaMemGetInfo(&free_b, &total_b) == cudaSuccess)
+            si->out_budget = std::max(si->out_budget, total_b / 16);
+        cudaGetLastError();
+    }
     e = cudaStreamCreateWithFlags(&si->st, cudaStreamNonBlocking);
     if (e != cudaSuccess) {
         delete si;
