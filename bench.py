@@ -38,13 +38,15 @@ sys.path.insert(0, ROOT)
 
 METRIC = ("overlap queries/s + result pairs/s on 1 GB300; % HBM peak; batched+learned vs plain")
 METRIC_SERVE = "serving loop on 1 GB300: queries/s (saturated) and p50/p99 request latency at the offered rate"
-ROW_OPS = ["intersect", "difference", "coverage", "keys", "bed_ingest"]
+ROW_OPS = ["intersect", "difference", "coverage", "keys", "count", "bed_ingest"]
 ROW_DEFAULT_SCALE = 0.25   # full-size intersection pieces (25.5e9 x 12 B) would not fit in HBM
 METRIC_UB = "upper-bound queries/s on 1 GB300: learned two-stage index vs binary search, bit-identical"
 PEAK_FALLBACK_GBS = 6800.0
-# DRAM bytes (read + write) of one emit launch, from one ncu capture (dram__bytes_read.sum +
-# dram__bytes_write.sum) of exactly this workload: (config, scale, path) -> bytes per launch
-EMIT_TRAFFIC = {("config3", 1.0, "batched"): 115.25e9}
+# DRAM traffic of the emit kernel per unit, from an ncu capture of dram__bytes_write.sum and
+# dram__bytes_read.sum on configuration 3's density (profiles/k_tiles_config3_dram.md): writes
+# scale with result pairs, reads with queries
+EMIT_DRAM_WRITE_PER_PAIR = 3.974
+EMIT_DRAM_READ_PER_QUERY = 183.3
 
 
 def parse():
@@ -66,7 +68,7 @@ def parse():
     ap.add_argument("--op", default=None, choices=["search_idxs", "upper_bound"] + ROW_OPS,
                     help="search_idxs (default); upper_bound (default for config4, whose full-size "
                          "result, ~2.9e13 pairs, cannot be materialised); or one of the operations "
-                         "built on the path (intersect, difference, coverage, keys, bed_ingest)")
+                         "built on the path (intersect, difference, coverage, keys, count, bed_ingest)")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default batched-path tunables")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
@@ -369,14 +371,14 @@ def run_gpu(args, rank, world, dist):
         res["h2d_bytes"] = wl.q_starts.nbytes + wl.q_ends.nbytes + (wl.q_contig.nbytes if hq_c else 0)
         res["d2h_bytes"] = 8 * (nq + 1) + 4 * P
         # the host link this box gives, copied the way the e2e call copies its result: 4 GiB
-        # device-to-host chunks (the default output budget) into the same pinned buffer, over
-        # up to 16 GiB, best of several repeats (the first also maps the fresh device buffer)
+        # device-to-host copies into the same pinned buffer, over the whole result span, best
+        # of two repeats (the first also maps the fresh device buffer)
         chunk = min(4 * P, 4 << 30)
         if chunk >= (64 << 20):
-            span = min(4 * P, 16 << 30)
+            span = 4 * P
             d_tmp = dalloc(chunk)
             best = None
-            for _ in range(4):
+            for _ in range(2):
                 t0 = time.perf_counter()
                 for off_b in range(0, span - chunk + 1, chunk):
                     _capi.check(lib.memcpyGpu(C.c_void_p(h_out.value + off_b), d_tmp, chunk, st))
@@ -652,8 +654,13 @@ def run_gpu_rows(args, op, rank, world, dist):
         if op == "keys":
             return lib.searchKeysDeviceGpu(idx.h, d_qs, d_qe, d_qc, nq, 1, d_off, out[0], out[1], out[2], cap,
                                            C.byref(total), st)
+        if op == "count":
+            return lib.countOverlapsDeviceGpu(idx.h, d_qs, d_qe, d_qc, nq, out[0], st)
         return lib.coverageDeviceGpu(idx.h, d_qs, d_qe, d_qc, nq, out[0], out[1], st)
-    if op == "coverage":
+    if op == "count":
+        out[0] = dalloc(4 * nq)
+        P = nq
+    elif op == "coverage":
         out[0], out[1] = dalloc(8 * nq), dalloc(s_bytes * nq)
         P = nq
     else:
@@ -697,6 +704,9 @@ def run_gpu_rows(args, op, rank, world, dist):
 def rows_algorithmic_bytes(op, Q, H, P, s):
     """Bytes the operation must move: every query read once and, per hit, the hit interval
     read and the output written."""
+    if op == "count":
+        # the survey's count bytes: query read, count written, one end read per hit
+        return Q * (2 * s + 4) + H * s, "Q(2s+4) + H*s"
     if op == "intersect":
         return Q * (2 * s + 8) + H * (2 * s) + P * (2 * s + 4), "Q(2s+8) + H(2s) + P(2s+4)"
     if op == "difference":
@@ -725,6 +735,8 @@ def rows_cpu(op, wl, seconds, nth):
             o.difference(m, qs[:k], qe[:k])
         elif op == "coverage":
             o.coverage(m, qs[:k], qe[:k])
+        elif op == "count":
+            o.count_batch(m, qs[:k], qe[:k], nthreads=nth)
         else:
             o.search_batch(m, qs[:k], qe[:k], order=1, values=True, nthreads=nth)
     probe = min(len(sel), 2000)
@@ -735,7 +747,7 @@ def rows_cpu(op, wl, seconds, nth):
     t0 = time.perf_counter()
     run(k)
     dt = time.perf_counter() - t0
-    threads = nth if op == "keys" else 1
+    threads = nth if op in ("keys", "count") else 1
     return {"q_per_s": k / dt, "sample_q": k, "threads": threads}
 
 
@@ -743,14 +755,14 @@ def rows_line(args, op, res, world):
     Q, H, P, s = res["nq"], res["hits"], res["out"], res["s_bytes"]
     ms = res["ms_per_step"]
     peak, peak_kind = measured_peak()
-    algo, formula = rows_algorithmic_bytes(op, Q, H, 0 if op == "coverage" else P, s)
+    algo, formula = rows_algorithmic_bytes(op, Q, H, 0 if op in ("coverage", "count") else P, s)
     wl = res["wl"]
     line = {"metric": f"{op} queries/s on 1 GB300 (device-resident)", "value": world * Q / (ms / 1e3),
             "unit": "queries/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "int64" if s == 8 else "int32", "data": "synthetic (seeded)",
             "config": dict(workload_desc(args.config, wl), op=op, scale=res["scale"],
-                           hits=H, outputs=P if op != "coverage" else Q),
+                           hits=H, outputs=P if op not in ("coverage", "count") else Q),
             "roofline": {"bound": "hbm", "achieved": algo / (ms / 1e3) / 1e9, "peak": peak, "unit": "GB/s",
                          "frac": algo / (ms / 1e3) / 1e9 / peak, "traffic": None, "peak_kind": peak_kind,
                          "algorithmic_bytes": algo, "formula": formula + " (Q queries, H hits, P outputs)"},
@@ -1216,9 +1228,12 @@ def main():
     emit_ms = ph[2] if ph[2] > 0 else ms
     algo = nq * (2 * s + 8) + P * (s + 4)
     achieved = algo / (emit_ms / 1000.0) / 1e9
-    traffic = None if args.contigs else EMIT_TRAFFIC.get((cfg, args.scale, args.path))
+    traffic = (EMIT_DRAM_WRITE_PER_PAIR * P + EMIT_DRAM_READ_PER_QUERY * nq
+               if cfg == "config3" and args.path == "batched" else None)
     line["roofline"] = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                         "frac": achieved / peak, "traffic": traffic, "kernel": "emit",
+                        "traffic_source": "per-unit DRAM bytes of profiles/k_tiles_config3_dram.md x this run's "
+                                          "P and Q" if traffic else None,
                         "traffic_frac": (traffic / (emit_ms / 1000.0) / 1e9 / peak) if traffic else None,
                         "peak_kind": peak_kind, "algorithmic_bytes": algo,
                         "phase_ms": {"count": ph[0], "scan": ph[1], "emit": ph[2], "prepare": ph[3]},

@@ -136,7 +136,17 @@ def test_reference_arm_rows(op):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("op", ["intersect", "difference", "coverage", "keys", "bed_ingest"])
+@pytest.mark.parametrize("op", ["intersect", "difference", "coverage", "keys", "count", "bed_ingest"])
 def test_bench_rows_gpu(op):
     (line,) = _run(["--op", op, "--scale", "0.004", "--steps", "2", "--warmup", "1", "--cpu-seconds", "0.3"])
     assert line["value"] > 0 and line["gpu_launches"] > 0 and "cpu_baseline" in line
+
+
+def test_emit_traffic_figures_match_their_profile():
+    """roofline.traffic is the per-unit DRAM traffic of the emit kernel, measured with ncu and
+    summarised under profiles/, scaled by the run's pairs and queries: the constants in bench.py
+    must be the ones that summary states."""
+    import bench
+    text = open(os.path.join(ROOT, "profiles", "k_tiles_config3_dram.md")).read()
+    assert f"**{bench.EMIT_DRAM_WRITE_PER_PAIR:.3f} B**" in text
+    assert f"**{bench.EMIT_DRAM_READ_PER_QUERY:.1f} B**" in text
