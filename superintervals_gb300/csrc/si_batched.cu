@@ -1268,27 +1268,74 @@ __global__ void k_pack_params(const unsigned long long* __restrict__ mm, int cod
 
 // One 32-bit key per query: class code above the end's offset from the batch's smallest end,
 // shifted right by `shift` (tiles need queries grouped by class and contig and close in
-// position, not exactly ordered).  Also writes (start, end) interleaved for the prepare pass.
+// position, not exactly ordered).  Also writes (start, end) interleaved for the prepare pass
+// and, with ghist, the counts of the key's three low bytes for the radix sort (the key has at
+// most 24 bits; byte 3 is counted by the caller).  Grid-stride, four queries per thread in
+// flight so that enough loads are outstanding to cover memory latency.
 template <typename S>
-__global__ void k_qkeys_packed(const S* __restrict__ qs, const S* __restrict__ qe, const int32_t* __restrict__ qc,
-                               int64_t nq, int64_t long_len, int G, const unsigned long long* __restrict__ mm,
-                               int shift, int ebits, const int* __restrict__ d_pack, uint32_t* __restrict__ key,
-                               uint32_t* __restrict__ pay, S* __restrict__ qpair) {
-    const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (q >= nq) return;
+__global__ void __launch_bounds__(kThreads) k_qkeys_packed(const S* __restrict__ qs, const S* __restrict__ qe,
+                                                           const int32_t* __restrict__ qc, int64_t nq,
+                                                           int64_t long_len, int G,
+                                                           const unsigned long long* __restrict__ mm, int shift,
+                                                           int ebits, const int* __restrict__ d_pack,
+                                                           uint32_t* __restrict__ key, uint32_t* __restrict__ pay,
+                                                           S* __restrict__ qpair, uint32_t* __restrict__ ghist) {
+    constexpr int U = 4;
+    __shared__ uint32_t h[3 * 256];
+    const int tid = threadIdx.x;
+    if (ghist) {
+        for (int i = tid; i < 3 * 256; i += kThreads) h[i] = 0;
+        __syncthreads();
+    }
     if (d_pack) {  // worked out on the device
         shift = d_pack[0];
         ebits = d_pack[1];
     }
-    const int32_t g = qc ? qc[q] : 0;
-    const S s = qs[q], e = qe[q];
-    const bool is_long = ((double)e - (double)s + 1.0) > (double)long_len;
-    const uint32_t code = query_code(g, G, s > e, is_long);
-    const unsigned long long rel = ((unsigned long long)(int64_t)e ^ 0x8000000000000000ull) - mm[0];
-    key[q] = (code << ebits) | (uint32_t)(rel >> shift);
-    pay[q] = (uint32_t)q;
-    qpair[2 * q] = s;
-    qpair[2 * q + 1] = e;
+    const unsigned long long m0 = mm[0];
+    const int64_t stride = (int64_t)gridDim.x * kThreads * U;
+    for (int64_t q0 = (int64_t)blockIdx.x * kThreads * U + tid; q0 < nq; q0 += stride) {
+        S s[U], e[U];
+        int32_t g[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int64_t q = q0 + u * kThreads;
+            g[u] = 0;
+            s[u] = 0;
+            e[u] = 0;
+            if (q < nq) {
+                g[u] = qc ? qc[q] : 0;
+                s[u] = qs[q];
+                e[u] = qe[q];
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int64_t q = q0 + u * kThreads;
+            if (q >= nq) continue;
+            const bool is_long = ((double)e[u] - (double)s[u] + 1.0) > (double)long_len;
+            const uint32_t code = query_code(g[u], G, s[u] > e[u], is_long);
+            const unsigned long long rel = ((unsigned long long)(int64_t)e[u] ^ 0x8000000000000000ull) - m0;
+            const uint32_t k = (code << ebits) | (uint32_t)(rel >> shift);
+            key[q] = k;
+            pay[q] = (uint32_t)q;
+            if constexpr (sizeof(S) == 4) {
+                reinterpret_cast<int2*>(qpair)[q] = make_int2((int)s[u], (int)e[u]);
+            } else {
+                reinterpret_cast<longlong2*>(qpair)[q] = make_longlong2((long long)s[u], (long long)e[u]);
+            }
+            if (ghist) {
+                atomicAdd(&h[k & 255u], 1u);
+                atomicAdd(&h[256 + ((k >> 8) & 255u)], 1u);
+                atomicAdd(&h[512 + ((k >> 16) & 255u)], 1u);
+            }
+        }
+    }
+    if (ghist) {
+        __syncthreads();
+        for (int i = tid; i < 3 * 256; i += kThreads)
+            if (h[i]) atomicAdd(&ghist[i], h[i]);
+        if (blockIdx.x == 0 && tid == 0) atomicAdd(&ghist[3 * 256], (uint32_t)nq);  // byte 3: all zero
+    }
 }
 
 template <typename S>
@@ -1334,6 +1381,7 @@ __global__ void __launch_bounds__(kThreads, 6) k_qprep(const uint32_t* __restric
                                                     int64_t* __restrict__ blk_cut, const S* __restrict__ end_sorted,
                                                     uint32_t* __restrict__ counts) {
     __shared__ S win[kPrepWindow];
+    __shared__ S win2[kPrepWindow];  // the sorted ends between the block's two ranks
     __shared__ S s_mn[kWarpsPerCta], s_mx[kWarpsPerCta], s_mq[kWarpsPerCta], s_xq[kWarpsPerCta];
     __shared__ int64_t s_a, s_b, s_ra, s_rb;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -1348,9 +1396,16 @@ __global__ void __launch_bounds__(kThreads, 6) k_qprep(const uint32_t* __restric
     if (valid) {
         orig = pay[j];
         cw = wc[j] >> code_shift;
-        if (qpair) {
-            v = qpair[2 * (int64_t)orig + 1];
-            vs = qpair[2 * (int64_t)orig];
+        if (qpair) {  // one 8- or 16-byte load of the record
+            if constexpr (sizeof(S) == 4) {
+                const int2 r = reinterpret_cast<const int2*>(qpair)[orig];
+                vs = r.x;
+                v = r.y;
+            } else {
+                const longlong2 r = reinterpret_cast<const longlong2*>(qpair)[orig];
+                vs = r.x;
+                v = r.y;
+            }
         } else {
             v = qe[orig];
             vs = qs[orig];
@@ -1434,14 +1489,22 @@ __global__ void __launch_bounds__(kThreads, 6) k_qprep(const uint32_t* __restric
             }
         }
         __syncthreads();
+        // both windows (the starts between the two upper bounds, the sorted ends between the two
+        // ranks) are staged together, behind one barrier
+        const int64_t a0 = s_a < 0 ? 0 : s_a, b0 = s_b;
+        const bool win_ok = n > 0 && b0 >= a0 && b0 - a0 + 1 <= kPrepWindow;
+        const int64_t A = rank_block ? s_ra : 0, B = rank_block ? s_rb : 0;
+        const bool staged = rank_block && B - A <= kPrepWindow;
+        if (win_ok)
+            for (int64_t k = a0 + tid; k <= b0; k += kThreads) win[k - a0] = m.starts[lo + k];
+        if (staged)
+            for (int64_t k = tid; k < B - A; k += kThreads) win2[k] = end_sorted[A + k];
+        if (win_ok || staged) __syncthreads();
         if (n > 0) {
-            const int64_t a0 = s_a < 0 ? 0 : s_a, b0 = s_b;
             if (b0 < a0) {
                 done = true;  // every end of the block precedes the contig's first start
                 u = -1;
-            } else if (b0 - a0 + 1 <= kPrepWindow) {
-                for (int64_t k = a0 + tid; k <= b0; k += kThreads) win[k - a0] = m.starts[lo + k];
-                __syncthreads();
+            } else if (win_ok) {
                 if (valid && !bad) u = a0 + ub_range(win, (int64_t)0, b0 - a0, v);
                 done = true;
             } else if (valid && !bad) {
@@ -1452,17 +1515,11 @@ __global__ void __launch_bounds__(kThreads, 6) k_qprep(const uint32_t* __restric
             done = true;
         }
         if (rank_block) {
-            __syncthreads();  // win is reused for the ends between the two ranks
-            const int64_t A = s_ra, B = s_rb;
-            const bool staged = B - A <= kPrepWindow;
-            if (staged)
-                for (int64_t k = tid; k < B - A; k += kThreads) win[k] = end_sorted[A + k];
-            __syncthreads();
             if (valid) {
                 int64_t b0 = 0, b1 = B - A;  // first index of the window whose end is >= qs
                 while (b0 < b1) {
                     const int64_t mid = (b0 + b1) >> 1;
-                    const S e = staged ? win[mid] : end_sorted[A + mid];
+                    const S e = staged ? win2[mid] : end_sorted[A + mid];
                     if (e < vs) b0 = mid + 1;
                     else b1 = mid;
                 }
@@ -1795,6 +1852,15 @@ __global__ void k_eytz_build(const S* __restrict__ starts, const int64_t* __rest
 
 inline unsigned nblk(int64_t n, int t = kThreads) { return (unsigned)std::max<int64_t>(1, ceil_div(n, t)); }
 
+// Blocks of `threads` that fit on the whole device at once (one wave of a grid-stride kernel).
+static int64_t resident_blocks(const void* fn, int threads) {
+    int dev = 0, nsm = 152, per_sm = 1;
+    if (cudaGetDevice(&dev) != cudaSuccess) return 152;
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, 0);
+    return (int64_t)nsm * std::max(per_sm, 1);
+}
+
 template <typename S>
 Pyr<S> make_pyr(MapView<S> m, Levels<S> L, int H) {
     Pyr<S> P;
@@ -2001,10 +2067,13 @@ int batched_prepare_queries(BatchedWorkspace& ws, MapView<S> m, const QueryBatch
         Kp = 1;
         wc = kp[0];
         SI_OKR(ws.qpair.reserve(2 * sizeof(S) * nq));
-        k_qkeys_packed<S><<<nblk(nq), kThreads, 0, st>>>(static_cast<const S*>(q.qs), static_cast<const S*>(q.qe),
-                                                         q.qc, nq, ws.prm.long_len, m.G,
-                                                         ws.qminmax.as<unsigned long long>(), shift, ebits, d_pack,
-                                                         kp[0], ws.pay.as<uint32_t>(), ws.qpair.as<S>());
+        // the sort's digit histograms are counted by the key kernel (radix_sort skips its own pass)
+        SI_CU(cudaMemsetAsync(radix_hist(ws.sort_tmp.p), 0, sizeof(uint32_t) * 4 * 256, st));
+        const int64_t kb = resident_blocks(reinterpret_cast<const void*>(&k_qkeys_packed<S>), kThreads);
+        k_qkeys_packed<S><<<(unsigned)std::min<int64_t>(nblk(nq, 4 * kThreads), kb), kThreads, 0, st>>>(
+            static_cast<const S*>(q.qs), static_cast<const S*>(q.qe), q.qc, nq, ws.prm.long_len, m.G,
+            ws.qminmax.as<unsigned long long>(), shift, ebits, d_pack, kp[0], ws.pay.as<uint32_t>(),
+            ws.qpair.as<S>(), radix_hist(ws.sort_tmp.p));
     } else {
         k_qkeys<S><<<nblk(nq), kThreads, 0, st>>>(static_cast<const S*>(q.qs), static_cast<const S*>(q.qe), q.qc,
                                                   nq, ws.prm.long_len, m.G, kp[0], K == 3 ? kp[1] : nullptr, wc,
@@ -2015,7 +2084,7 @@ int batched_prepare_queries(BatchedWorkspace& ws, MapView<S> m, const QueryBatch
     bool in_alt = false;
     int passes = 0;
     SI_CU(radix_sort(kp, ka, ws.pay.as<uint32_t>(), ws.palt.as<uint32_t>(), Kp, nq, ws.sort_tmp.p, tb, &in_alt,
-                     &passes, st, ws.capturing ? 0x7u : 0u, d_err));
+                     &passes, st, ws.capturing ? 0x7u : 0u, d_err, packed));
     const uint32_t* spay = in_alt ? ws.palt.as<uint32_t>() : ws.pay.as<uint32_t>();
     const uint32_t* swc = in_alt ? ka[Kp - 1] : kp[Kp - 1];
     UbView<S> U = make_ub<S>(ws, ub_mode);
@@ -2029,7 +2098,8 @@ int batched_prepare_queries(BatchedWorkspace& ws, MapView<S> m, const QueryBatch
                                               static_cast<const S*>(ws.end_sorted), counts);
     note_launch();
     SI_CU(cudaGetLastError());
-    ws.launches += 2 + 2 + passes + 1;  // keys, min/max, histogram, digit offsets, passes, prepare
+    // keys, min/max, histogram (counted by the key kernel when packed), digit offsets, passes, prepare
+    ws.launches += 2 + (packed ? 1 : 2) + passes + 1;
     ws.prepared_qs = q.qs;
     ws.prepared_nq = nq;
     ws.prepared_mode = ub_mode;

@@ -165,6 +165,9 @@ struct gSuperIntervals {
     // set operations: hit lists, staged pieces, and whether some interval has start > end
     DevBuf so_hoff, so_hits, so_off, so_os, so_oe, so_ob, so_flag;
     int inverted = -1;  // -1 unknown, else 0 / 1 (reset by every build)
+    // mean number of intervals at least 65536 long over a position (set by every build): hits
+    // of such intervals lie far apart in position order, so one walk per query is long
+    double long_depth = 0.0;
     // contig names, in contig-id order, when the intervals came from BED text
     std::vector<std::string> contig_names;
     // options
@@ -265,6 +268,7 @@ sig::MapView<S> view(const gSuperIntervals* si) {
     m.seg = si->seg.as<int64_t>();
     m.G = si->G;
     m.n = si->n;
+    m.end_sorted = (si->inverted == 0) ? static_cast<const S*>(si->bws.end_sorted) : nullptr;
     return m;
 }
 
@@ -411,12 +415,18 @@ int build_impl(gSuperIntervals* si) {
     // from which the batched path counts short queries (two ranks per query)
     {
         DevBuf flag2;
-        SI_TRY(flag2.reserve(sizeof(int)));
+        SI_TRY(flag2.reserve(sizeof(int) + 2 * sizeof(double)));
+        double* sums = reinterpret_cast<double*>(flag2.as<char>() + 8);
         SI_CK(sig::launch_any_inverted<S>(view<S>(si), flag2.as<int>(), st));
+        SI_CK(sig::launch_long_depth<S>(si->starts.as<S>(), si->ends.as<S>(), n, si->seg.as<int64_t>(), G,
+                                         sig::kLongIntervalSplit, sums, st));
         int f = 0;
+        double h[2] = {0.0, 0.0};
         SI_CK(cudaMemcpyAsync(&f, flag2.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+        SI_CK(cudaMemcpyAsync(h, sums, sizeof(h), cudaMemcpyDeviceToHost, st));
         SI_CK(cudaStreamSynchronize(st));
         si->inverted = f ? 1 : 0;
+        si->long_depth = h[1] > 0.0 ? h[0] / h[1] : 0.0;
     }
     if (si->inverted == 0) {
         const int K = sig::end_key_words<S>(G);
@@ -475,15 +485,22 @@ int read_dev_err(gSuperIntervals* si, cudaStream_t st = nullptr) {
     return SI_OK;
 }
 
-bool use_batched(const gSuperIntervals* si, int64_t nq) {
+// The automatic choice: the batched path for batches of 4096+ queries; for smaller ones the plain
+// path (one warp per query), except that searches (emit) over an index whose long intervals
+// nest deeply (kDeepLong or more over a position on average) take the batched path, which
+// gathers long candidates per tile instead of walking to each one.
+constexpr double kDeepLong = 32.0;
+bool use_batched(const gSuperIntervals* si, int64_t nq, bool emit = false) {
     if (si->path == SI_PATH_PLAIN) return false;
     if (si->path == SI_PATH_BATCHED) return true;
-    return nq >= 4096 && si->n >= 4096;
+    if (si->n < 4096) return false;
+    return nq >= 4096 || (emit && si->long_depth >= kDeepLong);
 }
 
 // count into d_counts (device) for device-resident queries
 template <typename S>
-int run_count(gSuperIntervals* si, const sig::QueryBatch& q, uint32_t* d_counts, cudaStream_t st) {
+int run_count(gSuperIntervals* si, const sig::QueryBatch& q, uint32_t* d_counts, cudaStream_t st,
+              bool for_emit = false) {
     SI_TRY(si->w_err.reserve(sizeof(int)));
     SI_CK(cudaMemsetAsync(si->w_err.p, 0, sizeof(int), st));
     if (si->n == 0) {
@@ -491,7 +508,7 @@ int run_count(gSuperIntervals* si, const sig::QueryBatch& q, uint32_t* d_counts,
         SI_CK(sig::launch_check_contigs(q.qc, q.nq, si->G, si->w_err.as<int>(), st));
         return SI_OK;
     }
-    if (use_batched(si, q.nq)) {
+    if (use_batched(si, q.nq, for_emit)) {
         {
             PhaseTimer pt(si, 3, st);
             int r = sig::batched_prepare_queries<S>(si->bws, view<S>(si), q, si->w_err.as<int>(), si->ub_mode, st,
@@ -515,7 +532,7 @@ int run_emit(gSuperIntervals* si, const sig::QueryBatch& q, int64_t q_offset, co
              int64_t out_base, int order, bool values, int32_t* d_out, cudaStream_t st, int64_t total_hits) {
     if (si->n == 0 || q.nq == 0) return SI_OK;
     PhaseTimer pt(si, 2, st);
-    if (use_batched(si, q.nq + q_offset)) {
+    if (use_batched(si, q.nq + q_offset, true)) {
         int r = sig::batched_emit<S>(si->bws, view<S>(si), levels<S>(si), si->H, q, q_offset, d_offsets, out_base,
                                      order, values, d_out, si->w_err.as<int>(), si->ub_mode, st, total_hits);
         if (r != SI_OK) return fail(r, "batched emit failed (status %d)", r);
@@ -534,7 +551,7 @@ int search_device(gSuperIntervals* si, const sig::QueryBatch& q, int order, bool
     SI_TRY(set_dev(si));
     SI_TRY(si->w_counts.reserve(sizeof(uint32_t) * std::max<int64_t>(q.nq, 1)));
     SI_TRY(si->w_tmp.reserve(sig::scan_temp_bytes(q.nq)));
-    SI_TRY(run_count<S>(si, q, si->w_counts.as<uint32_t>(), st));
+    SI_TRY(run_count<S>(si, q, si->w_counts.as<uint32_t>(), st, true));
     {
         PhaseTimer pt(si, 1, st);
         SI_CK(sig::exclusive_scan_u32_to_i64(si->w_counts.as<uint32_t>(), d_offsets, q.nq, si->w_tmp.p, st, si->w_err.as<int>()));
@@ -595,7 +612,7 @@ int search_host(gSuperIntervals* si, const S* qs, const S* qe, const int32_t* qc
     SI_TRY(si->w_counts.reserve(sizeof(uint32_t) * std::max<size_t>(nq, 1)));
     SI_TRY(si->w_offsets.reserve(sizeof(int64_t) * (nq + 1)));
     SI_TRY(si->w_tmp.reserve(sig::scan_temp_bytes((int64_t)nq)));
-    SI_TRY(run_count<S>(si, q, si->w_counts.as<uint32_t>(), st));
+    SI_TRY(run_count<S>(si, q, si->w_counts.as<uint32_t>(), st, true));
     int64_t* d_off = si->w_offsets.as<int64_t>();
     {
         PhaseTimer pt(si, 1, st);
@@ -1521,7 +1538,7 @@ int capture_batched(gSuperIntervals* si, const sig::QueryBatch& q, int order, in
     SI_CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
     ws.capturing = true;
     ws.out_cap = (int64_t)capacity;
-    int r = run_count<S>(si, q, si->w_counts.as<uint32_t>(), st);
+    int r = run_count<S>(si, q, si->w_counts.as<uint32_t>(), st, true);
     cudaError_t e = cudaSuccess;
     if (r == SI_OK)
         e = sig::exclusive_scan_u32_to_i64(si->w_counts.as<uint32_t>(), d_offsets, nq, si->w_tmp.p, st, si->w_err.as<int>());
@@ -1571,7 +1588,7 @@ extern "C" int searchDeviceGraphGpu(gSuperIntervals* si, const void* d_qs, const
     SI_TRY(si->w_counts.reserve(sizeof(uint32_t) * nq));
     SI_TRY(si->w_tmp.reserve(sig::scan_temp_bytes((int64_t)nq)));
     // batched when the handle would take it for this batch and the key packs on the device
-    const bool batched = use_batched(si, (int64_t)nq) && si->bits == 32 && sig::query_code_bits(si->G) <= 8 &&
+    const bool batched = use_batched(si, (int64_t)nq, true) && si->bits == 32 && sig::query_code_bits(si->G) <= 8 &&
                          nq < (size_t)INT32_MAX;
     const void* key[8] = {d_qs, d_qe, d_qc, d_offsets, d_values, (const void*)st, si->w_counts.p, si->w_tmp.p};
     const size_t key_n[5] = {nq, capacity, (size_t)order, (size_t)batched, (size_t)g_alloc_gen.load()};
@@ -1619,7 +1636,7 @@ int hit_lists(gSuperIntervals* si, const sig::QueryBatch& q, int order, cudaStre
     SI_TRY(si->so_hoff.reserve(sizeof(int64_t) * (q.nq + 1)));
     SI_TRY(si->w_counts.reserve(sizeof(uint32_t) * std::max<int64_t>(q.nq, 1)));
     SI_TRY(si->w_tmp.reserve(sig::scan_temp_bytes(q.nq)));
-    SI_TRY(run_count<S>(si, q, si->w_counts.as<uint32_t>(), st));
+    SI_TRY(run_count<S>(si, q, si->w_counts.as<uint32_t>(), st, true));
     SI_CK(sig::exclusive_scan_u32_to_i64(si->w_counts.as<uint32_t>(), si->so_hoff.as<int64_t>(), q.nq, si->w_tmp.p,
                                          st, si->w_err.as<int>()));
     int64_t P = 0;

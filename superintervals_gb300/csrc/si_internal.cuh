@@ -116,10 +116,13 @@ size_t radix_temp_bytes(int64_t n, int K);
 // With d_err (a device error word) each pass is one kernel with decoupled look-back across
 // tiles (one-sweep); a wait that gives up records kDevTimeout there.  Without it, each pass is
 // a tile histogram, a scan and a scatter.
+// With hist_ready the caller has already written the digit histograms of every key byte into
+// radix_hist(temp) (K x 4 x 256 counts, byte b of word w at (4w + b) x 256).
 cudaError_t radix_sort(uint32_t* const* keys, uint32_t* const* alt_keys, uint32_t* payload,
                        uint32_t* alt_payload, int K, int64_t n, void* temp, size_t temp_bytes,
                        bool* result_in_alt, int* passes_run, cudaStream_t st, uint32_t pass_mask = 0,
-                       int* d_err = nullptr);
+                       int* d_err = nullptr, bool hist_ready = false);
+uint32_t* radix_hist(void* temp);
 
 // ---------------------------------------------------------------- build
 template <typename S>
@@ -201,6 +204,10 @@ cudaError_t launch_end_keys(const S* ends, int64_t n, const int64_t* seg, int G,
                             cudaStream_t st);
 template <typename S>
 cudaError_t launch_end_decode(const uint32_t* const* kw, int64_t n, int64_t n_pad, S* out, cudaStream_t st);
+// out[0] = total length of intervals at least X long, out[1] = total contig extent (sorted starts)
+template <typename S>
+cudaError_t launch_long_depth(const S* starts, const S* ends, int64_t n, const int64_t* seg, int G, int64_t X,
+                              double* out, cudaStream_t st);
 
 // ---------------------------------------------------------------- query launchers (si_query.cu)
 struct QueryBatch {
@@ -221,6 +228,7 @@ struct MapView {
     const int64_t* seg;
     int32_t G;
     int64_t n;
+    const S* end_sorted = nullptr;  // each contig's ends ascending; only when no interval has start > end
 };
 
 // set operations over hit lists (CSR of contig-local positions): intersection pieces (kept when

@@ -231,11 +231,18 @@ __global__ void __launch_bounds__(kThreads, 3) k_onesweep(KeyPtrs kin, KeyOutPtr
         const int64_t i = base + r * kWarp;
         key[r] = (i < n) ? dword[i] : 0u;
     }
+    // every round's peer mask first (independent of one another), then the chain of
+    // per-warp digit counters through shared memory
+#pragma unroll
+    for (int r = 0; r < kItems; ++r) {
+        const int64_t i = base + r * kWarp;
+        lp[r] = __match_any_sync(kFull, (i < n) ? ((key[r] >> sh) & 255u) : (uint32_t)kRadix);
+    }
 #pragma unroll
     for (int r = 0; r < kItems; ++r) {
         const int64_t i = base + r * kWarp;
         const uint32_t d = (i < n) ? ((key[r] >> sh) & 255u) : (uint32_t)kRadix;
-        const uint32_t peers = __match_any_sync(kFull, d);
+        const uint32_t peers = lp[r];
         const uint32_t rank = __popc(peers & lanemask_lt());
         const uint32_t b = wcnt[w][d];
         __syncwarp();
@@ -372,10 +379,12 @@ size_t radix_temp_bytes(int64_t n, int K) {
     return b + std::max(three, one) + 1024;
 }
 
+uint32_t* radix_hist(void* temp) { return static_cast<uint32_t*>(temp); }
+
 cudaError_t radix_sort(uint32_t* const* keys, uint32_t* const* alt_keys, uint32_t* payload,
                        uint32_t* alt_payload, int K, int64_t n, void* temp, size_t temp_bytes,
                        bool* result_in_alt, int* passes_run, cudaStream_t st, uint32_t pass_mask,
-                       int* d_err) {
+                       int* d_err, bool hist_ready) {
     *result_in_alt = false;
     if (passes_run) *passes_run = 0;
     if (n <= 1) return cudaSuccess;
@@ -402,14 +411,16 @@ cudaError_t radix_sort(uint32_t* const* keys, uint32_t* const* alt_keys, uint32_
     cudaError_t e = cudaSuccess;
     uint32_t hh[kMaxKeyWords * 4 * kRadix];
     if (!pass_mask || one) {
-        e = cudaMemsetAsync(ghist, 0, sizeof(uint32_t) * K * 4 * kRadix, st);
-        if (e != cudaSuccess) return e;
-        KeyPtrs kp{};
-        for (int w = 0; w < K; ++w) kp.w[w] = keys[w];
-        int gblocks = (int)std::min<int64_t>(ceil_div(n, kThreads), 152 * 8);
-        k_global_hist<<<gblocks, kThreads, 0, st>>>(kp, K, n, ghist);
-        note_launch();
-        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        if (!hist_ready) {
+            e = cudaMemsetAsync(ghist, 0, sizeof(uint32_t) * K * 4 * kRadix, st);
+            if (e != cudaSuccess) return e;
+            KeyPtrs kp{};
+            for (int w = 0; w < K; ++w) kp.w[w] = keys[w];
+            int gblocks = (int)std::min<int64_t>(ceil_div(n, kThreads), 152 * 8);
+            k_global_hist<<<gblocks, kThreads, 0, st>>>(kp, K, n, ghist);
+            note_launch();
+            if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        }
         if (one) {
             k_digit_offsets<<<K * 4, kRadix, 0, st>>>(ghist, goff);
             note_launch();

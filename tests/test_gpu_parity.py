@@ -32,7 +32,7 @@ def _index(api, starts, ends, data=None, seg=None, path="plain"):
     idx = api.GpuIndex(bits)
     idx.add_arrays(starts, ends, data, seg=seg)
     idx.build()
-    idx.set_path(api.PATH_PLAIN if path == "plain" else api.PATH_BATCHED)
+    idx.set_path({"plain": api.PATH_PLAIN, "batched": api.PATH_BATCHED, "auto": api.PATH_AUTO}[path])
     return idx
 
 
@@ -195,6 +195,34 @@ def test_query_classes_both_count_modes(api, oracle, inverted_intervals):
         wl.starts[inv], wl.ends[inv] = wl.ends[inv].copy(), wl.starts[inv].copy()
         assert (wl.starts > wl.ends).any()
     _oracle_case(api, oracle, wl, "batched", orders=(0, 1))
+
+
+@pytest.mark.parametrize("path", ["plain", "auto"])
+@pytest.mark.parametrize("inverted_intervals", [False, True])
+@pytest.mark.parametrize("nq", [1, 20_000, 40_000])
+def test_small_batches_dense(api, oracle, inverted_intervals, nq, path):
+    """Small batches at the headline density (chr21's share of configuration 3, ~500 hits per
+    query from deeply nested 1-5 Mb intervals).  On the plain path, batches of up to 32768 queries
+    take one warp per query: the count from two ranks (no interval with start > end and query
+    start <= end) or a 32-wide ballot walk that skips misses through the branch array, and the
+    emit's 32-wide head run and walk; larger batches one thread per query.  The automatic path
+    sends searches of fewer than 4096 queries over such deeply nested long intervals to the
+    batched path and their counts to the plain one.  Some queries have start > end, and in one
+    case some intervals too."""
+    import dataclasses
+    from superintervals_gb300 import workloads as W
+    wl = W.config3_subset(["chr21"])
+    r = np.random.default_rng(11)
+    qs, qe = wl.q_starts[:nq].copy(), wl.q_ends[:nq].copy()
+    flip = r.random(nq) < 0.03
+    qs[flip], qe[flip] = qe[flip].copy(), qs[flip].copy()
+    starts, ends = wl.starts.copy(), wl.ends.copy()
+    if inverted_intervals:
+        inv = r.random(wl.n) < 0.005
+        starts[inv], ends[inv] = ends[inv].copy(), starts[inv].copy()
+    small = dataclasses.replace(wl, starts=starts, ends=ends, q_starts=qs, q_ends=qe,
+                                q_contig=None if wl.q_contig is None else wl.q_contig[:nq].copy())
+    _oracle_case(api, oracle, small, path, orders=(0, 1))
 
 
 @pytest.mark.parametrize("path", PATHS)
