@@ -231,18 +231,11 @@ __global__ void __launch_bounds__(kThreads, 3) k_onesweep(KeyPtrs kin, KeyOutPtr
         const int64_t i = base + r * kWarp;
         key[r] = (i < n) ? dword[i] : 0u;
     }
-    // every round's peer mask first (independent of one another), then the chain of
-    // per-warp digit counters through shared memory
-#pragma unroll
-    for (int r = 0; r < kItems; ++r) {
-        const int64_t i = base + r * kWarp;
-        lp[r] = __match_any_sync(kFull, (i < n) ? ((key[r] >> sh) & 255u) : (uint32_t)kRadix);
-    }
 #pragma unroll
     for (int r = 0; r < kItems; ++r) {
         const int64_t i = base + r * kWarp;
         const uint32_t d = (i < n) ? ((key[r] >> sh) & 255u) : (uint32_t)kRadix;
-        const uint32_t peers = lp[r];
+        const uint32_t peers = __match_any_sync(kFull, d);
         const uint32_t rank = __popc(peers & lanemask_lt());
         const uint32_t b = wcnt[w][d];
         __syncwarp();
