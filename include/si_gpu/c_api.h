@@ -247,8 +247,9 @@ int searchDeviceGpu(gSuperIntervals* si, const void* d_qs, const void* d_qe,
 /* Allocation-free search.  No counterpart in the reference: it exists for callers
  * that cannot allocate device memory while they query (a host whose device memory
  * belongs to another allocator or a fixed pool, or a query thread that must not
- * call cudaMalloc).  Same result as searchDeviceGpu with values_not_idxs = 0 (the
- * plain one-query-per-thread path), into caller-provided device buffers; the
+ * call cudaMalloc).  Same result as searchDeviceGpu with values_not_idxs = 0 (on
+ * the plain path: one warp per query up to 32,768 queries, one thread per query
+ * above), into caller-provided device buffers; the
  * scratch it needs sits in one fixed device array inside the library (about
  * 16.1 MiB, held on every device that loads the library until exit), so the call
  * performs no cudaMalloc / cudaFree.  Limit: at most 4,194,304 queries per call
@@ -256,7 +257,8 @@ int searchDeviceGpu(gSuperIntervals* si, const void* d_qs, const void* d_qe,
  * that overlap on the GPU race and must be serialized by the caller.  The first
  * call on a device looks the array up on that device; make it before any stream
  * capture.  Every call reads the result size back into host memory and waits for
- * `stream`, so it returns with the search finished.  A result larger than
+ * `stream`, so it returns with the search finished (and no call can be captured
+ * into a graph).  A result larger than
  * `capacity` returns SI_ERR_CAPACITY with the offsets and *total filled and
  * nothing written to d_values, which may be NULL only with capacity 0.  The index
  * must already be built. */
