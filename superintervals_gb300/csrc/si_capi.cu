@@ -149,6 +149,8 @@ struct gSuperIntervals {
     // ranks; built by the first such call after a build
     DevBuf ps_start, ps_end;
     bool cov_ready = false;
+    DevBuf rec;             // the intervals as (start, end, payload) records, made on first use
+    bool rec_ready = false;
     DevBuf long_lvl[sig::kMaxLevels];
     int64_t long_sizes[sig::kMaxLevels + 1] = {0};
     int long_H = 0;
@@ -272,6 +274,22 @@ sig::MapView<S> view(const gSuperIntervals* si) {
     return m;
 }
 
+// The view with the interval records, made on the first call after a build: the operations
+// that read every field of each hit (set operations, keys, coverage) read one record per hit.
+template <typename S>
+int view_rec(gSuperIntervals* si, cudaStream_t st, sig::MapView<S>* out) {
+    *out = view<S>(si);
+    if (si->n <= 0) return SI_OK;
+    if (!si->rec_ready) {
+        SI_TRY(si->rec.reserve(sizeof(sig::IvRec<S>) * (size_t)si->n));
+        SI_CK(sig::launch_records<S>(si->starts.as<S>(), si->ends.as<S>(), si->data.as<int32_t>(), si->n,
+                                     si->rec.as<sig::IvRec<S>>(), st));
+        si->rec_ready = true;
+    }
+    out->rec = si->rec.as<sig::IvRec<S>>();
+    return SI_OK;
+}
+
 template <typename S>
 sig::Levels<S> levels(const gSuperIntervals* si) {
     sig::Levels<S> L;
@@ -296,6 +314,7 @@ int build_impl(gSuperIntervals* si) {
     si->bws.long_ends = nullptr;  // set again once the long-interval list exists
     si->bws.end_sorted = nullptr;
     si->cov_ready = false;
+    si->rec_ready = false;
     if (si->gexec) {              // a captured graph holds the old buffers
         cudaGraphExecDestroy(si->gexec);
         si->gexec = nullptr;
@@ -1682,6 +1701,8 @@ int setop_device(gSuperIntervals* si, const sig::QueryBatch& q, int op, int orde
     if (op == 1) sequential = si->inverted == 1;
     const int64_t* hoff = si->so_hoff.as<int64_t>();
     const int32_t* hits = si->so_hits.as<int32_t>();
+    sig::MapView<S> rv;
+    SI_TRY(view_rec<S>(si, st, &rv));
     if (op == 0 && si->inverted == 0) {
         // with start <= end for every interval and every query, each hit gives one piece:
         // the pieces' offsets are the hits' offsets and no counting pass is needed
@@ -1705,7 +1726,7 @@ int setop_device(gSuperIntervals* si, const sig::QueryBatch& q, int op, int orde
             }
             if (P > 0 && (!d_os || !d_oe || !d_ob)) return fail(SI_ERR_INVALID, "null output buffer");
             if (P > 0)
-                SI_CK(sig::launch_isect<S>(view<S>(si), q, hoff, hits, nullptr, d_off, d_os, d_oe, d_ob,
+                SI_CK(sig::launch_isect<S>(rv, q, hoff, hits, nullptr, d_off, d_os, d_oe, d_ob,
                                            si->w_err.as<int>(), st));
             return read_dev_err(si, st);
         }
@@ -1714,9 +1735,9 @@ int setop_device(gSuperIntervals* si, const sig::QueryBatch& q, int op, int orde
     SI_TRY(si->w_tmp.reserve(sig::scan_temp_bytes(q.nq)));
     uint32_t* cnt = si->w_counts.as<uint32_t>();
     if (op == 0)
-        SI_CK(sig::launch_isect<S>(view<S>(si), q, hoff, hits, cnt, nullptr, nullptr, nullptr, nullptr, si->w_err.as<int>(), st));
+        SI_CK(sig::launch_isect<S>(rv, q, hoff, hits, cnt, nullptr, nullptr, nullptr, nullptr, si->w_err.as<int>(), st));
     else
-        SI_CK(sig::launch_diff<S>(view<S>(si), q, hoff, hits, sequential, cnt, nullptr, nullptr, nullptr, si->w_err.as<int>(), st));
+        SI_CK(sig::launch_diff<S>(rv, q, hoff, hits, sequential, cnt, nullptr, nullptr, nullptr, si->w_err.as<int>(), st));
     SI_CK(sig::exclusive_scan_u32_to_i64(cnt, d_off, q.nq, si->w_tmp.p, st, si->w_err.as<int>()));
     int64_t T = 0;
     SI_CK(cudaMemcpyAsync(&T, d_off + q.nq, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
@@ -1726,9 +1747,9 @@ int setop_device(gSuperIntervals* si, const sig::QueryBatch& q, int op, int orde
     if (T > 0 && (!d_os || !d_oe || (op == 0 && !d_ob))) return fail(SI_ERR_INVALID, "null output buffer");
     if (T > 0) {
         if (op == 0)
-            SI_CK(sig::launch_isect<S>(view<S>(si), q, hoff, hits, nullptr, d_off, d_os, d_oe, d_ob, si->w_err.as<int>(), st));
+            SI_CK(sig::launch_isect<S>(rv, q, hoff, hits, nullptr, d_off, d_os, d_oe, d_ob, si->w_err.as<int>(), st));
         else
-            SI_CK(sig::launch_diff<S>(view<S>(si), q, hoff, hits, sequential, nullptr, d_off, d_os, d_oe, si->w_err.as<int>(), st));
+            SI_CK(sig::launch_diff<S>(rv, q, hoff, hits, sequential, nullptr, d_off, d_os, d_oe, si->w_err.as<int>(), st));
     }
     return read_dev_err(si, st);
 }
@@ -1757,11 +1778,13 @@ int setop_host(gSuperIntervals* si, const S* qs, const S* qe, const int32_t* qc,
     // the hit lists are still in place: emit the pieces only
     const int64_t* hoff = si->so_hoff.as<int64_t>();
     const int32_t* hits = si->so_hits.as<int32_t>();
+    sig::MapView<S> rv;
+    SI_TRY(view_rec<S>(si, si->st, &rv));
     if (op == 0)
-        SI_CK(sig::launch_isect<S>(view<S>(si), q, hoff, hits, nullptr, si->so_off.as<int64_t>(), si->so_os.as<S>(),
+        SI_CK(sig::launch_isect<S>(rv, q, hoff, hits, nullptr, si->so_off.as<int64_t>(), si->so_os.as<S>(),
                                    si->so_oe.as<S>(), si->so_ob.as<int32_t>(), si->w_err.as<int>(), si->st));
     else
-        SI_CK(sig::launch_diff<S>(view<S>(si), q, hoff, hits, si->inverted == 1, nullptr, si->so_off.as<int64_t>(),
+        SI_CK(sig::launch_diff<S>(rv, q, hoff, hits, si->inverted == 1, nullptr, si->so_off.as<int64_t>(),
                                   si->so_os.as<S>(), si->so_oe.as<S>(), si->w_err.as<int>(), si->st));
     if (!h_os || !h_oe || (op == 0 && !h_ob)) return fail(SI_ERR_INVALID, "null output buffer");
     SI_CK(cudaMemcpyAsync(h_os, si->so_os.p, sizeof(S) * T, cudaMemcpyDeviceToHost, si->st));
@@ -1875,7 +1898,9 @@ int keys_device(gSuperIntervals* si, const sig::QueryBatch& q, int order, int64_
     }
     if (P > 0) {
         if (!d_s || !d_e) return fail(SI_ERR_INVALID, "null output buffer");
-        SI_CK(sig::launch_keys<S>(view<S>(si), q, si->so_hoff.as<int64_t>(), si->so_hits.as<int32_t>(), d_s, d_e,
+        sig::MapView<S> rv;
+        SI_TRY(view_rec<S>(si, st, &rv));
+        SI_CK(sig::launch_keys<S>(rv, q, si->so_hoff.as<int64_t>(), si->so_hits.as<int32_t>(), d_s, d_e,
                                   d_d, st));
     }
     SI_CK(cudaStreamSynchronize(st));
@@ -1932,7 +1957,9 @@ int coverage_device(gSuperIntervals* si, const sig::QueryBatch& q, uint64_t* d_c
     }
     int64_t P = 0;
     SI_TRY(lists_or_empty<S>(si, q, SI_ORDER_DESC, st, &P));
-    SI_CK(sig::launch_coverage<S>(view<S>(si), q, si->so_hoff.as<int64_t>(), si->so_hits.as<int32_t>(), d_count,
+    sig::MapView<S> rv;
+    SI_TRY(view_rec<S>(si, st, &rv));
+    SI_CK(sig::launch_coverage<S>(rv, q, si->so_hoff.as<int64_t>(), si->so_hits.as<int32_t>(), d_count,
                                   d_cov, st));
     SI_CK(cudaStreamSynchronize(st));
     SI_CK(cudaGetLastError());
@@ -1982,12 +2009,16 @@ extern "C" int searchKeysBatchGpu(gSuperIntervals* si, const void* qs, const voi
     SI_TRY(si->so_oe.reserve(sb * T));
     if (data) SI_TRY(si->so_ob.reserve(sizeof(int32_t) * T));
     // the hit lists are still in place: gather only
+    sig::MapView<int64_t> rv64;
+    sig::MapView<int32_t> rv32;
+    if (si->bits == 64) SI_TRY(view_rec<int64_t>(si, si->st, &rv64));
+    else SI_TRY(view_rec<int32_t>(si, si->st, &rv32));
     if (si->bits == 64)
-        SI_CK(sig::launch_keys<int64_t>(view<int64_t>(si), q, si->so_hoff.as<int64_t>(), si->so_hits.as<int32_t>(),
+        SI_CK(sig::launch_keys<int64_t>(rv64, q, si->so_hoff.as<int64_t>(), si->so_hits.as<int32_t>(),
                                         si->so_os.as<int64_t>(), si->so_oe.as<int64_t>(),
                                         data ? si->so_ob.as<int32_t>() : nullptr, si->st));
     else
-        SI_CK(sig::launch_keys<int32_t>(view<int32_t>(si), q, si->so_hoff.as<int64_t>(), si->so_hits.as<int32_t>(),
+        SI_CK(sig::launch_keys<int32_t>(rv32, q, si->so_hoff.as<int64_t>(), si->so_hits.as<int32_t>(),
                                         si->so_os.as<int32_t>(), si->so_oe.as<int32_t>(),
                                         data ? si->so_ob.as<int32_t>() : nullptr, si->st));
     SI_CK(cudaMemcpyAsync(starts, si->so_os.p, sb * T, cudaMemcpyDeviceToHost, si->st));

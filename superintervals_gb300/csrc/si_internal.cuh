@@ -219,6 +219,22 @@ struct QueryBatch {
 
 enum Order : int { kOrderIdxsCpp = 0, kOrderDesc = 1 };
 
+// One interval as one aligned record (start, end, payload): the operations that read all of a
+// hit's fields (intersection, difference, keys, coverage) then make one memory transaction per
+// hit instead of one per field.
+template <typename S>
+struct IvRec;
+template <>
+struct alignas(16) IvRec<int32_t> {
+    int32_t s, e, d, pad;
+};
+template <>
+struct alignas(32) IvRec<int64_t> {
+    int64_t s, e;
+    int32_t d, pad;
+    int64_t pad2;
+};
+
 template <typename S>
 struct MapView {
     const S* starts;
@@ -229,7 +245,13 @@ struct MapView {
     int32_t G;
     int64_t n;
     const S* end_sorted = nullptr;  // each contig's ends ascending; only when no interval has start > end
+    const IvRec<S>* rec = nullptr;  // the intervals as records, where an operation asked for them
 };
+
+// rec[i] = (starts[i], ends[i], data[i]) for i < n
+template <typename S>
+cudaError_t launch_records(const S* starts, const S* ends, const int32_t* data, int64_t n, IvRec<S>* rec,
+                           cudaStream_t st);
 
 // set operations over hit lists (CSR of contig-local positions): intersection pieces (kept when
 // start <= end) and difference pieces; counts when ooff is null, else writes at ooff

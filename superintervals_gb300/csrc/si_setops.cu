@@ -75,8 +75,17 @@ __global__ void __launch_bounds__(kThreads) k_isect(MapView<S> m, const S* __res
             int32_t h = 0;
             if (p < b) {
                 h = hits[p];
-                s = smax(s0, m.starts[lo + h]);
-                e = smin(e0, m.ends[lo + h]);
+                S hs, he;
+                if (m.rec) {
+                    const IvRec<S> r = m.rec[lo + h];
+                    hs = r.s;
+                    he = r.e;
+                } else {
+                    hs = m.starts[lo + h];
+                    he = m.ends[lo + h];
+                }
+                s = smax(s0, hs);
+                e = smin(e0, he);
                 keep = s <= e;
             }
             const uint32_t bal = __ballot_sync(kFull, keep);
@@ -183,8 +192,17 @@ __global__ void __launch_bounds__(kThreads) k_diff(MapView<S> m, const S* __rest
             bool cl = false;
             if (valid) {
                 const int32_t h = hits[b - 1 - t];  // ascending position order
-                cs = smax(st[h], s0);
-                const S ce = smin(en[h], e0);
+                S hs, he;
+                if (m.rec) {
+                    const IvRec<S> r = m.rec[lo + h];
+                    hs = r.s;
+                    he = r.e;
+                } else {
+                    hs = st[h];
+                    he = en[h];
+                }
+                cs = smax(hs, s0);
+                const S ce = smin(he, e0);
                 cl = ce == Lim<S>::hi;
                 nxt = cl ? Lim<S>::lo : ce + 1;
             }
@@ -234,9 +252,16 @@ __global__ void __launch_bounds__(kThreads) k_keys(MapView<S> m, const int32_t* 
         const int64_t lo = m.seg[g];
         for (int64_t p = hoff[q] + lane; p < hoff[q + 1]; p += 32) {
             const int64_t k = lo + hits[p];
-            os[p] = m.starts[k];
-            oe[p] = m.ends[k];
-            if (od) od[p] = m.data[k];
+            if (m.rec) {
+                const IvRec<S> r = m.rec[k];
+                os[p] = r.s;
+                oe[p] = r.e;
+                if (od) od[p] = r.d;
+            } else {
+                os[p] = m.starts[k];
+                oe[p] = m.ends[k];
+                if (od) od[p] = m.data[k];
+            }
         }
     }
 }
@@ -267,7 +292,16 @@ __global__ void __launch_bounds__(kThreads) k_coverage(MapView<S> m, const S* __
         U acc = 0;
         for (int64_t p = hoff[q] + lane; p < hoff[q + 1]; p += 32) {
             const int64_t k = lo + hits[p];
-            acc += (U)smin(m.ends[k], e0) - (U)smax(m.starts[k], s0);
+            S hs, he;
+            if (m.rec) {
+                const IvRec<S> r = m.rec[k];
+                hs = r.s;
+                he = r.e;
+            } else {
+                hs = m.starts[k];
+                he = m.ends[k];
+            }
+            acc += (U)smin(he, e0) - (U)smax(hs, s0);
         }
 #pragma unroll
         for (int d = 16; d > 0; d >>= 1) acc += __shfl_xor_sync(kFull, acc, d);
@@ -349,6 +383,30 @@ cudaError_t launch_coverage(MapView<S> m, QueryBatch q, const int64_t* hoff, con
 }
 
 template <typename S>
+__global__ void __launch_bounds__(kThreads) k_records(const S* __restrict__ starts, const S* __restrict__ ends,
+                                                      const int32_t* __restrict__ data, int64_t n,
+                                                      IvRec<S>* __restrict__ rec) {
+    const int64_t stride = (int64_t)gridDim.x * kThreads;
+    for (int64_t i = (int64_t)blockIdx.x * kThreads + threadIdx.x; i < n; i += stride) {
+        IvRec<S> r{};
+        r.s = starts[i];
+        r.e = ends[i];
+        r.d = data[i];
+        rec[i] = r;
+    }
+}
+
+template <typename S>
+cudaError_t launch_records(const S* starts, const S* ends, const int32_t* data, int64_t n, IvRec<S>* rec,
+                           cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    k_records<S><<<(unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(n, kThreads), 152 * 8)), kThreads, 0,
+                   st>>>(starts, ends, data, n, rec);
+    note_launch();
+    return cudaGetLastError();
+}
+
+template <typename S>
 cudaError_t launch_any_inverted(MapView<S> m, int* flag, cudaStream_t st) {
     cudaError_t e = cudaMemsetAsync(flag, 0, sizeof(int), st);
     if (e != cudaSuccess || m.n <= 0) return e;
@@ -367,7 +425,8 @@ cudaError_t launch_any_inverted(MapView<S> m, int* flag, cudaStream_t st) {
     template cudaError_t launch_keys<S>(MapView<S>, QueryBatch, const int64_t*, const int32_t*, S*, S*,        \
                                         int32_t*, cudaStream_t);                                              \
     template cudaError_t launch_coverage<S>(MapView<S>, QueryBatch, const int64_t*, const int32_t*,            \
-                                            uint64_t*, S*, cudaStream_t);
+                                            uint64_t*, S*, cudaStream_t);                                     \
+    template cudaError_t launch_records<S>(const S*, const S*, const int32_t*, int64_t, IvRec<S>*, cudaStream_t);
 SIG_SINST(int32_t)
 SIG_SINST(int64_t)
 
