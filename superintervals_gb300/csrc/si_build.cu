@@ -299,8 +299,10 @@ __global__ void __launch_bounds__(kThreads) k_branch_lookback(const S* __restric
     __shared__ S se[kBrTile];
     __shared__ S cmax[kBrTile / 32];
     __shared__ int16_t s_un[kBrTile];
+    __shared__ int16_t s_look[kBrTile];  // the ones of them that look back
     __shared__ int s_nun;
     __shared__ unsigned int s_t;
+    __shared__ S s_before;  // the largest end of every earlier tile
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     if (tid == 0) {
         s_t = atomicAdd(tile_ctr, 1u);  // tiles in start order: earlier tiles run
@@ -394,12 +396,33 @@ __global__ void __launch_bounds__(kThreads) k_branch_lookback(const S* __restric
             S m = t_max[t];
             t_pre[t] = m > pre ? m : pre;
             st_flag_release(t_flag + t, 2);
+            s_before = pre;
         }
     }
-    // positions whose end exceeds every earlier end of the tile: one warp each
+    if (tid == 0 && t == 0) s_before = Lim<S>::lo;
+    __syncthreads();
+    // positions whose end exceeds every earlier end of the tile: those above every earlier
+    // tile's ends too have none (-1); the others look back, one warp each
+    {
+        const S before = s_before;
+        const int nun0 = s_nun;
+        __syncthreads();
+        if (tid == 0) s_nun = 0;
+        __syncthreads();
+        for (int u = tid; u < nun0; u += kThreads) {
+            const int k = s_un[u];
+            const int64_t i = base + k;
+            if (se[k] > before) {
+                if (i < n) branch[i] = -1;
+            } else {
+                s_look[atomicAdd(&s_nun, 1)] = (int16_t)k;
+            }
+        }
+        __syncthreads();
+    }
     const int nun = s_nun;
     for (int u = warp; u < nun; u += kThreads / 32) {
-        const int k = s_un[u];
+        const int k = s_look[u];
         const int64_t i = base + k;
         const S e = se[k];
         const int64_t cs = G > 1 ? seg[seg_of(seg, G, i)] : 0;  // the contig's first position
