@@ -302,15 +302,21 @@ __global__ void __launch_bounds__(kThreads) k_branch_lookback(const S* __restric
     __shared__ int16_t s_look[kBrTile];  // the ones of them that look back
     __shared__ int s_nun;
     __shared__ unsigned int s_t;
-    __shared__ S s_before;  // the largest end of every earlier tile
+    __shared__ S s_before;  // the largest end of the tile's first contig before the tile
+    __shared__ int64_t s_cs[2];  // contig start of the tile's first and last position
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     if (tid == 0) {
         s_t = atomicAdd(tile_ctr, 1u);  // tiles in start order: earlier tiles run
         s_nun = 0;
+        const int64_t b = (int64_t)s_t * kBrTile;
+        const int64_t last = (b + kBrTile < n ? b + kBrTile : n) - 1;
+        s_cs[0] = G > 1 ? seg[seg_of(seg, G, b)] : 0;
+        s_cs[1] = G > 1 ? seg[seg_of(seg, G, last)] : 0;
     }
     __syncthreads();
     const int64_t t = s_t;
     const int64_t base = t * kBrTile;
+    const int64_t cs_first = s_cs[0], cs_last = s_cs[1];
     for (int k = tid; k < kBrTile; k += kThreads) {
         const int64_t p = base + k;
         se[k] = p < n_pad ? ends[p] : Lim<S>::lo;
@@ -326,12 +332,30 @@ __global__ void __launch_bounds__(kThreads) k_branch_lookback(const S* __restric
         if (lane == 0) cmax[c] = v;
     }
     __syncthreads();
-    if (tid == 0) {
-        S m = cmax[0];
-        for (int c = 1; c < kBrTile / 32; ++c) m = cmax[c] > m ? cmax[c] : m;
-        t_max[t] = m;
-        if (t == 0) t_pre[0] = m;
-        st_flag_release(t_flag + t, t == 0 ? 2 : 1);
+    // t_max: the tile's largest end.  t_pre: the largest end from the start of the contig of the
+    // tile's last position to the tile's end, published with flag 2; a tile where that contig
+    // starts publishes it at once (it needs no earlier tile), the others after the look-back.
+    if (warp == 0) {
+        S m = cmax[lane];
+        const int off = cs_last > base ? (int)(cs_last - base) : 0;  // positions of the last contig
+        S l = Lim<S>::lo;
+        if (lane * 32 >= off) {
+            l = cmax[lane];
+        } else if (lane * 32 + 31 >= off) {
+            for (int j = off - lane * 32; j < 32; ++j) l = se[lane * 32 + j] > l ? se[lane * 32 + j] : l;
+        }
+#pragma unroll
+        for (int d = 16; d > 0; d >>= 1) {
+            const S o = __shfl_xor_sync(kFull, m, d);
+            m = o > m ? o : m;
+            const S p = __shfl_xor_sync(kFull, l, d);
+            l = p > l ? p : l;
+        }
+        if (lane == 0) {
+            t_max[t] = m;
+            if (cs_last >= base) t_pre[t] = l;
+            st_flag_release(t_flag + t, cs_last >= base ? 2 : 1);
+        }
     }
     // inside the tile: the chunk by shuffles, then the tile's earlier chunks
     for (int c = warp; c < kBrTile / 32; c += kThreads / 32) {
@@ -362,8 +386,9 @@ __global__ void __launch_bounds__(kThreads) k_branch_lookback(const S* __restric
         }
     }
     __syncthreads();
-    // warp 0: this tile's inclusive prefix maximum, from the earlier tiles' published values
-    if (warp == 0 && t > 0) {
+    // warp 0: the largest end of the tile's first contig before the tile, from the earlier
+    // tiles' published values (every tile walked lies in that contig, or holds its start)
+    if (warp == 0 && cs_first < base) {
         S pre = Lim<S>::lo;
         int64_t top = t - 1;
         int spins = 0;
@@ -393,13 +418,15 @@ __global__ void __launch_bounds__(kThreads) k_branch_lookback(const S* __restric
             top -= 32;
         }
         if (lane == 0) {
-            S m = t_max[t];
-            t_pre[t] = m > pre ? m : pre;
-            st_flag_release(t_flag + t, 2);
+            if (cs_last < base) {  // one contig throughout: its prefix runs on from the earlier tiles
+                S m = t_max[t];
+                t_pre[t] = m > pre ? m : pre;
+                st_flag_release(t_flag + t, 2);
+            }
             s_before = pre;
         }
     }
-    if (tid == 0 && t == 0) s_before = Lim<S>::lo;
+    if (tid == 0 && cs_first >= base) s_before = Lim<S>::lo;
     __syncthreads();
     // positions whose end exceeds every earlier end of the tile: those above every earlier
     // tile's ends too have none (-1); the others look back, one warp each
@@ -412,7 +439,9 @@ __global__ void __launch_bounds__(kThreads) k_branch_lookback(const S* __restric
         for (int u = tid; u < nun0; u += kThreads) {
             const int k = s_un[u];
             const int64_t i = base + k;
-            if (se[k] > before) {
+            // a contig that starts inside the tile has no position before it
+            const bool first_contig = G <= 1 || i < n && seg[seg_of(seg, G, i)] == cs_first;
+            if (!first_contig || cs_first >= base || se[k] > before) {
                 if (i < n) branch[i] = -1;
             } else {
                 s_look[atomicAdd(&s_nun, 1)] = (int16_t)k;
