@@ -197,8 +197,9 @@ def test_query_classes_both_count_modes(api, oracle, inverted_intervals):
     _oracle_case(api, oracle, wl, "batched", orders=(0, 1))
 
 
-@pytest.mark.parametrize("layout", ["reads_24_contigs", "many_small_contigs"])
-def test_branch_fixed_length_reads_multicontig(api, oracle, layout):
+@pytest.mark.parametrize("layout,dt", [("reads_24_contigs", np.int32), ("many_small_contigs", np.int32),
+                                       ("many_small_contigs", np.int64)])
+def test_branch_fixed_length_reads_multicontig(api, oracle, layout, dt):
     """Fixed-length reads: every end exceeds all earlier ends of its contig, so the branch pass's
     cross-tile step decides nearly every position (-1 unless an earlier read of the same contig
     reaches it).  Its prefix maxima are per contig: a contig's first positions must not see the
@@ -215,14 +216,14 @@ def test_branch_fixed_length_reads_multicontig(api, oracle, layout):
         counts[r.random(600) < 0.1] = 0
         lens = r.integers(10_000, 2_000_000, 600)
     seg = np.concatenate([[0], np.cumsum(counts)]).astype(np.int64)
-    starts = np.concatenate([r.integers(0, ln - 200, c) for c, ln in zip(counts, lens)]).astype(np.int32)
+    starts = np.concatenate([r.integers(0, ln - 200, c) for c, ln in zip(counts, lens)]).astype(dt)
     ln = np.where(r.random(starts.size) < 0.02, 5_000, 150)      # a few longer reads
-    ends = (starts + ln - 1).astype(np.int32)
+    ends = (starts + ln - 1).astype(dt)
     n = starts.size
     qc = r.integers(0, len(counts), 20_000).astype(np.int32)
-    qs = (r.random(20_000) * lens[qc]).astype(np.int32)
+    qs = (r.random(20_000) * lens[qc]).astype(dt)
     wl = W.Workload(name=layout, starts=starts, ends=ends, data=np.arange(n, dtype=np.int32), seg=seg,
-                    q_starts=qs, q_ends=(qs + 300).astype(np.int32), q_contig=qc)
+                    q_starts=qs, q_ends=(qs + 300).astype(dt), q_contig=qc)
     _oracle_case(api, oracle, wl, "batched", orders=(0,))
 
 
