@@ -2361,6 +2361,9 @@ int bed_ingest(gSuperIntervals* si, const char* text, size_t len, int options, c
     si->built = false;
     if (m == 0) return SI_OK;
     // 1. dictionary: sort records by name hash (stable: file order inside a hash group)
+    DevBuf serr;  // the one-sweep sorts' error word (a bounded wait that gave up)
+    SI_TRY(serr.reserve(sizeof(int)));
+    SI_CK(cudaMemsetAsync(serr.p, 0, sizeof(int), st));
     DevBuf lo2, hi2, rec2, stmp;
     SI_TRY(lo2.reserve(4 * m));
     SI_TRY(hi2.reserve(4 * m));
@@ -2370,7 +2373,7 @@ int bed_ingest(gSuperIntervals* si, const char* text, size_t len, int options, c
     uint32_t* ka[2] = {lo2.as<uint32_t>(), hi2.as<uint32_t>()};
     bool alt = false;
     SI_CK(sig::radix_sort(kp, ka, B.rec.as<uint32_t>(), rec2.as<uint32_t>(), 2, m, stmp.p, stmp.bytes, &alt, nullptr,
-                          st));
+                          st, 0, serr.as<int>()));
     const uint32_t* slo = alt ? ka[0] : kp[0];
     const uint32_t* shi = alt ? ka[1] : kp[1];
     const uint32_t* perm = alt ? rec2.as<uint32_t>() : B.rec.as<uint32_t>();
@@ -2408,7 +2411,7 @@ int bed_ingest(gSuperIntervals* si, const char* text, size_t len, int options, c
     uint32_t* gka[1] = {gk2.as<uint32_t>()};
     bool galt = false;
     SI_CK(sig::radix_sort(gkp, gka, gp.as<uint32_t>(), gp2.as<uint32_t>(), 1, G, gtmp.p, gtmp.bytes, &galt, nullptr,
-                          st));
+                          st, 0, serr.as<int>()));
     const uint32_t* sorted_groups = galt ? gp2.as<uint32_t>() : gp.as<uint32_t>();
     // the sorted keys are each contig's first record, in contig order
     const uint32_t* first_rec = galt ? gka[0] : gkp[0];
@@ -2428,7 +2431,13 @@ int bed_ingest(gSuperIntervals* si, const char* text, size_t len, int options, c
     uint32_t* cka[1] = {cid2.as<uint32_t>()};
     bool calt = false;
     SI_CK(sig::radix_sort(ckp, cka, ord.as<uint32_t>(), ord2.as<uint32_t>(), 1, m, otmp.p, otmp.bytes, &calt, nullptr,
-                          st));
+                          st, 0, serr.as<int>()));
+    {
+        int se = 0;
+        SI_CK(cudaMemcpyAsync(&se, serr.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+        SI_CK(cudaStreamSynchronize(st));
+        if (se != 0) return fail(SI_ERR_CUDA, "a bounded wait in the BED sorts gave up (device error word %d)", se);
+    }
     const uint32_t* cid_sorted = calt ? cka[0] : ckp[0];
     const uint32_t* order = calt ? ord2.as<uint32_t>() : ord.as<uint32_t>();
     DevBuf os, oe, ol, seg, noff, nlen;
