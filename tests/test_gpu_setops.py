@@ -264,6 +264,22 @@ def test_keys_and_coverage_multicontig(api, oracle):
     idx.close()
 
 
+@pytest.mark.parametrize("dt", [np.int32, np.int64])
+def test_keys_records_both_widths(api, dt):
+    """Keys gathered through the (start, end, payload) records, both coordinate widths, both
+    orders, against the index's own arrays at the hit positions."""
+    from superintervals_gb300 import workloads as W
+    wl = W.random_nested(41, 20_000, 5_000, dtype=dt, span=1_000_000, max_len=20_000)
+    idx = _index(api, wl.starts, wl.ends, wl.data, path="batched")
+    bs, be, bd, _ = idx.arrays()
+    for order in (api.ORDER_DESC, api.ORDER_IDXS_CPP):
+        off, out = idx.search(wl.q_starts, wl.q_ends, order=order)
+        koff, ks, ke, kd = idx.search_keys(wl.q_starts, wl.q_ends, order=order, with_data=True)
+        assert np.array_equal(koff, off)
+        assert np.array_equal(ks, bs[out]) and np.array_equal(ke, be[out]) and np.array_equal(kd, bd[out])
+    idx.close()
+
+
 def test_python_keys_items_coverage(api):
     """The Python mirror's single-query search_keys / search_items / coverage (pyx:302-361)."""
     g = load("kat_coverage_int32")
