@@ -172,28 +172,37 @@ __global__ void k_differs_i32(const int32_t* __restrict__ a, const int32_t* __re
 
 // out[0] += total length of the intervals at least X long; out[1] += the contigs' extents (last
 // start - first start + 1 over the sorted starts).  Their ratio is the depth of long intervals.
+// Integer sums (a length is clamped to 2^40, which leaves room for 2^23 such intervals per
+// block before the 64-bit total could wrap; the ratio only steers a path choice).
 template <typename S>
 __global__ void __launch_bounds__(kThreads) k_long_depth(const S* __restrict__ starts, const S* __restrict__ ends,
                                                          int64_t n, const int64_t* __restrict__ seg, int G,
-                                                         int64_t X, double* __restrict__ out) {
-    __shared__ double red[kThreads / 32];
-    double a = 0.0, b = 0.0;
+                                                         int64_t X, unsigned long long* __restrict__ out) {
+    __shared__ unsigned long long red[kThreads / 32];
+    constexpr unsigned long long kClamp = 1ull << 40;
+    unsigned long long a = 0, b = 0;
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-        const double len = (double)ends[i] - (double)starts[i] + 1.0;
-        a += len >= (double)X ? len : 0.0;
+        const int64_t s0 = (int64_t)starts[i], e0 = (int64_t)ends[i];
+        const unsigned long long d = (unsigned long long)e0 - (unsigned long long)s0;  // e - s when e >= s
+        if (e0 >= s0 && d >= (unsigned long long)(X - 1))                                 // length >= X
+            a += d < kClamp ? d + 1ull : kClamp;
     }
     for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < G; g += stride)
-        if (seg[g + 1] > seg[g]) b += (double)starts[seg[g + 1] - 1] - (double)starts[seg[g]] + 1.0;
+        if (seg[g + 1] > seg[g]) {
+            const unsigned long long d =
+                (unsigned long long)(int64_t)starts[seg[g + 1] - 1] - (unsigned long long)(int64_t)starts[seg[g]];
+            b += d < kClamp ? d + 1ull : kClamp;
+        }
     for (int k = 0; k < 2; ++k) {
-        double v = k == 0 ? a : b;
+        unsigned long long v = k == 0 ? a : b;
         for (int d = 16; d > 0; d >>= 1) v += __shfl_xor_sync(kFull, v, d);
         if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
         __syncthreads();
         if (threadIdx.x == 0) {
-            double t = 0.0;
+            unsigned long long t = 0;
             for (int w = 0; w < kThreads / 32; ++w) t += red[w];
-            if (t != 0.0) atomicAdd(&out[k], t);
+            if (t) atomicAdd(&out[k], t);
         }
         __syncthreads();
     }
@@ -608,8 +617,8 @@ cudaError_t launch_long_scatter(const S* starts, const S* ends, int64_t n, int64
 
 template <typename S>
 cudaError_t launch_long_depth(const S* starts, const S* ends, int64_t n, const int64_t* seg, int G, int64_t X,
-                              double* out, cudaStream_t st) {
-    cudaError_t e = cudaMemsetAsync(out, 0, 2 * sizeof(double), st);
+                              unsigned long long* out, cudaStream_t st) {
+    cudaError_t e = cudaMemsetAsync(out, 0, 2 * sizeof(unsigned long long), st);
     if (e != cudaSuccess || n <= 0) return e;
     k_long_depth<S><<<(unsigned)std::min<int64_t>(blocks_for(std::max<int64_t>(n, G)), 152 * 4), kThreads, 0, st>>>(
         starts, ends, n, seg, G, X, out);
@@ -730,7 +739,8 @@ cudaError_t launch_branch(const S* ends, int64_t n, int64_t n_pad, Levels<S> L, 
     template cudaError_t launch_branch<S>(const S*, int64_t, int64_t, Levels<S>, int,           \
                                           const int64_t*, int, int32_t*, cudaStream_t, void*, int*); \
     template int end_key_words<S>(int);                                                          \
-    template cudaError_t launch_long_depth<S>(const S*, const S*, int64_t, const int64_t*, int, int64_t, double*, \
+    template cudaError_t launch_long_depth<S>(const S*, const S*, int64_t, const int64_t*, int, int64_t,         \
+                                              unsigned long long*,                                              \
                                               cudaStream_t);                                                    \
     template cudaError_t launch_end_keys<S>(const S*, int64_t, const int64_t*, int, uint32_t* const*, \
                                             cudaStream_t);                                       \

@@ -434,18 +434,18 @@ int build_impl(gSuperIntervals* si) {
     // from which the batched path counts short queries (two ranks per query)
     {
         DevBuf flag2;
-        SI_TRY(flag2.reserve(sizeof(int) + 2 * sizeof(double)));
-        double* sums = reinterpret_cast<double*>(flag2.as<char>() + 8);
+        SI_TRY(flag2.reserve(8 + 2 * sizeof(unsigned long long)));
+        unsigned long long* sums = reinterpret_cast<unsigned long long*>(flag2.as<char>() + 8);
         SI_CK(sig::launch_any_inverted<S>(view<S>(si), flag2.as<int>(), st));
         SI_CK(sig::launch_long_depth<S>(si->starts.as<S>(), si->ends.as<S>(), n, si->seg.as<int64_t>(), G,
                                          sig::kLongIntervalSplit, sums, st));
         int f = 0;
-        double h[2] = {0.0, 0.0};
+        unsigned long long h[2] = {0, 0};
         SI_CK(cudaMemcpyAsync(&f, flag2.p, sizeof(int), cudaMemcpyDeviceToHost, st));
         SI_CK(cudaMemcpyAsync(h, sums, sizeof(h), cudaMemcpyDeviceToHost, st));
         SI_CK(cudaStreamSynchronize(st));
         si->inverted = f ? 1 : 0;
-        si->long_depth = h[1] > 0.0 ? h[0] / h[1] : 0.0;
+        si->long_depth = h[1] > 0 ? (double)h[0] / (double)h[1] : 0.0;
     }
     if (si->inverted == 0) {
         const int K = sig::end_key_words<S>(G);

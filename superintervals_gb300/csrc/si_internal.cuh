@@ -207,7 +207,7 @@ cudaError_t launch_end_decode(const uint32_t* const* kw, int64_t n, int64_t n_pa
 // out[0] = total length of intervals at least X long, out[1] = total contig extent (sorted starts)
 template <typename S>
 cudaError_t launch_long_depth(const S* starts, const S* ends, int64_t n, const int64_t* seg, int G, int64_t X,
-                              double* out, cudaStream_t st);
+                              unsigned long long* out, cudaStream_t st);
 
 // ---------------------------------------------------------------- query launchers (si_query.cu)
 struct QueryBatch {
