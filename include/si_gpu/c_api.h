@@ -164,7 +164,7 @@ int getBatchedParamsGpu(const gSuperIntervals* si, int* tile_queries, int* tile_
                         int64_t* long_query_len, int64_t* split_len);
 /* Further tunables of the batched path (no reference counterpart); results never depend on
  * them.  SI_OPT_EMIT_COPY: 1 writes the section of a tile's long candidates that comes from
- * the long-interval list (intervals at least 65536 long) as copied runs between its few
+ * the long-interval list (intervals at least 32768 long) as copied runs between its few
  * misses, 0 (default) checks every candidate.  SI_OPT_EYTZ_DEPTH: levels of the Eytzinger
  * tree (1-13, 0 automatic), resampled at once when it is the current provider.
  * getBatchedOptionGpu reports the depth in use. */

@@ -12,7 +12,7 @@
 //     candidate set C = { k <= max ub : ends[k] >= min qs } holds every hit of every query of
 //     the tile; it is gathered into shared memory, in descending position order, by a
 //     block-wide top-down BFS over the max-of-32 pyramid of ends for the positions near the
-//     tile, and over the pyramid of the long-interval list (intervals at least 65536 long)
+//     tile, and over the pyramid of the long-interval list (intervals at least 32768 long)
 //     for the positions further back.  C is split by interval length: near-start candidates
 //     are filtered per query, long ones are nearly all hits.  The count pass counts (one
 //     query per thread) and records the query's head-run length (the run of consecutive hits
@@ -853,7 +853,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_tiles(TileArgs<S> a) {
                         }
                         __syncthreads();
                         // nlm: long candidates from the tile's own gather (positions >= p_cut).  The
-                        // lnu list: the others (from the long-interval list, at least 65536 long)
+                        // lnu list: the others (from the long-interval list, at least 32768 long)
                         // that end before Q, i.e. possible misses for some query, in long-list order
                         // as their long-list indices (at most kLnu kept; a larger count makes every
                         // query filter them)

@@ -111,7 +111,7 @@ inline int query_code_bits(int G) {
 }
 
 // Interval length from which an interval enters the long-interval list.
-constexpr int64_t kLongIntervalSplit = 65536;
+constexpr int64_t kLongIntervalSplit = 32768;
 
 template <typename S>
 int batched_prepare(BatchedWorkspace& ws, MapView<S> m, Levels<S> L, int H, const int64_t* lvl_sizes,

@@ -167,7 +167,7 @@ struct gSuperIntervals {
     // set operations: hit lists, staged pieces, and whether some interval has start > end
     DevBuf so_hoff, so_hits, so_off, so_os, so_oe, so_ob, so_flag;
     int inverted = -1;  // -1 unknown, else 0 / 1 (reset by every build)
-    // mean number of intervals at least 65536 long over a position (set by every build): hits
+    // mean number of intervals at least 32768 long over a position (set by every build): hits
     // of such intervals lie far apart in position order, so one walk per query is long
     double long_depth = 0.0;
     // contig names, in contig-id order, when the intervals came from BED text
