@@ -45,8 +45,8 @@ PEAK_FALLBACK_GBS = 6800.0
 # DRAM traffic of the emit kernel per unit, from an ncu capture of dram__bytes_write.sum and
 # dram__bytes_read.sum on configuration 3's density (profiles/k_tiles_config3_dram.md): writes
 # scale with result pairs, reads with queries
-EMIT_DRAM_WRITE_PER_PAIR = 3.974
-EMIT_DRAM_READ_PER_QUERY = 183.3
+EMIT_DRAM_WRITE_PER_PAIR = 3.972
+EMIT_DRAM_READ_PER_QUERY = 182.1
 
 
 def parse():
