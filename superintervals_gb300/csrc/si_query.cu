@@ -167,8 +167,8 @@ __device__ __forceinline__ int64_t warp_rank(const S* __restrict__ arr, int64_t 
     return a + __popc(__ballot_sync(kFull, in)) - a0;
 }
 
-// From a miss at p the walk goes on at branch[p] (hpp:551-579): every position between the two
-// ends before ends[p] < qs.  For a 32-position chunk ending at i (lane l is position i - l), the
+// From a miss at p the walk goes on at branch[p] (hpp:551-579): every position strictly between
+// branch[p] and p ends before ends[p] < qs.  For a 32-position chunk ending at i (lane l is position i - l), the
 // next position to look at: below the chunk, and below the branch of every miss in it (each
 // miss's skipped range reaches into the chunk, so together they cover everything from the
 // smallest branch up).  br is the lane's branch entry, loaded beside its end.
